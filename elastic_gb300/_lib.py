@@ -1,0 +1,89 @@
+"""ctypes binding of libelastic_rtm.so (the C-ABI in include/elastic_rtm.h).
+
+There is no fallback: if the shared library is missing or cannot be loaded,
+every call raises.  Build it with ``python -m elastic_gb300.build`` (or
+``__graft_entry__.build()``).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libelastic_rtm.so")
+
+_c_int, _c_float, _c_double = ctypes.c_int, ctypes.c_float, ctypes.c_double
+_P = ctypes.c_void_p
+
+# name -> (restype, argtypes); one line per entry point of include/elastic_rtm.h
+SIGNATURES = {
+    "rtm_last_error": (ctypes.c_char_p, []),
+    "rtm_last_status": (_c_int, []),
+    "rtm_set_exact": (None, [_c_int]),
+    "rtm_op3_c_": (None, [_c_int] * 4 + [_P] * 10),
+    "rtm_gpu_init": (None, [_c_int] * 3),
+    "rtm_gpu_copy_in": (None, [_c_int] * 3 + [_P] * 10),
+    "rtm_gpu_copy_out": (None, [_c_int] * 3 + [_P] * 5),
+    "rtm_gpu_func": (None, [_c_int] * 4 + [_P] * 12),
+    "rtm_gpu_final": (None, []),
+    "rtm_model_op_c_": (_c_int, [_c_int, _c_int, _c_float, _c_float] + [_P] * 8),
+    "rtm_source_c_": (_c_int, [_c_int, _c_float, _c_float, _c_int, _P]),
+    "rtm_abc_c_": (_c_int, [_c_int, _P]),
+    "rtm_fwd_c_": (_c_int, [_c_int, _c_int, _c_int, _c_float, _c_int, _c_int, _c_int] + [_P] * 11),
+    "rtm_image_init_c_": (_c_int, [_c_int, _c_int, _c_int, _c_float, _c_float] + [_P] * 8),
+    "rtm_model_delta_c_": (_c_int, [_c_int, _c_int, _P, _P, _P]),
+    "rtm_image_op_c_": (_c_int, [_c_int] * 4 + [_P] * 14),
+    "rtm_born_scatter_c_": (_c_int, [_c_int] * 5 + [_P] * 15),
+    "rtm_op3_full_c_": (_c_int, [_c_int] * 6 + [_P] * 15),
+    "rtm_op_c_": (_c_int, [_c_int] * 4 + [_c_float, _c_float] + [_c_int] * 3 + [_c_float, _c_int, _c_int]
+                  + [_P] * 11 + [_c_int, _c_int]),
+    "rtm_op_d_": (_c_int, [_c_int] * 4 + [_c_double, _c_double] + [_c_int] * 3 + [_c_double, _c_int, _c_int]
+                  + [_P] * 11 + [_c_int, _c_int]),
+}
+
+_lib = None
+
+
+class RtmError(RuntimeError):
+    pass
+
+
+def load():
+    """Load the CUDA library (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RtmError(f"{LIB_PATH} is missing: build it with elastic_gb300.build.build()")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ptr(a):
+    """Pointer to a C-contiguous numpy array (or a torch tensor's data_ptr)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array must be C-contiguous")
+        return a.ctypes.data_as(ctypes.c_void_p)
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def check(status):
+    """Raise RtmError for a non-zero status of an int-returning entry point."""
+    if status != 0:
+        msg = load().rtm_last_error().decode(errors="replace")
+        raise RtmError(f"status {status}: {msg}")
+    return status
+
+
+def check_void():
+    """Raise RtmError when the last void drop-in call failed."""
+    check(load().rtm_last_status())

@@ -1,0 +1,101 @@
+// Host-side building blocks shared by the 2D elastic entry points.
+#pragma once
+#include <vector>
+
+#include "common.cuh"
+#include "elastic2d.cuh"
+
+#define TRY(x)                   \
+    do {                         \
+        int s_ = (x);            \
+        if (s_) return s_;       \
+    } while (0)
+
+namespace eg {
+
+constexpr int TZ_TILE = 32;  // tile height (one warp along z)
+
+int ensure_device();
+int device_sm_count();
+
+// Owning device allocation that grows on demand.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count)
+    {
+        if (count <= n && p) return RTM_OK;
+        release();
+        if (count == 0) return RTM_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            cudaGetLastError();
+            rtm_set_error("cudaMalloc of %zu bytes failed: %s", count * sizeof(T), cudaGetErrorString(e));
+            return RTM_ERR_NOMEM;
+        }
+        n = count;
+        return RTM_OK;
+    }
+};
+
+// One shot of a batch as the host sees it (0-based cells; -1 = none).
+struct HostShot {
+    long long off;   // element offset of the shot's planes
+    long long doff;  // element offset of the shot's traces
+    int nz, nx;
+    int src_iz, src_ix;
+    int rec_iz;
+};
+
+// Work-item table of a batch for a given tile width (device copy in d_geom).
+struct ShotTable {
+    std::vector<HostShot> shots;
+    int ldz = 0;
+    int tx = 16;
+    int ntiles = 0;
+    ShotGeom *d_geom = nullptr;
+    ShotTable() = default;
+    ShotTable(const ShotTable &) = delete;
+    ShotTable &operator=(const ShotTable &) = delete;
+    ~ShotTable();
+    int build(int tx);
+};
+
+// Tile width giving at least two work items per SM when the grid allows.
+inline int pick_tile_width(long long cells_z, long long cells_x)
+{
+    const long long ntz = (cells_z + TZ_TILE - 1) / TZ_TILE;
+    const long long want = 2LL * device_sm_count();
+    for (int tx : {32, 16}) if (ntz * ((cells_x + tx - 1) / tx) >= want) return tx;
+    return 8;
+}
+
+template <typename T>
+int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st);
+
+template <typename T>
+int model_coefs(int nz, int nx, T dx, T dt, const T *d_rho, const T *d_lam, const T *d_mu, int ldin, T *m1x, T *m1z,
+                T *m2o, T *m3o, T *a2, T *a3, T *a23, int ldout, cudaStream_t st);
+
+template <typename T>
+int mask_coefs(int nz, int nx, const T *const in[5], int ldin, T *const out[5], int ldout, cudaStream_t st);
+
+template <typename T>
+void host_abc_filter(int abc, T *filter);
+
+template <typename T>
+void host_ricker(int nt, T dt, T fp, int nsource, T *source);
+
+}  // namespace eg

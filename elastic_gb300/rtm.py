@@ -1,0 +1,162 @@
+"""Python mirror of the reference's operator interface for the elastic RTM path.
+
+The names, argument meanings and error behaviour follow the Fortran modules
+of lgan/elastic (W = 2d_rtm_restart/Src_working):
+
+* ``rtm_init`` / ``RtmOperator.rtm_op`` -- W/rtm-mod-adj.f90:43-129
+  (``rtm_op`` returns stat 0 on success; failures raise ``RtmError``).
+* ``rtm_op3`` -- the Fortran->C call of W/rtmlib-mod.f90:158 into
+  ``rtm_op3_c_`` (W/rtmlib-modC.c:29), in place on full histories.
+* ``model_op``, ``source_op2``, ``abc_init``, ``image_init``, ``image_op2``,
+  ``model_delta``, ``born_scatter``, ``rtm_op3_full`` -- one per reference
+  routine of the path.
+
+Arrays are numpy, C-ordered views of the Fortran layout: a plane (nz,nx) is
+``a[ix, iz]``, a history (nz,nx,nt) is ``h[it, ix, iz]``, a gather (nt,nx) is
+``d[ix, it]``.  Grid positions are 1-based.  Every computation runs in
+libelastic_rtm.so on the GPU.
+"""
+import numpy as np
+
+from ._lib import check, check_void, load, ptr
+
+F32 = np.float32
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=F32)
+
+
+def set_exact(exact=True):
+    """Exact (reference bit-identical) or fast arithmetic for the drop-in calls."""
+    load().rtm_set_exact(1 if exact else 0)
+
+
+# ----------------------------------------------------------------- a1..a4
+def model_op(rho, lam, mu, dx, dt):
+    """model_op + rtmmod_init + aux_*_c.  Returns (m1_x, m1_z, aux_m2_c,
+    aux_m3_c, aux_m2m3_c, lambda_avg, mu_avg)."""
+    rho, lam, mu = _f32(rho), _f32(lam).copy(), _f32(mu).copy()
+    nx, nz = rho.shape
+    out = [np.zeros_like(rho) for _ in range(5)]
+    check(load().rtm_model_op_c_(nz, nx, dx, dt, ptr(rho), ptr(lam), ptr(mu), *[ptr(o) for o in out]))
+    return (*out, lam, mu)
+
+
+def source_op2(nt, dt, fp, nsource=250):
+    s = np.zeros(nt, F32)
+    check(load().rtm_source_c_(nt, dt, fp, nsource, ptr(s)))
+    return s
+
+
+def abc_init(abc):
+    f = np.zeros(abc + 5, F32)
+    check(load().rtm_abc_c_(abc, ptr(f)))
+    return f
+
+
+# ----------------------------------------------------------------- a6..a13
+def forward(coefs, nt, dt, xsrc, zsrc, abc, source):
+    """Source wavefield histories (Vx0, Vz0, sxx0, szz0, sxz0)."""
+    coefs = [_f32(c) for c in coefs]
+    nx, nz = coefs[0].shape
+    H = [np.zeros((nt, nx, nz), F32) for _ in range(5)]
+    check(load().rtm_fwd_c_(nt, nz, nx, dt, xsrc, zsrc, abc, ptr(_f32(source)), *[ptr(c) for c in coefs],
+                            *[ptr(h) for h in H]))
+    return H
+
+
+def image_init(Vx0, Vz0, dx, dt):
+    Vx0, Vz0 = _f32(Vx0), _f32(Vz0)
+    nt, nx, nz = Vx0.shape
+    S = [np.zeros_like(Vx0) for _ in range(6)]
+    check(load().rtm_image_init_c_(nt, nz, nx, dx, dt, ptr(Vx0), ptr(Vz0), *[ptr(s) for s in S]))
+    return S
+
+
+def model_delta(drho, dlambda, dmu):
+    dl, dm = _f32(dlambda).copy(), _f32(dmu).copy()
+    nx, nz = dl.shape
+    check(load().rtm_model_delta_c_(nz, nx, ptr(_f32(drho)), ptr(dl), ptr(dm)))
+    return dl, dm
+
+
+def image_op2(adj, S, images=None, H=None):
+    """adj=True: histories H -> images (drho, dlambda, dmu);
+    adj=False: images -> five secondary-source histories."""
+    S = [_f32(s) for s in S]
+    nt, nx, nz = S[0].shape
+    if adj:
+        H = [_f32(h) for h in H]
+        img = [np.zeros((nx, nz), F32) for _ in range(3)]
+    else:
+        img = [_f32(i).copy() for i in images]
+        H = [np.zeros((nt, nx, nz), F32) for _ in range(5)]
+    check(load().rtm_image_op_c_(1 if adj else 0, nt, nz, nx, *[ptr(i) for i in img], *[ptr(h) for h in H],
+                                 *[ptr(s) for s in S]))
+    return img if adj else H
+
+
+def born_scatter(H, coefs, zrec, abc):
+    """Scattered propagation in place on H; returns five gathers [nx, nt]."""
+    H = [np.ascontiguousarray(h, F32) for h in H]
+    nt, nx, nz = H[0].shape
+    D = [np.zeros((nx, nt), F32) for _ in range(5)]
+    check(load().rtm_born_scatter_c_(nt, nz, nx, zrec, abc, *[ptr(_f32(c)) for c in coefs], *[ptr(h) for h in H],
+                                     *[ptr(d) for d in D]))
+    return H, D
+
+
+def rtm_op3_full(D, coefs, nz, zrec, abc=0, exact_adjoint=False):
+    """rtm_op3: five gathers [nx, nt] -> five adjoint histories."""
+    D = [_f32(d) for d in D]
+    nx, nt = D[0].shape
+    H = [np.zeros((nt, nx, nz), F32) for _ in range(5)]
+    check(load().rtm_op3_full_c_(nt, nz, nx, zrec, abc, 1 if exact_adjoint else 0, *[ptr(d) for d in D],
+                                 *[ptr(_f32(c)) for c in coefs], *[ptr(h) for h in H]))
+    return H
+
+
+def rtm_op3(nt, nz, nx, zrec, Vx0, Vz0, sigmaxx0, sigmazz0, sigmaxz0, m1_x, m1_z, aux_m2_c, aux_m3_c, aux_m2m3_c):
+    """Drop-in rtm_op3_c_: adjoint recursion in place on the five histories."""
+    arrs = [Vx0, Vz0, sigmaxx0, sigmazz0, sigmaxz0, m1_x, m1_z, aux_m2_c, aux_m3_c, aux_m2m3_c]
+    for a in arrs:
+        if a.dtype != F32 or not a.flags["C_CONTIGUOUS"]:
+            raise TypeError("rtm_op3 works in place on C-contiguous float32 arrays")
+    load().rtm_op3_c_(nt, nz, nx, zrec, *[ptr(a) for a in arrs])
+    check_void()
+
+
+# ----------------------------------------------------------------- rtm_op
+class RtmOperator:
+    """rtm_init + rtm_op of W/rtm-mod-adj.f90 for the Lame parameterisation.
+
+    ``rtm_op(adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz)``
+    follows the reference: adj=True migrates the five gathers into the three
+    images (overwritten in place); adj=False Born-models the images into the
+    gathers (dlambda/dmu are averaged in place by model_delta unless
+    linear=True).  Returns stat 0.
+    """
+
+    def __init__(self, nz, dz, nx, dx, dt, xsource, zsource, zrec, fp, nt, abc, rho, lam, mu, nsource=250,
+                 dtype=F32, linear=False, exact_adjoint=False):
+        self.nz, self.nx, self.nt = nz, nx, nt
+        self.dz, self.dx, self.dt = dz, dx, dt
+        self.xsource, self.zsource, self.zrec = xsource, zsource, zrec
+        self.fp, self.abc, self.nsource = fp, abc, nsource
+        self.dtype = np.dtype(dtype)
+        self.rho = np.ascontiguousarray(rho, self.dtype)
+        self.lam = np.ascontiguousarray(lam, self.dtype)
+        self.mu = np.ascontiguousarray(mu, self.dtype)
+        self.linear, self.exact_adjoint = linear, exact_adjoint
+
+    def rtm_op(self, adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz):
+        arrs = [drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz]
+        for a in arrs:
+            if a.dtype != self.dtype or not a.flags["C_CONTIGUOUS"]:
+                raise TypeError(f"rtm_op works in place on C-contiguous {self.dtype} arrays")
+        fn = load().rtm_op_d_ if self.dtype == np.float64 else load().rtm_op_c_
+        check(fn(1 if adj else 0, self.nz, self.nx, self.nt, self.dx, self.dt, self.xsource, self.zsource,
+                 self.zrec, self.fp, self.nsource, self.abc, ptr(self.rho), ptr(self.lam), ptr(self.mu),
+                 *[ptr(a) for a in arrs], 1 if self.linear else 0, 1 if self.exact_adjoint else 0))
+        return 0

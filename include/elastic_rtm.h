@@ -1,0 +1,144 @@
+/*
+ * elastic_rtm.h -- C-ABI of libelastic_rtm.so, the GB300 (sm_103a) engine for
+ * the 2D elastic RTM / Born hot path of lgan/elastic and its single-domain 3D
+ * acoustic propagator.
+ *
+ * Conventions (all entry points):
+ *  - Arrays are plain pointers in the reference's Fortran layout:
+ *    planes (nz,nx) column-major, z fastest; wavefield histories (nz,nx,nt);
+ *    receiver gathers (nt,nx), one per component.
+ *  - Grid positions (xsrc, zsrc, zrec) are 1-based, as in the Fortran.
+ *  - Pointers are host memory unless the name ends in _dev.
+ *  - int-returning functions return 0 on success or an RtmStatus code
+ *    (1 bad argument, 2 out of memory, 3 CUDA error, 4 device wait timed
+ *    out, 5 bad call order); rtm_last_error() gives the message.
+ *  - The library uses CUDA device 0 unless ELASTIC_RTM_DEVICE names another.
+ *    Every entry point is synchronous with respect to the host.
+ *  - "exact" arithmetic reproduces the reference's CPU code bit for bit
+ *    (every product and sum separately rounded, in the reference's order);
+ *    "fast" arithmetic may fuse multiply-adds and reassociate the adjoint
+ *    stencil (results agree to ~1e-6 relative L2).
+ *
+ * Reference paths below are inside the lgan/elastic project, with
+ * W = 2d_rtm_restart/Src_working.
+ */
+#ifndef ELASTIC_RTM_H
+#define ELASTIC_RTM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+const char *rtm_last_error(void);
+/* Status of the last void drop-in call (rtm_op3_c_, rtm_gpu_*). */
+int rtm_last_status(void);
+/* Select exact (1, default) or fast (0) arithmetic for the drop-in calls. */
+void rtm_set_exact(int exact);
+
+/* ------------------------------------------------- drop-in replacements */
+/* Adjoint recursion for levels nt-3 .. 0 (0-based) on full histories, in
+ * place.  Replaces rtm_op3_c_ of W/rtmlib-modC.c:29-313 as bound by
+ * W/rtmlib-modF.f90:27-52 (bind(c, name='rtm_op3_c_'), value scalars).
+ * Coefficients are the unmasked (nz,nx) planes already scaled by dt/dx; the
+ * reference's masks (W/rtmlib-modC.c:83-93) are applied on the device.
+ * zrec is unused, as in the reference.  Errors: rtm_last_status(). */
+void rtm_op3_c_(int nt, int nz, int nx, int zrec, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
+                float *sigmaxz0, float *m1_x, float *m1_z, float *aux_m2_c, float *aux_m3_c, float *aux_m2m3_c);
+
+/* The reference's internal C<->CUDA layer (W/rtmlib-modC-gpu.cu:35,77,100,
+ * 115,425), same arguments and padded layout: arrays (nz+10,nx+10[,nt+10])
+ * with a 5-cell offset on every axis (W/gpu.h:9,13), masked coefficients.
+ * rtm_gpu_func runs levels it_max .. 0, copying in and out itself, and
+ * stores the device time per step (seconds) in gpu_kernel_time_ps[0];
+ * `debug` is ignored. */
+void rtm_gpu_init(int nt, int nz, int nx);
+void rtm_gpu_copy_in(int nt, int nz, int nx, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
+                     float *sigmaxz0, float *ex_m1_x, float *ex_m1_z, float *ex_aux_m2_c, float *ex_aux_m3_c,
+                     float *ex_aux_m2m3_c);
+void rtm_gpu_copy_out(int nt, int nz, int nx, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
+                      float *sigmaxz0);
+void rtm_gpu_func(int it_max, int nt, int nz, int nx, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
+                  float *sigmaxz0, float *ex_m1_x, float *ex_m1_z, float *ex_aux_m2_c, float *ex_aux_m3_c,
+                  float *ex_aux_m2m3_c, float *debug, double *gpu_kernel_time_ps);
+void rtm_gpu_final(void);
+
+/* ------------------------------------------- siblings (one per reference
+ * routine of the path; the Fortran calls them through bind(c) in the same
+ * style as rtm_op3_c_) */
+
+/* model_op + rtmmod_init + aux_*_c (W/model-mod.f90:21-89,
+ * W/rtmlib-mod.f90:23-65, W/rtm-mod-adj.f90:99-113).  lambda and mu are
+ * replaced in place by their staggered harmonic averages, as in the
+ * reference.  Outputs m1_x, m1_z (scaled by dt/dx) and aux_m2_c, aux_m3_c,
+ * aux_m2m3_c. */
+int rtm_model_op_c_(int nz, int nx, float dx, float dt, const float *rho, float *lambda, float *mu, float *m1_x,
+                    float *m1_z, float *aux_m2_c, float *aux_m3_c, float *aux_m2m3_c);
+
+/* Ricker wavelet (W/source-mod.f90:31-44): source[nt]. */
+int rtm_source_c_(int nt, float dt, float fp, int nsource, float *source);
+
+/* Sponge filter table (W/abc-mod.f90:20-57): filter[abc+5].  abc=0 (which
+ * reads out of bounds in the reference) gives an all-ones table. */
+int rtm_abc_c_(int abc, float *filter);
+
+/* Forward source wavefield history (W/rtm-mod-adj.f90:178-261): five
+ * (nz,nx,nt) outputs.  Coefficients as returned by rtm_model_op_c_. */
+int rtm_fwd_c_(int nt, int nz, int nx, float dt, int xsrc, int zsrc, int abc, const float *source,
+               const float *m1_x, const float *m1_z, const float *aux_m2_c, const float *aux_m3_c,
+               const float *aux_m2m3_c, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0, float *sigmaxz0);
+
+/* image_init (W/image-mod-rtm.f90:26-67): S1..S6 histories from Vx0, Vz0. */
+int rtm_image_init_c_(int nt, int nz, int nx, float dx, float dt, const float *Vx0, const float *Vz0, float *S1,
+                      float *S2, float *S3, float *S4, float *S5, float *S6);
+
+/* model_delta (W/model-mod.f90:91-171): dlambda, dmu averaged in place. */
+int rtm_model_delta_c_(int nz, int nx, const float *drho, float *dlambda, float *dmu);
+
+/* image_op2, Lame parameterisation (W/image-mod-rtm.f90:145-180).
+ * adj=1: images (drho,dlambda,dmu) = imaging sums over the five histories;
+ * adj=0: the five histories = Born secondary sources of the images. */
+int rtm_image_op_c_(int adj, int nt, int nz, int nx, float *drho, float *dlambda, float *dmu, float *Vx0,
+                    float *Vz0, float *sigmaxx0, float *sigmazz0, float *sigmaxz0, const float *S1, const float *S2,
+                    const float *S3, const float *S4, const float *S5, const float *S6);
+
+/* Born scattered propagation with the secondary sources already in the five
+ * histories (W/rtm-mod-adj.f90:291-357), in place, then receiver sampling
+ * of all five components at row zrec into (nt,nx) gathers (:361-375). */
+int rtm_born_scatter_c_(int nt, int nz, int nx, int zrec, int abc, const float *m1_x, const float *m1_z,
+                        const float *aux_m2_c, const float *aux_m3_c, const float *aux_m2m3_c, float *Vx0,
+                        float *Vz0, float *sigmaxx0, float *sigmazz0, float *sigmaxz0, float *Vx, float *Vz,
+                        float *sigmaxx, float *sigmazz, float *sigmaxz);
+
+/* rtm_op3 (W/rtmlib-mod.f90:72-196): the five (nt,nx) receiver gathers are
+ * written at row zrec and propagated backwards; outputs the five adjoint
+ * histories.  exact_adjoint=1 applies the sponge to every adjoint level
+ * (the transpose of the sponged Born operator); 0 is the reference. */
+int rtm_op3_full_c_(int nt, int nz, int nx, int zrec, int abc, int exact_adjoint, const float *Vx,
+                    const float *Vz, const float *sigmaxx, const float *sigmazz, const float *sigmaxz,
+                    const float *m1_x, const float *m1_z, const float *aux_m2_c, const float *aux_m3_c,
+                    const float *aux_m2m3_c, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
+                    float *sigmaxz0);
+
+/* Whole rtm_op (W/rtm-mod-adj.f90:120-496, lame=.true.) for one shot, on
+ * the raw model (rho, lambda, mu).  adj=1 (RTM): gathers in -> images
+ * (drho, dlambda, dmu) out.  adj=0 (Born): images in -> gathers out; with
+ * linear=0 dlambda and dmu are averaged in place by model_delta as in the
+ * reference, linear=1 skips model_delta (the linear Born operator whose
+ * transpose is adj=1 with exact_adjoint=1).  Full histories are kept on the
+ * device (11 volumes of nz*nx*nt floats at most). */
+int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,
+              int nsource, int abc, const float *rho, const float *lambda, const float *mu, float *drho,
+              float *dlambda, float *dmu, float *Vx, float *Vz, float *sigmaxx, float *sigmazz, float *sigmaxz,
+              int linear, int exact_adjoint);
+/* Double-precision twin of rtm_op_c_ (used for the FP64 oracle comparison
+ * and the adjoint dot-product test). */
+int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, int zsrc, int zrec, double fp,
+              int nsource, int abc, const double *rho, const double *lambda, const double *mu, double *drho,
+              double *dlambda, double *dmu, double *Vx, double *Vz, double *sigmaxx, double *sigmazz,
+              double *sigmaxz, int linear, int exact_adjoint);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ELASTIC_RTM_H */

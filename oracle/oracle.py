@@ -1,0 +1,260 @@
+"""ctypes front end for the C oracle (test infrastructure only).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, as the checker.  The product never imports it.
+
+Array conventions mirror the Fortran memory layout with C-ordered numpy
+arrays: a wavefield history (nz,nx,nt) column-major is ``H[it, ix, iz]``; a
+model plane (nz,nx) is ``M[ix, iz]``; receiver data (nt,nx) is ``D[ix, it]``.
+Grid indices passed to the C functions (zsrc, xsrc, zrec) are 1-based as in
+the Fortran.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "librefc.so")
+REF_ROOT = "/root/reference"
+
+_lib = None
+_ref = None
+
+
+def build(ref=False):
+    """Compile liboracle.so (and, when the reference tree exists, _ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    if ref and os.path.isdir(REF_ROOT):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFROOT=" + REF_ROOT], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        _lib = ctypes.CDLL(LIB_PATH)
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_PATH) or os.path.isdir(REF_ROOT)
+
+
+def ref():
+    """The reference's own rtmlib-modC.c compiled CPU-only (see Makefile)."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            build(ref=True)
+        _ref = ctypes.CDLL(REF_PATH)
+    return _ref
+
+
+def _p(a):
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _sfx(dtype):
+    return "_d" if np.dtype(dtype) == np.float64 else "_f"
+
+
+def _R(dtype):
+    return ctypes.c_double if np.dtype(dtype) == np.float64 else ctypes.c_float
+
+
+# ------------------------------------------------------------------ a1..a4
+def model_op(rho, lam, mu):
+    """model_op: returns (m1_x, m1_z, lambda_avg, mu_avg)."""
+    dt = rho.dtype
+    nx, nz = rho.shape
+    m2, m3 = lam.copy(), mu.copy()
+    m1x, m1z = np.zeros_like(rho), np.zeros_like(rho)
+    getattr(lib(), "ora_model_op" + _sfx(dt))(nz, nx, _p(rho), _p(m2), _p(m3), _p(m1x), _p(m1z))
+    return m1x, m1z, m2, m3
+
+
+def rtmmod_init(m1x, m1z, m2, m3, dx, dt):
+    """Scale m1_x, m1_z by dt/dx; return (m1_x, m1_z, aux_m2, aux_m3, aux_m2m3)."""
+    d = m1x.dtype
+    nx, nz = m1x.shape
+    m1x, m1z = m1x.copy(), m1z.copy()
+    a2, a3, a23 = (np.zeros_like(m1x) for _ in range(3))
+    R = _R(d)
+    getattr(lib(), "ora_rtmmod_init" + _sfx(d))(nz, nx, R(dx), R(dt), _p(m1x), _p(m1z), _p(m2), _p(m3),
+                                                _p(a2), _p(a3), _p(a23))
+    return m1x, m1z, a2, a3, a23
+
+
+def coefficients(rho, lam, mu, dx, dt):
+    """model_op + rtmmod_init: the five scaled coefficient planes."""
+    m1x, m1z, m2, m3 = model_op(rho, lam, mu)
+    return rtmmod_init(m1x, m1z, m2, m3, dx, dt)
+
+
+def source_op2(nt, dt, fp, nsource=250, dtype=np.float32):
+    s = np.zeros(nt, dtype)
+    R = _R(dtype)
+    getattr(lib(), "ora_source_op2" + _sfx(dtype))(nt, R(dt), R(fp), nsource, _p(s))
+    return s
+
+
+def abc_init(abc, dtype=np.float32):
+    f = np.zeros(abc + 5, dtype)
+    getattr(lib(), "ora_abc_init" + _sfx(dtype))(abc, _p(f))
+    return f
+
+
+def K(data, abc, filt):
+    d = data.copy()
+    nx, nz = d.shape
+    getattr(lib(), "ora_K" + _sfx(d.dtype))(nz, nx, abc, _p(filt), _p(d))
+    return d
+
+
+# ------------------------------------------------------------------ a6..a13
+def forward(coefs, nt, dt, zsrc, xsrc, source, abc, filt):
+    """Source wavefield history: returns (Vx, Vz, sxx, szz, sxz), each [nt,nx,nz]."""
+    m1x = coefs[0]
+    d = m1x.dtype
+    nx, nz = m1x.shape
+    H = [np.zeros((nt, nx, nz), d) for _ in range(5)]
+    getattr(lib(), "ora_forward" + _sfx(d))(nz, nx, nt, _R(d)(dt), zsrc, xsrc, _p(source), abc, _p(filt),
+                                            *[_p(c) for c in coefs], *[_p(h) for h in H])
+    return H
+
+
+def image_init(Vx, Vz, dx, dt):
+    d = Vx.dtype
+    nt, nx, nz = Vx.shape
+    S = [np.zeros_like(Vx) for _ in range(6)]
+    R = _R(d)
+    getattr(lib(), "ora_image_init" + _sfx(d))(nz, nx, nt, R(dx), R(dt), _p(Vx), _p(Vz), *[_p(s) for s in S])
+    return S
+
+
+def model_delta(dm1, dm2, dm3):
+    d = dm1.dtype
+    nx, nz = dm1.shape
+    dm2, dm3 = dm2.copy(), dm3.copy()
+    t1, t2 = np.zeros_like(dm1), np.zeros_like(dm1)
+    getattr(lib(), "ora_model_delta" + _sfx(d))(nz, nx, _p(dm1), _p(t1), _p(t2), _p(dm2), _p(dm3))
+    return dm2, dm3
+
+
+def image_adj(H, S):
+    """Imaging condition: returns (dm1, dm2, dm3) from adjoint history H and S1..S6."""
+    d = H[0].dtype
+    nt, nx, nz = H[0].shape
+    dm = [np.zeros((nx, nz), d) for _ in range(3)]
+    H = [h.copy() for h in H]
+    getattr(lib(), "ora_image_op2" + _sfx(d))(nz, nx, nt, 1, 0, *[_p(x) for x in dm], *[_p(h) for h in H],
+                                              *[_p(s) for s in S])
+    return dm
+
+
+def image_fwd(dm1, dm2, dm3, S):
+    """Born secondary sources: returns 5 histories."""
+    d = dm1.dtype
+    nt, nx, nz = S[0].shape
+    H = [np.zeros((nt, nx, nz), d) for _ in range(5)]
+    getattr(lib(), "ora_image_op2" + _sfx(d))(nz, nx, nt, 0, 0, _p(dm1), _p(dm2), _p(dm3), *[_p(h) for h in H],
+                                              *[_p(s) for s in S])
+    return H
+
+
+def born_scatter(H, coefs, zrec, abc, filt):
+    """Scattered propagation in place on H (5 histories); returns 5 gathers [nx,nt]."""
+    d = H[0].dtype
+    nt, nx, nz = H[0].shape
+    D = [np.zeros((nx, nt), d) for _ in range(5)]
+    getattr(lib(), "ora_born_scatter" + _sfx(d))(nz, nx, nt, zrec, abc, _p(filt), *[_p(c) for c in coefs],
+                                                 *[_p(h) for h in H], *[_p(x) for x in D])
+    return D
+
+
+def rtm_op3_c(H, coefs):
+    """The C gather recursion (restated) in place on 5 histories."""
+    d = H[0].dtype
+    nt, nx, nz = H[0].shape
+    getattr(lib(), "ora_rtm_op3_c" + _sfx(d))(nt, nz, nx, *[_p(h) for h in H], *[_p(c) for c in coefs])
+    return H
+
+
+def rtm_op3(D, coefs, nz, zrec, exact=False, abc=0, filt=None):
+    """rtm_op3: receivers D (5 gathers [nx,nt]) -> 5 adjoint histories."""
+    d = D[0].dtype
+    nx, nt = D[0].shape
+    H = [np.zeros((nt, nx, nz), d) for _ in range(5)]
+    if filt is None:
+        filt = abc_init(abc, d)
+    getattr(lib(), "ora_rtm_op3" + _sfx(d))(nt, nz, nx, zrec, *[_p(h) for h in H], *[_p(x) for x in D],
+                                            *[_p(c) for c in coefs], int(exact), abc, _p(filt))
+    return H
+
+
+def rtm_op2(adj, rho, lam, mu, dm, D, dx, dt, nt, zsrc, xsrc, zrec, fp, abc, nsource=250, exact=False):
+    """Whole rtm_op2.  adj=True: D (5 gathers [nx,nt]) -> image (dm1,dm2,dm3).
+    adj=False: dm (3 planes) -> 5 gathers.  Returns (dm, D) after the call."""
+    d = rho.dtype
+    nx, nz = rho.shape
+    R = _R(d)
+    dm = [x.copy() for x in dm]
+    D = [x.copy() for x in D]
+    getattr(lib(), "ora_rtm_op2" + _sfx(d))(int(adj), nz, nx, nt, R(dx), R(dt), zsrc, xsrc, zrec, R(fp), nsource,
+                                            abc, _p(rho), _p(lam), _p(mu), *[_p(x) for x in dm],
+                                            *[_p(x) for x in D], int(exact))
+    return dm, D
+
+
+# ------------------------------------------------------------------ reference C
+def ref_rtm_op3_c(H, coefs, zrec=1):
+    """Run the reference's own rtm_op3_c_ (CPU-only build) in place on float32 histories."""
+    r = ref()
+    nt, nx, nz = H[0].shape
+    f = r.rtm_op3_c_
+    f.restype = None
+    f(ctypes.c_int(nt), ctypes.c_int(nz), ctypes.c_int(nx), ctypes.c_int(zrec), *[_p(h) for h in H],
+      *[_p(c) for c in coefs])
+    return H
+
+
+# ------------------------------------------------------------------ 3D acoustic
+def acoustic_coeffs(d1, d2, d3):
+    c = np.zeros(16, np.float32)
+    lib().ora3d_coeffs(ctypes.c_double(d1), ctypes.c_double(d2), ctypes.c_double(d3), _p(c))
+    return c
+
+
+def acoustic_damp_table(a, b):
+    t = np.zeros(max(a, 1), np.float32)
+    if a > 0:
+        lib().ora3d_damp_table(a, ctypes.c_float(b), _p(t))
+    return t
+
+
+def acoustic_forward(vel2, coef, damp_a, table, src_pos, wavelet, zr, record=True):
+    """vel2 [n3,n2,n1] (v^2 dt^2).  Returns (d [nt,n3,n2] or None, p0, p1)."""
+    n3, n2, n1 = vel2.shape
+    nt = wavelet.shape[0]
+    p0 = np.zeros_like(vel2)
+    p1 = np.zeros_like(vel2)
+    d = np.zeros((nt, n3, n2), np.float32) if record else None
+    zs, xs, ys = src_pos
+    lib().ora3d_forward(n1, n2, n3, nt, _p(vel2), _p(coef), damp_a, _p(table), zs, xs, ys, _p(wavelet),
+                        ctypes.c_float(1.0), zr, _p(d) if record else None, _p(p0), _p(p1))
+    return d, p0, p1
+
+
+def acoustic_rtm(vel2, coef, damp_a, table, src_pos, wavelet, zr, d, jt):
+    n3, n2, n1 = vel2.shape
+    nt = wavelet.shape[0]
+    img = np.zeros_like(vel2)
+    zs, xs, ys = src_pos
+    lib().ora3d_rtm(n1, n2, n3, nt, jt, _p(vel2), _p(coef), damp_a, _p(table), zs, xs, ys, _p(wavelet), zr,
+                    _p(np.ascontiguousarray(d)), _p(img))
+    return img

@@ -1,0 +1,134 @@
+"""CPU tests of the oracle: pinned against the reference's own C code (when the
+reference tree is present), against the committed golden vectors, and by
+transposition / dot-product identities."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = os.path.join(HERE, "golden", "rtm_op3_c_ref.npz")
+
+
+def test_stagger_coefficients_single_precision():
+    # W/rtmlib-mod.f90:15 divides in single precision; the C code
+    # (W/rtmlib-modC.c:45) rounds the double quotient.  Both agree.
+    for a, b in [(35.0, 294912.0), (-405.0, 229376.0), (567.0, 40960.0), (-735.0, 8192.0), (19845.0, 16384.0)]:
+        assert np.float32(a) / np.float32(b) == np.float32(a / b)
+
+
+def test_oracle_matches_golden_vectors():
+    g = np.load(GOLD)
+    coefs = list(g["coefs"])
+    H = [h.copy() for h in g["hin"]]
+    O.rtm_op3_c(H, coefs)
+    for a, b in zip(H, g["hout"]):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference tree not present")
+@pytest.mark.parametrize("nz,nx,nt", [(37, 45, 64), (11, 13, 59), (40, 24, 70)])
+def test_oracle_rtm_op3_c_bit_exact_vs_reference(nz, nx, nt):
+    rng = np.random.default_rng(nz * 1000 + nx)
+    coefs = [(0.05 * rng.standard_normal((nx, nz))).astype(np.float32) for _ in range(5)]
+    H = [rng.standard_normal((nt, nx, nz)).astype(np.float32) for _ in range(5)]
+    H1 = [h.copy() for h in H]
+    H2 = [h.copy() for h in H]
+    O.ref_rtm_op3_c(H1, coefs)
+    O.rtm_op3_c(H2, coefs)
+    for a, b in zip(H1, H2):
+        np.testing.assert_array_equal(a, b)
+
+
+def _fwd_single_level(x, coefs):
+    """One forward update A x (no sponge, no source, zero older level) via
+    the oracle's forward operators: returns level 3 of a 3-level history."""
+    nx, nz = x[0].shape
+    # oracle.forward needs a source; emulate A by running the Born scattered
+    # update with level 1 = 0, level 2 = x and no sponge: level 3 = x(1)=0 + A x
+    H = [np.zeros((3, nx, nz), x[0].dtype) for _ in range(5)]
+    for f in range(5):
+        H[f][1] = x[f]
+    filt = np.ones(5, x[0].dtype)  # abc=0: all-ones sponge
+    O.born_scatter(H, coefs, 1, 0, filt)
+    # born_scatter adds: level2 = x + A(level1=0) = x; level3 = 0 + level1 + A x
+    return [H[f][2] for f in range(5)]
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference tree not present")
+def test_forward_operators_are_transposes_of_reference_gather():
+    """Pins the restated forward stencils Ax..J (Fortran, not compilable here)
+    through the reference's own C adjoint: <A x, y> = <x, G y>."""
+    rng = np.random.default_rng(7)
+    nz, nx, nt = 30, 34, 59
+    coefs = [(0.1 + 0.1 * rng.random((nx, nz))).astype(np.float32) for _ in range(5)]
+    # the C gather uses masked coefficients internally; the forward ops use
+    # the same planes inside their loop ranges
+    x = [rng.standard_normal((nx, nz)).astype(np.float32) for _ in range(5)]
+    y = [rng.standard_normal((nx, nz)).astype(np.float32) for _ in range(5)]
+    Ax = _fwd_single_level(x, coefs)
+    # G y: reference C on a history whose only non-zero level is nt-2 (0-based),
+    # so level nt-3 becomes in(nt-3)=0 + in(nt-1)=0 + G(level nt-2 = y)
+    H = [np.zeros((nt, nx, nz), np.float32) for _ in range(5)]
+    for f in range(5):
+        H[f][nt - 2] = y[f]
+    O.ref_rtm_op3_c(H, coefs)
+    Gy = [H[f][nt - 3] for f in range(5)]
+    lhs = sum(float(np.dot(a.ravel().astype(np.float64), b.ravel().astype(np.float64))) for a, b in zip(Ax, y))
+    rhs = sum(float(np.dot(a.ravel().astype(np.float64), b.ravel().astype(np.float64))) for a, b in zip(x, Gy))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), abs(rhs))
+
+
+def _tiny_model(nz, nx, dtype):
+    vp = np.full((nx, nz), 2000.0)
+    vp[:, nz // 2:] = 2800.0
+    vs = vp / 1.73
+    rho = 310.0 * vp ** 0.25
+    lam = rho * (vp ** 2 - 2 * vs ** 2)
+    mu = rho * vs ** 2
+    return rho.astype(dtype), lam.astype(dtype), mu.astype(dtype)
+
+
+def test_fp64_dot_product_linear_born():
+    """<L m, d> = <m, L^T d> for the linear Born operator and the exact
+    (sponged) adjoint, in the FP64 oracle."""
+    nz, nx, nt = 40, 44, 90
+    rho, lam, mu = _tiny_model(nz, nx, np.float64)
+    rng = np.random.default_rng(3)
+    m = [rng.standard_normal((nx, nz)) for _ in range(3)]
+    d = [rng.standard_normal((nx, nt)) for _ in range(5)]
+    kw = dict(dx=10.0, dt=1e-3, nt=nt, zsrc=12, xsrc=22, zrec=8, fp=40.0, abc=12, nsource=40, exact=True)
+    zeros_d = [np.zeros((nx, nt)) for _ in range(5)]
+    _, Lm = O.rtm_op2(False, rho, lam, mu, m, zeros_d, **kw)
+    Ltd, _ = O.rtm_op2(True, rho, lam, mu, [np.zeros((nx, nz))] * 3, d, **kw)
+    lhs = sum(float(np.vdot(a, b)) for a, b in zip(Lm, d))
+    rhs = sum(float(np.vdot(a, b)) for a, b in zip(m, Ltd))
+    assert abs(lhs) > 0
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)
+
+
+def test_reference_adjoint_is_not_transpose_with_sponge():
+    """The reference RTM omits the sponge in the adjoint; with abc>0 the
+    dot-product test therefore fails for the reference pair (documented)."""
+    nz, nx, nt = 40, 44, 90
+    rho, lam, mu = _tiny_model(nz, nx, np.float64)
+    rng = np.random.default_rng(4)
+    m = [rng.standard_normal((nx, nz)) for _ in range(3)]
+    d = [rng.standard_normal((nx, nt)) for _ in range(5)]
+    kw = dict(dx=10.0, dt=1e-3, nt=nt, zsrc=12, xsrc=22, zrec=8, fp=40.0, abc=12, nsource=40)
+    _, Lm = O.rtm_op2(False, rho, lam, mu, m, [np.zeros((nx, nt))] * 5, exact=True, **kw)
+    Ltd, _ = O.rtm_op2(True, rho, lam, mu, [np.zeros((nx, nz))] * 3, d, exact=False, **kw)
+    lhs = sum(float(np.vdot(a, b)) for a, b in zip(Lm, d))
+    rhs = sum(float(np.vdot(a, b)) for a, b in zip(m, Ltd))
+    assert abs(lhs - rhs) > 1e-6 * abs(lhs)
+
+
+def test_ricker_and_filter_tables():
+    s = O.source_op2(400, 1e-3, 15.0, 250)
+    assert np.all(s[:24] == 0) and s[24] != 0          # first non-zero sample nsource/10
+    assert np.argmax(s) == 124                           # peak at nsource/2 (1-based 125)
+    f = O.abc_init(40)
+    assert f.shape == (45,) and np.all(np.diff(f[:40]) < 0) and np.all(f[40:] == f[39])
+    np.testing.assert_allclose(f[39], np.exp(-0.09), rtol=1e-6)
