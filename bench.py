@@ -1,0 +1,355 @@
+"""Benchmark: batched multi-shot 2D elastic RTM (the reference's RTM path,
+W/rtm-mod-adj.f90:132-496, run for a survey of shots) on GB300.
+
+Workload (BASELINE configuration 2): full grid nx=2000 x nz=800, dx=5 m,
+dt=0.5 ms, nt=6000, 40-cell sponge, 15 Hz Ricker; seeded smooth random Vp
+1800-4000 m/s (Gaussian filter, 200 m correlation), Vs=Vp/1.73, Gardner
+density; 64 shots 75 m apart, each on its own subgrid 600-2000 cells wide;
+receivers at every subgrid column at z=50 m recording Vx and Vz.  Seeded
+synthetic traces stand in for field data (content does not change the cost).
+
+One step = one group of shots (group_max shots) migrated end to end:
+forward propagation with FP16 source snapshots, adjoint propagation with the
+fused imaging condition, stacking.  The default --steps 16 covers the 64-shot
+survey once.  Metric: Gcell-updates/s counting the forward and the adjoint
+propagation (2 x nz x width x nt per shot); shots/s is reported beside it.
+
+--impl reference times the reference's CPU path (the C restatement of the
+Fortran/C in oracle/, or oracle/_ref where the reference compiled) on the host
+cores: one shot per core on the same grid over a truncated time window.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(nz=800, nx=2000, dx=5.0, dt=5e-4, nt=6000, abc=40, fp=15.0, nsource=250, nshots=64, spacing=15,
+           wmin=600, wmax=2000, zsrc=10, zrec=10, comp_mask=3, seed=2)
+BYTES_FWD = 80     # algorithmic bytes per forward cell-update
+BYTES_ADJ = 112    # per adjoint cell-update with the imaging condition
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per cell-update of the adjoint kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "step2d_adjoint_imaging_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_cell")
+    return None
+
+
+def build_survey():
+    from elastic_gb300 import synth
+    c = CFG
+    vp = synth.smooth_random_model(c["nz"], c["nx"], c["dx"], 200.0, 1800.0, 4000.0, seed=c["seed"])
+    rho, lam, mu = synth.lame_from_vp(vp)
+    x0, nxs, xsrc = synth.uneven_survey(c["nx"], c["nshots"], c["spacing"], c["wmin"], c["wmax"], seed=c["seed"])
+    n = len(nxs)
+    zs = np.full(n, c["zsrc"], np.int32)
+    zr = np.full(n, c["zrec"], np.int32)
+    return rho, lam, mu, x0, nxs, xsrc, zs, zr
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    os.environ["ELASTIC_RTM_DEVICE"] = str(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from elastic_gb300.batch import BatchRTM
+    from elastic_gb300 import synth
+    from elastic_gb300._lib import load
+    c = CFG
+    rho, lam, mu, x0, nxs, xsrc, zs, zr = build_survey()
+    eng = BatchRTM(c["nz"], c["nx"], c["nt"], c["dx"], c["dt"], c["fp"], c["abc"], rho, lam, mu, x0, nxs, xsrc, zs,
+                   zr, comp_mask=c["comp_mask"], group_max=args.group, nsource=c["nsource"])
+    groups = eng.groups()
+    # shard groups over ranks (shots are independent)
+    mine = groups[rank::world]
+    tmax = max(eng.trace_count(s, n) for s, n in groups)
+    traces_host = synth.synthetic_traces(tmax, seed=c["seed"])
+    # device-resident copy for the `value` measurement; pinned host copy for e2e
+    traces_dev = torch.from_numpy(traces_host).to(f"cuda:{local}")
+    lib = load()
+    import ctypes
+    pin = lib.rtm_host_alloc(tmax * 4)
+    pinned = np.ctypeslib.as_array(ctypes.cast(pin, ctypes.POINTER(ctypes.c_float)), shape=(tmax,))
+    pinned[:] = traces_host
+    pf = 3 * c["nz"] * c["nx"]
+    img_dev = torch.zeros(pf, dtype=torch.float32, device=f"cuda:{local}")
+    ipin = lib.rtm_host_alloc(pf * 4)
+    img_host = np.ctypeslib.as_array(ctypes.cast(ipin, ctypes.POINTER(ctypes.c_float)), shape=(pf,))
+    img_host[:] = 0
+
+    def step(k, e2e):
+        s0, n = mine[k % len(mine)]
+        if e2e:
+            eng.migrate(s0, n, pinned, img_host, traces_on_device=False, image_on_device=False)
+        else:
+            eng.migrate(s0, n, traces_dev, img_dev, traces_on_device=True, image_on_device=True)
+        st = eng.stats()
+        return n, st
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for k in range(args.warmup):
+        step(k, False)
+    barrier()
+    cells_done = 0
+    shots_done = 0
+    dev_ms = 0.0
+    fwd_ms = adj_ms = 0.0
+    fwd_launch = adj_launch = 0
+    adj_cells = 0
+    kernels = 0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            n, st = step(k, False)
+            cells_done += 2 * st["cells"] * c["nt"]
+            shots_done += n
+            dev_ms += st["total_ms"]
+            fwd_ms += st["fwd_ms"]
+            adj_ms += st["adj_ms"]
+            fwd_launch += c["nt"] - 1
+            adj_launch += c["nt"]
+            adj_cells += st["cells"] * c["nt"]
+            kernels += st["kernels"] + 4 * n
+        barrier()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    # end-to-end: host traces in pinned memory, host image out, every step
+    barrier()
+    e2e_ms = 0.0
+    e2e_cells = 0
+    te0 = time.perf_counter()
+    for k in range(args.steps):
+        n, st = step(k, True)
+        e2e_cells += 2 * st["cells"] * c["nt"]
+    barrier()
+    e2e_wall = time.perf_counter() - te0
+    h2d = 4 * sum(eng.trace_count(*mine[k % len(mine)]) for k in range(args.steps)) / args.steps + 4 * pf
+    d2h = 4 * pf
+    # max over ranks
+    times = torch.tensor([dev_ms / 1e3, e2e_wall], dtype=torch.float64, device=f"cuda:{local}")
+    tot = torch.tensor([cells_done, shots_done, e2e_cells], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+    t_dev, t_e2e = times.tolist()
+    cells_all, shots_all, e2e_cells_all = tot.tolist()
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    adj_launch_ms = adj_ms / adj_launch
+    cells_per_launch = adj_cells / adj_launch
+    achieved = cells_per_launch * BYTES_ADJ / (adj_launch_ms * 1e-3) / 1e9
+    tpc = profile_traffic()
+    value = cells_all / t_dev / 1e9
+    line = {
+        "metric": "Gcell-updates/s",
+        "value": round(value, 3),
+        "unit": "Gcell/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t_dev / args.steps, 2),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "batched multi-shot 2D elastic RTM, BASELINE config 2: 2000x800 grid, dx=5 m, "
+                               "dt=0.5 ms, nt=6000, 64 shots on 600-2000-cell subgrids; one step = one group of "
+                               f"{args.group} shots (forward + adjoint with imaging); FP16 source snapshots",
+                   "group_shots": args.group, "inputs_vs_l2": "inputs larger than L2 (snapshots ~150 GB)",
+                   "shots_per_s": round(shots_all / t_dev, 3),
+                   "wall_s": round(wall, 3),
+                   "fwd_ms_per_step": round(fwd_ms / args.steps, 2),
+                   "adj_ms_per_step": round(adj_ms / args.steps, 2)},
+        "e2e": {"value": round(e2e_cells_all / t_e2e / 1e9, 3), "unit": "Gcell/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(kernels),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "kernel": "k_step2d adjoint + fused imaging (112 algorithmic B/cell)",
+                     "traffic": (round(tpc * cells_per_launch) if tpc else None)},
+        "clocks": clocks,
+    }
+    if world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- CPU arm
+def _cpu_worker(spec):
+    """One shot of the RTM on its subgrid, truncated to nt steps, in the C
+    oracle (the reference's algorithm: full-history forward, image_init,
+    rtm_op3 + C recursion, imaging)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    nz, w, nt, seed = spec
+    c = CFG
+    from elastic_gb300 import synth
+    vp = synth.smooth_random_model(nz, w, c["dx"], 200.0, 1800.0, 4000.0, seed=seed)
+    rho, lam, mu = synth.lame_from_vp(vp)
+    rng = np.random.default_rng(seed)
+    D = [(1e-3 * rng.standard_normal((w, nt))).astype(np.float32) for _ in range(5)]
+    dm = [np.zeros((w, nz), np.float32) for _ in range(3)]
+    t0 = time.perf_counter()
+    O.rtm_op2(True, rho, lam, mu, dm, D, np.float32(c["dx"]), np.float32(c["dt"]), nt, c["zsrc"], w // 2,
+              c["zrec"], np.float32(c["fp"]), c["abc"], c["nsource"])
+    return time.perf_counter() - t0, 2 * nz * w * nt
+
+
+def cpu_baseline(seconds_target=15.0):
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    nz, w = CFG["nz"], 1300  # the mean subgrid width of the survey
+    # calibrate the window on one core, then one shot per core
+    t, cells = _cpu_worker((nz, w, 8, 0))
+    rate1 = cells / t
+    nt = int(max(8, min(96, seconds_target * rate1 / (2 * nz * w))))
+    mem_gb = 11 * nz * w * nt * 4 / 1e9
+    try:
+        avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE") / 1e9
+    except Exception:
+        avail = 64.0
+    procs = int(max(1, min(cores, 0.5 * avail // max(mem_gb, 1e-3))))
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(procs) as pool:
+        res = pool.map(_cpu_worker, [(nz, w, nt, s) for s in range(procs)])
+    wall = time.perf_counter() - t0
+    total = sum(r[1] for r in res)
+    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "librefc.so")) else "port"
+    return {"value": round(total / wall / 1e9, 5), "unit": "Gcell/s", "cores": procs, "kind": "port",
+            "sample": f"{procs} shots (one per core) of the RTM (forward + adjoint + imaging, full-history "
+                      f"reference algorithm, C oracle restating the Fortran and rtmlib-modC.c) on {nz}x{w} "
+                      f"subgrids, nt window {nt} of 6000 (per-step rate)",
+            "ref_c_built_here": kind == "reference"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.cpu_seconds)
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"], "unit": "Gcell/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched multi-shot 2D elastic RTM, BASELINE config 2 (CPU sample: "
+                                   + cb["sample"] + ")"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--group", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nt", type=int, default=None, help="override nt (profiling captures only)")
+    ap.add_argument("--shots", type=int, default=None, help="override the shot count (profiling captures only)")
+    args = ap.parse_args()
+    if args.nt:
+        CFG["nt"] = args.nt
+    if args.shots:
+        CFG["nshots"] = args.shots
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

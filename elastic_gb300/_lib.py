@@ -39,6 +39,14 @@ SIGNATURES = {
                   + [_P] * 11 + [_c_int, _c_int]),
     "rtm_op_d_": (_c_int, [_c_int] * 4 + [_c_double, _c_double] + [_c_int] * 3 + [_c_double, _c_int, _c_int]
                   + [_P] * 11 + [_c_int, _c_int]),
+    "rtm_batch_create": (ctypes.c_void_p, [_c_int, _c_int, _c_int, _c_float, _c_float, _c_float, _c_int, _c_int]
+                         + [_P] * 3 + [_c_int] + [_P] * 5 + [_c_int, _c_int, _c_int]),
+    "rtm_batch_migrate": (_c_int, [_P, _c_int, _c_int, _P, _c_int, _P, _c_int]),
+    "rtm_batch_stats": (_c_int, [_P, _P]),
+    "rtm_batch_set": (_c_int, [_P, _c_int]),
+    "rtm_batch_destroy": (None, [_P]),
+    "rtm_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "rtm_host_free": (None, [_P]),
 }
 
 _lib = None

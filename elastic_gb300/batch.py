@@ -1,0 +1,63 @@
+"""Batched multi-shot RTM (the C-ABI's rtm_batch_* entry points).
+
+Shots sit on their own subgrids of a full model; groups of shots are migrated
+together on the GPU (see csrc/batch.cu).  Traces and images may be host numpy
+arrays or device tensors (anything with ``data_ptr()``).
+"""
+import ctypes
+
+import numpy as np
+
+from ._lib import RtmError, check, load, ptr
+
+
+class BatchRTM:
+    def __init__(self, nz, nx, nt, dx, dt, fp, abc, rho, lam, mu, x0, nxs, xsrc, zsrc, zrec, comp_mask=3,
+                 group_max=4, nsource=250, exact_adjoint=False):
+        lib = load()
+        self.nz, self.nx, self.nt = nz, nx, nt
+        self.nxs = np.ascontiguousarray(nxs, np.int32)
+        self.nshots = len(self.nxs)
+        self.comp_mask = comp_mask
+        self.ncomp = bin(comp_mask & 31).count("1")
+        self.group_max = min(group_max, self.nshots)
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (rho, lam, mu)]
+        ints = [np.ascontiguousarray(a, np.int32) for a in (x0, nxs, xsrc, zsrc, zrec)]
+        self._keep = arrs + ints
+        h = lib.rtm_batch_create(nz, nx, nt, dx, dt, fp, nsource, abc, *[ptr(a) for a in arrs], self.nshots,
+                                 *[ptr(a) for a in ints], comp_mask, group_max, 1 if exact_adjoint else 0)
+        if not h:
+            raise RtmError(lib.rtm_last_error().decode())
+        self.h = ctypes.c_void_p(h)
+
+    def trace_count(self, s0, ns):
+        """Number of floats of the traces of shots [s0, s0+ns)."""
+        return int(self.ncomp * self.nt * self.nxs[s0:s0 + ns].sum())
+
+    def groups(self):
+        """Consecutive groups of at most group_max shots."""
+        return [(s, min(self.group_max, self.nshots - s)) for s in range(0, self.nshots, self.group_max)]
+
+    def migrate(self, shot0, nshot, traces, image, traces_on_device=False, image_on_device=False):
+        check(load().rtm_batch_migrate(self.h, shot0, nshot, ptr(traces), int(traces_on_device), ptr(image),
+                                       int(image_on_device)))
+
+    def stats(self):
+        out = np.zeros(8, np.float64)
+        check(load().rtm_batch_stats(self.h, ptr(out)))
+        return dict(fwd_ms=out[0], adj_ms=out[1], cells=int(out[2]), kernels=int(out[3]), total_ms=out[4],
+                    tile_x=int(out[5]), work_items=int(out[6]))
+
+    def set_graph(self, use_graph):
+        check(load().rtm_batch_set(self.h, 1 if use_graph else 0))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().rtm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,509 @@
+// Batched multi-shot 2D elastic RTM on one GPU.
+//
+// Shots live on their own subgrids (uneven widths) of a full model.  A batch
+// ("group") of shots is propagated together: every time level is ONE launch
+// of the fused step kernel over the work items of all shots of the group
+// (a persistent grid of CTAs walking the (shot, tile) list), and the whole
+// nt-level loop of both passes is captured once per group as a CUDA graph.
+//
+// Source side: the forward pass stores per-level FP16 snapshots of Vx, Vz
+// (each plane scaled by 2^14/max|.|, the max being reduced by the kernel
+// that wrote the level) -- the only part of the source wavefield the imaging
+// condition needs (W/image-mod-rtm.f90:57-65 uses Vx0, Vz0 only).
+// Receiver side: the adjoint pass injects the traces at the receiver row
+// and applies the imaging condition of W/image-mod-rtm.f90:146-162 in the
+// same kernel, accumulating the three images in FP32 with Kahan
+// compensation.  Propagation stays FP32 throughout.
+//
+// Each shot is an independent problem on its subgrid (model_op, masks and
+// sponge are those of the subgrid), so a shot migrated in a batch gives the
+// same image as the single-shot pipeline on its subgrid (up to the FP16
+// snapshot rounding and the summation order of the imaging condition).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/elastic_rtm.h"
+#include "elastic2d.cuh"
+#include "elastic2d_aux.cuh"
+#include "engine.h"
+
+using namespace eg;
+
+static char g_pending_at[128] = "";
+static void note_pending(const char *where)
+{
+    if (!g_pending_at[0] && cudaPeekAtLastError() != cudaSuccess) snprintf(g_pending_at, sizeof g_pending_at, "%s", where);
+}
+
+namespace {
+
+__global__ void k_snap_plane(const ShotGeom *shots, int ld, const float *vx, const float *vz, const float *maxes,
+                             __half *s0, __half *s1)
+{
+    const ShotGeom g = shots[blockIdx.z];
+    const int iz = blockIdx.x * blockDim.x + threadIdx.x, ix = blockIdx.y;
+    if (iz >= g.nz || ix >= g.nx) return;
+    const long long o = g.off + (long long)ix * ld + iz;
+    const float m0 = maxes[2 * blockIdx.z], m1 = maxes[2 * blockIdx.z + 1];
+    s0[o] = __float2half_rn(vx[o] * (m0 > 0.f ? SNAP_Q / m0 : 0.f));
+    s1[o] = __float2half_rn(vz[o] * (m1 > 0.f ? SNAP_Q / m1 : 0.f));
+}
+
+// traces of one shot: reference layout comp-major (nt,nx) gathers -> [it][slot][ix]
+__global__ void k_traces_in(int nt, int nx, int ncomp, const float *src, float *dst)
+{
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x, it = blockIdx.y, c = blockIdx.z;
+    if (ix >= nx) return;
+    dst[((long long)it * ncomp + c) * nx + ix] = src[((long long)c * nx + ix) * nt + it];
+}
+
+// full image (3 planes, ld nz) += shot images (sum minus Kahan residual)
+// One launch per shot: overlapping subgrids are summed in shot order.
+__global__ void k_stack(const ShotGeom *shots, int shot, int ld, int nz, long long plane_full, const int *x0,
+                        const float *img, const float *cmp, long long gplane, float *full)
+{
+    const ShotGeom g = shots[shot];
+    const int iz = blockIdx.x * blockDim.x + threadIdx.x, ix = blockIdx.y;
+    if (iz >= g.nz || ix >= g.nx) return;
+    const long long o = g.off + (long long)ix * ld + iz;
+    const long long f = (long long)(x0[shot] + ix) * nz + iz;
+#pragma unroll
+    for (int i = 0; i < 3; i++) full[i * plane_full + f] += img[i * gplane + o] - cmp[i * gplane + o];
+}
+
+}  // namespace
+
+struct rtm_batch {
+    int nz = 0, nx = 0, nt = 0;
+    float dx = 0, dt = 0, fp = 0;
+    int nsource = 250, abc = 0, comp_mask = 3, ncomp = 2, group_max = 1, exact_adj = 0;
+    std::vector<int> x0, nxs, xsrc, zsrc, zrec;  // 0-based
+    int ldz = 0;
+    long long cap_cols = 0, gplane = 0;
+    DevBuf<float> model, coefraw, coef, F, A, zero, img, filt, maxes, traces, tstage, full;
+    DevBuf<__half> snaps;
+    DevBuf<int> dx0;
+    ShotTable tab;
+    std::vector<float> dtsrc;
+    cudaStream_t st = nullptr;
+    double last_fwd_ms = 0, last_adj_ms = 0, last_total_ms = 0;
+    long long last_cells = 0;
+    int kernels_last = 0;
+    bool use_graph = true;
+
+    ~rtm_batch()
+    {
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_dev, float *image, int image_dev)
+{
+    RTM_CHECK_ARG(s0 >= 0 && ns >= 1 && s0 + ns <= (int)b->x0.size() && ns <= b->group_max, "bad shot range");
+    {
+        const cudaError_t pend = cudaGetLastError();
+        if (pend != cudaSuccess) {
+            rtm_set_error("rtm_batch_migrate: CUDA error pending on entry: %s (first seen at %s)",
+                          cudaGetErrorString(pend), g_pending_at[0] ? g_pending_at : "?");
+            return RTM_ERR_CUDA;
+        }
+    }
+    const int nz = b->nz, nt = b->nt, ld = b->ldz;
+    cudaStream_t st = b->st;
+    // ---- group geometry
+    long long col = 0, doff = 0, tin = 0;
+    b->tab.shots.clear();
+    std::vector<int> x0g(ns);
+    std::vector<long long> tin_off(ns);
+    for (int i = 0; i < ns; i++) {
+        const int s = s0 + i;
+        HostShot h;
+        h.off = col * ld;
+        h.doff = doff;
+        h.nz = nz;
+        h.nx = b->nxs[s];
+        h.src_iz = b->zsrc[s];
+        h.src_ix = b->xsrc[s] - b->x0[s];
+        h.rec_iz = b->zrec[s];
+        b->tab.shots.push_back(h);
+        x0g[i] = b->x0[s];
+        tin_off[i] = tin;
+        col += b->nxs[s];
+        doff += (long long)nt * b->ncomp * b->nxs[s];
+        tin += (long long)b->ncomp * b->nxs[s] * nt;
+    }
+    RTM_CHECK_ARG(col <= b->cap_cols, "group wider than the batch capacity");
+    b->tab.ldz = ld;
+    TRY(b->tab.build(pick_tile_width((long long)nz, col)));
+    RTM_CUDA(cudaMemcpyAsync(b->dx0.p, x0g.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+    const long long gp = b->gplane;
+    // ---- coefficients of every shot's subgrid
+    for (int i = 0; i < ns; i++) {
+        const HostShot &h = b->tab.shots[i];
+        const long long mo = (long long)x0g[i] * nz;
+        float *r[5], *c[5];
+        for (int k = 0; k < 5; k++) {
+            r[k] = b->coefraw.p + k * gp + h.off;
+            c[k] = b->coef.p + k * gp + h.off;
+        }
+        const long long pf = (long long)nz * b->nx;
+        TRY(model_coefs<float>(nz, h.nx, b->dx, b->dt, b->model.p + mo, b->model.p + pf + mo, b->model.p + 2 * pf + mo,
+                               nz, r[M1X], r[M1Z], nullptr, nullptr, r[A2], r[A3], r[A23], ld, st));
+        const float *rc[5] = {r[0], r[1], r[2], r[3], r[4]};
+        TRY(mask_coefs<float>(nz, h.nx, rc, ld, c, ld, st));
+    }
+    // ---- traces -> device internal layout
+    const float *tsrc = traces;
+    if (!traces_dev) {
+        RTM_CUDA(cudaMemcpyAsync(b->tstage.p, traces, tin * sizeof(float), cudaMemcpyHostToDevice, st));
+        tsrc = b->tstage.p;
+    }
+    for (int i = 0; i < ns; i++) {
+        const HostShot &h = b->tab.shots[i];
+        dim3 blk(128), grd(ceil_div(h.nx, 128), nt, b->ncomp);
+        k_traces_in<<<grd, blk, 0, st>>>(nt, h.nx, b->ncomp, tsrc + tin_off[i], b->traces.p + h.doff);
+        RTM_CUDA(cudaGetLastError());
+    }
+    // ---- state
+    RTM_CUDA(cudaMemsetAsync(b->F.p, 0, 10 * gp * sizeof(float), st));
+    RTM_CUDA(cudaMemsetAsync(b->A.p, 0, 10 * gp * sizeof(float), st));
+    RTM_CUDA(cudaMemsetAsync(b->img.p, 0, 6 * gp * sizeof(float), st));
+    RTM_CUDA(cudaMemsetAsync(b->maxes.p, 0, (size_t)(nt + 2) * b->group_max * 2 * sizeof(float), st));
+
+    auto fb = [&](int par, int f) { return b->F.p + (par * 5 + f) * gp; };
+    auto ab = [&](int par, int f) { return b->A.p + (par * 5 + f) * gp; };
+    auto snap = [&](int L, int f) { return b->snaps.p + ((size_t)(L - 1) * 2 + f) * gp; };  // level L (1-based)
+    auto mx = [&](int L) { return b->maxes.p + (size_t)L * b->group_max * 2; };
+    const float inv_dt = 1.0f / b->dt, inv_dx = 1.0f / b->dx;
+
+    auto base_args = [&]() {
+        Step2DArgs<float> a;
+        memset(&a, 0, sizeof a);
+        for (int k = 0; k < 5; k++) a.coef[k] = b->coef.p + k * gp;
+        a.shots = b->tab.d_geom;
+        a.nshots = ns;
+        a.ntiles = b->tab.ntiles;
+        a.ldz = ld;
+        a.filt = b->filt.p;
+        a.abc2 = b->abc + 5;
+        a.inv_dt = inv_dt;
+        a.inv_dx = inv_dx;
+        return a;
+    };
+    // initialise launch configuration outside any capture
+    {
+        Step2DArgs<float> a = base_args();
+        a.ntiles = 0;
+        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st));
+        a.img[0] = b->img.p;
+        TRY(launch_step<float>(a, true, false, b->tab.tx, 0, st));
+    }
+
+    cudaEvent_t e0, e1, e2;
+    RTM_CUDA(cudaEventCreate(&e0));
+    RTM_CUDA(cudaEventCreate(&e1));
+    RTM_CUDA(cudaEventCreate(&e2));
+    int nkern = 0;
+    // ---- forward pass: levels 2..nt (level 1 is zero), then the snapshot
+    // of the last level
+    auto record_fwd = [&]() -> int {
+        for (int L = 2; L <= nt; L++) {
+            Step2DArgs<float> a = base_args();
+            for (int f = 0; f < 5; f++) {
+                a.out[f] = fb(L & 1, f);
+                a.own2[f] = fb(L & 1, f);
+                a.nb[f] = fb((L - 1) & 1, f);
+            }
+            a.sponge = L >= 3;
+            a.has_src = 1;
+            a.srcval = b->dtsrc[L - 2];
+            a.snap_out[0] = snap(L - 1, 0);
+            a.snap_out[1] = snap(L - 1, 1);
+            a.snap_max_in = mx(L - 1);
+            a.snap_max_out = mx(L);
+            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st));
+            nkern++;
+        }
+        dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
+        k_snap_plane<<<grd, blk, 0, st>>>(b->tab.d_geom, ld, fb(nt & 1, VX), fb(nt & 1, VZ), mx(nt), snap(nt, 0), snap(nt, 1));
+        RTM_CUDA(cudaGetLastError());
+        nkern++;
+        return RTM_OK;
+    };
+    // ---- adjoint pass with the imaging condition: levels nt..1
+    auto record_adj = [&]() -> int {
+        for (int L = nt; L >= 1; L--) {
+            Step2DArgs<float> a = base_args();
+            for (int f = 0; f < 5; f++) {
+                a.out[f] = ab(L & 1, f);
+                a.own2[f] = L + 2 <= nt ? ab(L & 1, f) : b->zero.p;
+                a.nb[f] = L + 1 <= nt ? ab((L + 1) & 1, f) : b->zero.p;
+            }
+            a.sponge = b->exact_adj;
+            a.rec = b->traces.p;
+            a.comp_mask = b->comp_mask;
+            a.ncomp = b->ncomp;
+            a.it = L - 1;
+            a.isnap0[0] = snap(L, 0);
+            a.isnap0[1] = snap(L, 1);
+            a.imax0 = mx(L);
+            a.ilast = L == nt;
+            a.isnap1[0] = L < nt ? snap(L + 1, 0) : snap(L, 0);
+            a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
+            a.imax1 = L < nt ? mx(L + 1) : mx(L);
+            for (int i = 0; i < 3; i++) {
+                a.img[i] = b->img.p + i * gp;
+                a.imgc[i] = b->img.p + (3 + i) * gp;
+            }
+            TRY(launch_step<float>(a, true, false, b->tab.tx, 0, st));
+            nkern++;
+        }
+        return RTM_OK;
+    };
+    // capture one graph per pass; timing events stay outside the graphs
+    cudaGraphExec_t gx[2] = {nullptr, nullptr};
+    auto capture = [&](int which, cudaGraphExec_t *out) -> int {
+        cudaGraph_t g = nullptr;
+        RTM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int s = which == 0 ? record_fwd() : record_adj();
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (s) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (ce != cudaSuccess) {
+            rtm_set_error("graph capture failed: %s", cudaGetErrorString(ce));
+            return RTM_ERR_CUDA;
+        }
+        const cudaError_t ie = cudaGraphInstantiate(out, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            rtm_set_error("graph instantiation failed: %s", cudaGetErrorString(ie));
+            return RTM_ERR_CUDA;
+        }
+        return RTM_OK;
+    };
+    int rc = RTM_OK;
+    if (b->use_graph) {
+        rc = capture(0, &gx[0]);
+        if (!rc) rc = capture(1, &gx[1]);
+        if (!rc) {
+            RTM_CUDA(cudaEventRecord(e0, st));
+            RTM_CUDA(cudaGraphLaunch(gx[0], st));
+            RTM_CUDA(cudaEventRecord(e1, st));
+            RTM_CUDA(cudaGraphLaunch(gx[1], st));
+            RTM_CUDA(cudaEventRecord(e2, st));
+        }
+    } else {
+        RTM_CUDA(cudaEventRecord(e0, st));
+        rc = record_fwd();
+        if (!rc) RTM_CUDA(cudaEventRecord(e1, st));
+        if (!rc) rc = record_adj();
+        if (!rc) RTM_CUDA(cudaEventRecord(e2, st));
+    }
+    if (rc) {
+        for (auto &x : gx) if (x) cudaGraphExecDestroy(x);
+        cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+        return rc;
+    }
+    // ---- stack into the full image
+    {
+        for (int i = 0; i < ns; i++) {
+            dim3 blk(128), grd(ceil_div(nz, 128), b->nxs[s0 + i], 1);
+            k_stack<<<grd, blk, 0, st>>>(b->tab.d_geom, i, ld, nz, (long long)nz * b->nx, b->dx0.p, b->img.p,
+                                         b->img.p + 3 * gp, gp, b->full.p);
+            RTM_CUDA(cudaGetLastError());
+        }
+    }
+    const size_t pf = (size_t)nz * b->nx;
+    if (image_dev) {
+        RTM_CUDA(cudaMemcpyAsync(image, b->full.p, 3 * pf * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    } else {
+        RTM_CUDA(cudaMemcpyAsync(image, b->full.p, 3 * pf * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    RTM_CUDA(cudaStreamSynchronize(st));
+    float f_ms = 0, a_ms = 0;
+    RTM_CUDA(cudaEventElapsedTime(&f_ms, e0, e1));
+    RTM_CUDA(cudaEventElapsedTime(&a_ms, e1, e2));
+    b->last_fwd_ms = f_ms;
+    b->last_adj_ms = a_ms;
+    b->kernels_last = nkern;
+    long long cells = 0;
+    for (int i = 0; i < ns; i++) cells += (long long)nz * b->nxs[s0 + i];
+    b->last_cells = cells;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    for (auto &x : gx) if (x) cudaGraphExecDestroy(x);
+    return RTM_OK;
+}
+
+}  // namespace
+
+extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc,
+                                       const float *rho, const float *lambda, const float *mu, int nshots,
+                                       const int *x0, const int *nxs, const int *xsrc, const int *zsrc,
+                                       const int *zrec, int comp_mask, int group_max, int exact_adjoint)
+{
+    auto fail = [](int code, const char *msg) -> rtm_batch * {
+        if (msg) rtm_set_error("%s", msg);
+        (void)code;
+        return nullptr;
+    };
+    if (nz < 11 || nx < 11 || nt < 3 || nshots < 1 || group_max < 1 || !(comp_mask & 31))
+        return fail(RTM_ERR_ARG, "rtm_batch_create: bad sizes");
+    note_pending("create entry");
+    if (ensure_device()) return nullptr;
+    note_pending("after ensure_device");
+    rtm_batch *b = new rtm_batch();
+    b->nz = nz; b->nx = nx; b->nt = nt; b->dx = dx; b->dt = dt; b->fp = fp;
+    b->nsource = nsource; b->abc = abc; b->comp_mask = comp_mask & 31; b->exact_adj = exact_adjoint ? 1 : 0;
+    b->ncomp = __builtin_popcount(b->comp_mask);
+    b->group_max = std::min(group_max, nshots);
+    for (int s = 0; s < nshots; s++) {
+        const int a0 = x0[s] - 1, w = nxs[s], xs = xsrc[s] - 1, zs = zsrc[s] - 1, zr = zrec[s] - 1;
+        if (a0 < 0 || w < abc + 5 || w < 11 || a0 + w > nx || xs < a0 || xs >= a0 + w || zs < 0 || zs >= nz || zr < 0 ||
+            zr >= nz || nz < abc + 5) {
+            delete b;
+            rtm_set_error("rtm_batch_create: shot %d geometry outside the grid or narrower than the sponge", s);
+            return nullptr;
+        }
+        b->x0.push_back(a0); b->nxs.push_back(w); b->xsrc.push_back(xs); b->zsrc.push_back(zs); b->zrec.push_back(zr);
+    }
+    b->ldz = (nz + 31) / 32 * 32;
+    // capacity: the group_max widest shots
+    std::vector<int> w(b->nxs);
+    std::sort(w.begin(), w.end(), std::greater<int>());
+    long long cap = 0;
+    for (int i = 0; i < b->group_max; i++) cap += w[i];
+    b->cap_cols = cap;
+    b->gplane = cap * b->ldz;
+    long long tcap = 0;
+    for (int i = 0; i < b->group_max; i++) tcap += (long long)w[i] * nt * b->ncomp;
+    const size_t gp = (size_t)b->gplane, pf = (size_t)nz * nx;
+    int s = 0;
+    if (!s) s = b->model.alloc(3 * pf);
+    if (!s) s = b->coefraw.alloc(5 * gp);
+    if (!s) s = b->coef.alloc(5 * gp);
+    if (!s) s = b->F.alloc(10 * gp);
+    if (!s) s = b->A.alloc(10 * gp);
+    if (!s) s = b->zero.alloc(gp);
+    if (!s) s = b->img.alloc(6 * gp);
+    if (!s) s = b->filt.alloc(abc + 5);
+    if (!s) s = b->maxes.alloc((size_t)(nt + 2) * b->group_max * 2);
+    if (!s) s = b->traces.alloc((size_t)tcap);
+    if (!s) s = b->tstage.alloc((size_t)tcap);
+    if (!s) s = b->full.alloc(3 * pf);
+    if (!s) s = b->snaps.alloc((size_t)nt * 2 * gp);
+    if (!s) s = b->dx0.alloc(b->group_max);
+    note_pending("after allocations");
+    if (s) { delete b; return nullptr; }
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        rtm_set_error("stream creation failed");
+        return nullptr;
+    }
+    note_pending("after stream");
+    std::vector<float> f(abc + 5), src(nt);
+    host_abc_filter<float>(abc, f.data());
+    host_ricker<float>(nt, dt, fp, nsource, src.data());
+    b->dtsrc.resize(nt);
+    for (int i = 0; i < nt; i++) b->dtsrc[i] = dt * src[i];
+    const struct { cudaError_t e; const char *what; } ops[] = {
+        {cudaMemcpy(b->model.p, rho, pf * sizeof(float), cudaMemcpyHostToDevice), "rho upload"},
+        {cudaMemcpy(b->model.p + pf, lambda, pf * sizeof(float), cudaMemcpyHostToDevice), "lambda upload"},
+        {cudaMemcpy(b->model.p + 2 * pf, mu, pf * sizeof(float), cudaMemcpyHostToDevice), "mu upload"},
+        {cudaMemset(b->zero.p, 0, gp * sizeof(float)), "zero plane"},
+        {cudaMemset(b->coefraw.p, 0, 5 * gp * sizeof(float)), "coefficient planes"},
+        {cudaMemset(b->coef.p, 0, 5 * gp * sizeof(float)), "masked coefficient planes"},
+        {cudaMemcpy(b->filt.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice), "filter upload"},
+        {cudaDeviceSynchronize(), "synchronize"},
+    };
+    for (const auto &op : ops)
+        if (op.e != cudaSuccess) {
+            rtm_set_error("rtm_batch_create: %s failed: %s", op.what, cudaGetErrorString(op.e));
+            cudaGetLastError();
+            delete b;
+            return nullptr;
+        }
+    note_pending("end of create");
+    return b;
+}
+
+extern "C" int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device,
+                                 float *image, int image_on_device)
+{
+    RTM_CHECK_ARG(b && traces && image, "rtm_batch_migrate: null argument");
+    note_pending("migrate entry");
+    TRY(ensure_device());
+    note_pending("migrate after ensure_device");
+    cudaEvent_t t0, t1;
+    RTM_CUDA(cudaEventCreate(&t0));
+    RTM_CUDA(cudaEventCreate(&t1));
+    // the full image accumulates across calls: load the caller's image first
+    const size_t pf = (size_t)b->nz * b->nx;
+    RTM_CUDA(cudaEventRecord(t0, b->st));
+    note_pending("migrate before image load");
+    RTM_CUDA(cudaMemcpyAsync(b->full.p, image, 3 * pf * sizeof(float),
+                             image_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, b->st));
+    note_pending("migrate after image load");
+    int s = batch_group(b, shot0, nshot, traces, traces_on_device, image, image_on_device);
+    RTM_CUDA(cudaEventRecord(t1, b->st));
+    RTM_CUDA(cudaEventSynchronize(t1));
+    float ms = 0;
+    if (!s) RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+    b->last_total_ms = ms;
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return s;
+}
+
+extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
+{
+    RTM_CHECK_ARG(b && out, "null argument");
+    out[0] = b->last_fwd_ms;
+    out[1] = b->last_adj_ms;
+    out[2] = (double)b->last_cells;
+    out[3] = (double)b->kernels_last;
+    out[4] = b->last_total_ms;
+    out[5] = (double)b->tab.tx;
+    out[6] = (double)b->tab.ntiles;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_set(rtm_batch *b, int use_graph)
+{
+    RTM_CHECK_ARG(b, "null argument");
+    b->use_graph = use_graph != 0;
+    return RTM_OK;
+}
+
+extern "C" void rtm_batch_destroy(rtm_batch *b) { delete b; }
+
+// Diagnostic: the pending CUDA error of this library's runtime and where it
+// was first seen (not part of the public header).
+extern "C" int rtm_debug_peek(char *where, int n)
+{
+    if (where && n > 0) snprintf(where, n, "%s", g_pending_at);
+    return (int)cudaPeekAtLastError();
+}
+
+extern "C" void *rtm_host_alloc(size_t bytes)
+{
+    void *p = nullptr;
+    note_pending("host_alloc entry");
+    if (ensure_device()) return nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+        rtm_set_error("cudaMallocHost of %zu bytes failed", bytes);
+        return nullptr;
+    }
+    return p;
+}
+
+extern "C" void rtm_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}

@@ -58,15 +58,17 @@ template <typename T, bool EXACT, bool ADJ, int TX>
 static int launch_step_tx(const Step2DArgs<T> &a, int grid_cap, cudaStream_t st)
 {
     auto kern = k_step2d<T, EXACT, ADJ, TZ_TILE, TX>;
-    constexpr size_t smem = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>();
-    static int grid_max = 0;
-    if (!grid_max) {
-        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const bool img = ADJ && a.img[0] != nullptr;
+    const size_t smem = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>(img);
+    static int grid_max[2] = {0, 0};
+    if (!grid_max[img]) {
+        const size_t smax = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>(true);
+        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
         int nb = 0;
         RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
-        grid_max = (nb > 0 ? nb : 1) * device_sm_count();
+        grid_max[img] = (nb > 0 ? nb : 1) * device_sm_count();
     }
-    int grid = a.ntiles < grid_max ? a.ntiles : grid_max;
+    int grid = a.ntiles < grid_max[img] ? a.ntiles : grid_max[img];
     if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
     if (grid <= 0) return RTM_OK;
     kern<<<grid, 256, smem, st>>>(a);
@@ -133,9 +135,17 @@ int model_coefs(int nz, int nx, T dx, T dt, const T *d_rho, const T *d_lam, cons
                 T *m2o, T *m3o, T *a2, T *a3, T *a23, int ldout, cudaStream_t st)
 {
     const T aux = dt / dx;
+    RTM_CHECK_ARG(nz > 0 && nx > 0 && nx <= 65535, "model_coefs: bad grid %d x %d", nz, nx);
     dim3 b(128), g(ceil_div(nz, 128), nx);
     k_model_coef<T><<<g, b, 0, st>>>(nz, nx, d_rho, d_lam, d_mu, ldin, aux, m1x, m1z, m2o, m3o, a2, a3, a23, ldout);
-    RTM_CUDA(cudaGetLastError());
+    {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            rtm_set_error("k_model_coef launch (grid %u x %u, stream %p): %s", g.x, g.y, (void *)st,
+                          cudaGetErrorString(e));
+            return RTM_ERR_CUDA;
+        }
+    }
     return RTM_OK;
 }
 template int model_coefs<float>(int, int, float, float, const float *, const float *, const float *, int, float *,
@@ -789,7 +799,7 @@ int dropin_run(int it_max, int nt, int nz, int nx, int ldz, size_t pstride, floa
     RTM_CUDA(cudaEventRecord(e1, h.st));
     RTM_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
+    RTM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (ms_per_step) *ms_per_step = it_max >= 0 ? ms / (it_max + 1) : 0;

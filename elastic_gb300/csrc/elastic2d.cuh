@@ -67,7 +67,29 @@ struct Step2DArgs {
     int comp_mask;
     int ncomp;
     int it;  // level index used to address the traces
+
+    // ---- streaming RTM extensions (float only) ----------------------------
+    // forward: FP16 snapshot of Vx, Vz of the neighbour level (it-1), each
+    // plane scaled by 2^14 / max|.| of that level (snap_max_in[shot][2]); the
+    // max-abs of the level being written goes to snap_max_out[shot][2].
+    __half *snap_out[2];
+    const float *snap_max_in;
+    float *snap_max_out;
+    // adjoint: fused imaging condition with the source partials S1..S6 taken
+    // from the FP16 snapshots of levels it (isnap0, with halo) and it+1
+    // (isnap1, centre only); ilast marks the last level (S1 = S2 = 0).
+    // Images img[3] accumulate with Kahan compensation imgc[3].
+    const __half *isnap0[2];
+    const __half *isnap1[2];
+    const float *imax0;
+    const float *imax1;
+    int ilast;
+    T *img[3];
+    T *imgc[3];
+    T inv_dt, inv_dx;
 };
+
+constexpr float SNAP_Q = 16384.0f;  // FP16 snapshot full scale (2^14, headroom to 65504)
 
 template <bool EXACT>
 struct Ar {
@@ -191,6 +213,7 @@ __global__ void __launch_bounds__(256) k_step2d(const __grid_constant__ Step2DAr
     T *sm = reinterpret_cast<T *>(smem_raw);
     using TL = Tile<TZ, TX>;
     constexpr int ROWS = TX / 8;  // x rows per warp (8 warps)
+    constexpr int IMG0 = NArr<ADJ, EXACT>::value;  // first imaging array
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
@@ -232,10 +255,17 @@ __global__ void __launch_bounds__(256) k_step2d(const __grid_constant__ Step2DAr
                 sm[P_M1XVX * TL::SIZE + idx] = cv[M1X] * fv[VX];
                 sm[P_M1ZVZ * TL::SIZE + idx] = cv[M1Z] * fv[VZ];
             }
+            if (ADJ && a.img[0]) {
+                // dequantised source Vx, Vz of level it for S4..S6
+                const float dq0 = a.imax0[2 * s] * (1.0f / SNAP_Q), dq1 = a.imax0[2 * s + 1] * (1.0f / SNAP_Q);
+                sm[(IMG0 + 0) * TL::SIZE + idx] = in ? T(__half2float(a.isnap0[0][o]) * dq0) : T(0);
+                sm[(IMG0 + 1) * TL::SIZE + idx] = in ? T(__half2float(a.isnap0[1][o]) * dq1) : T(0);
+            }
         }
         __syncthreads();
 
         // ---- update: lane = z, each warp owns ROWS consecutive x rows
+        float wmax0 = 0.f, wmax1 = 0.f;  // max-abs of the written Vx, Vz (snapshots)
 #pragma unroll 1
         for (int r = 0; r < ROWS; r++) {
             const int x = warp * ROWS + r, z = lane;
@@ -322,6 +352,61 @@ __global__ void __launch_bounds__(256) k_step2d(const __grid_constant__ Step2DAr
             }
 #pragma unroll
             for (int f = 0; f < 5; f++) a.out[f][o] = v[f];
+            if (!ADJ && a.snap_out[0]) {
+                // FP16 snapshot of the neighbour level (it-1) at this cell and
+                // the max-abs of the level just written
+                const float m0 = a.snap_max_in[2 * s], m1 = a.snap_max_in[2 * s + 1];
+                const float q0 = m0 > 0.f ? SNAP_Q / m0 : 0.f, q1 = m1 > 0.f ? SNAP_Q / m1 : 0.f;
+                a.snap_out[0][o] = __float2half_rn(float(sm[TL::at(VX, x, z)]) * q0);
+                a.snap_out[1][o] = __float2half_rn(float(sm[TL::at(VZ, x, z)]) * q1);
+                wmax0 = fmaxf(wmax0, fabsf(float(v[VX])));
+                wmax1 = fmaxf(wmax1, fabsf(float(v[VZ])));
+            }
+            if (ADJ && a.img[0]) {
+                // imaging condition of level it (W/image-mod-rtm.f90:146-162),
+                // accumulated in reverse time order with Kahan compensation
+                const T *svx = sm + IMG0 * TL::SIZE, *svz = sm + (IMG0 + 1) * TL::SIZE;
+                auto SX = [&](const T *b, int dx_, int dz_) { return b[(x + dx_ + HALO) * TL::LZ + (z + dz_ + HALO)]; };
+                T s1 = T(0), s2 = T(0), s4 = T(0), s5 = T(0), s6 = T(0);
+                if (!a.ilast) {
+                    const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
+                    s1 = a.inv_dt * (T(__half2float(a.isnap1[0][o]) * e0) - SX(svx, 0, 0));
+                    s2 = a.inv_dt * (T(__half2float(a.isnap1[1][o]) * e1) - SX(svz, 0, 0));
+                }
+                if (gz >= 4 && gz <= nz - 6 && gx >= 4 && gx <= nx - 6) {
+                    T p4 = T(0), p5 = T(0);
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        p4 += StagCoef<T>::c(k) * (SX(svx, 5 - k, 0) - SX(svx, -4 + k, 0));
+                        p5 += StagCoef<T>::c(k) * (SX(svz, 0, 5 - k) - SX(svz, 0, -4 + k));
+                    }
+                    s4 = p4 * a.inv_dx;
+                    s5 = p5 * a.inv_dx;
+                }
+                if (gz >= 5 && gz <= nz - 6 && gx >= 5 && gx <= nx - 6) {
+                    T p6 = T(0), p7 = T(0);
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        p6 += StagCoef<T>::c(k) * (SX(svx, 0, 4 - k) - SX(svx, 0, -5 + k));
+                        p7 += StagCoef<T>::c(k) * (SX(svz, 4 - k, 0) - SX(svz, -5 + k, 0));
+                    }
+                    s6 = (p6 + p7) * a.inv_dx;
+                }
+                const T s3 = s4 + s5;
+                const T t1 = v[VX] * s1 + v[VZ] * s2;
+                const T t2 = -(v[SXX] + v[SZZ]) * s3;
+                const T t3 = -(T(2) * v[SXX] * s4 + T(2) * v[SZZ] * s5 + v[SXZ] * s6);
+                const T tt[3] = {t1, t2, t3};
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    T sum = a.img[i][o], c = a.imgc[i][o];
+                    const T y = tt[i] - c;
+                    const T tsum = sum + y;
+                    c = (tsum - sum) - y;
+                    a.img[i][o] = tsum;
+                    a.imgc[i][o] = c;
+                }
+            }
             if (!ADJ && a.rec && gz == g.rec_iz) {
                 int slot = 0;
 #pragma unroll
@@ -332,10 +417,24 @@ __global__ void __launch_bounds__(256) k_step2d(const __grid_constant__ Step2DAr
                     }
             }
         }
+        if (!ADJ && a.snap_out[0]) {  // warp-converged here
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                wmax0 = fmaxf(wmax0, __shfl_xor_sync(0xffffffffu, wmax0, d));
+                wmax1 = fmaxf(wmax1, __shfl_xor_sync(0xffffffffu, wmax1, d));
+            }
+            if (lane == 0) {
+                atomic_max_abs(a.snap_max_out + 2 * s, wmax0);
+                atomic_max_abs(a.snap_max_out + 2 * s + 1, wmax1);
+            }
+        }
     }
 }
 
 template <typename T, bool EXACT, bool ADJ, int TZ, int TX>
-constexpr size_t step2d_smem() { return (size_t)NArr<ADJ, EXACT>::value * Tile<TZ, TX>::SIZE * sizeof(T); }
+constexpr size_t step2d_smem(bool img = false)
+{
+    return (size_t)(NArr<ADJ, EXACT>::value + (ADJ && img ? 2 : 0)) * Tile<TZ, TX>::SIZE * sizeof(T);
+}
 
 }  // namespace eg

@@ -25,6 +25,8 @@
 #ifndef ELASTIC_RTM_H
 #define ELASTIC_RTM_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -137,6 +139,39 @@ int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, i
               int nsource, int abc, const double *rho, const double *lambda, const double *mu, double *drho,
               double *dlambda, double *dmu, double *Vx, double *Vz, double *sigmaxx, double *sigmazz,
               double *sigmaxz, int linear, int exact_adjoint);
+
+/* -------------------------------------------- batched multi-shot RTM
+ * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
+ * shots of a survey, each on its own subgrid [x0, x0+nxs) of the full model
+ * (uneven widths), are migrated in groups of up to group_max shots.  Each
+ * time level of a group is one launch over all its shots; the nt-level
+ * loops of both passes are captured as one CUDA graph per group.  The
+ * source side keeps per-level FP16 snapshots of Vx, Vz (per-snapshot
+ * scaled); propagation and image accumulation (Kahan) are FP32; fast
+ * arithmetic.  Positions are 1-based in the full grid.  comp_mask selects
+ * the recorded components (bit 0 Vx, 1 Vz, 2 sigma_xx, 3 sigma_zz,
+ * 4 sigma_xz).  exact_adjoint=1 applies the sponge in the adjoint. */
+typedef struct rtm_batch rtm_batch;
+rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc,
+                            const float *rho, const float *lambda, const float *mu, int nshots, const int *x0,
+                            const int *nxs, const int *xsrc, const int *zsrc, const int *zrec, int comp_mask,
+                            int group_max, int exact_adjoint);
+/* Migrate shots [shot0, shot0+nshot) (nshot <= group_max).  traces: for
+ * each shot in order, for each selected component, an (nt, nxs) gather in
+ * the reference layout.  image: three (nz,nx) planes (drho, dlambda, dmu)
+ * to which the group's images are added.  *_on_device selects device or
+ * host pointers. */
+int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device, float *image,
+                      int image_on_device);
+/* out[0..6]: forward ms, adjoint ms, cells of the last group, kernels
+ * launched, total ms of the last call, tile width, work items. */
+int rtm_batch_stats(const rtm_batch *b, double *out);
+/* use_graph=0 launches the time loop kernel by kernel. */
+int rtm_batch_set(rtm_batch *b, int use_graph);
+void rtm_batch_destroy(rtm_batch *b);
+/* Page-locked host memory for fast host<->device traces and images. */
+void *rtm_host_alloc(size_t bytes);
+void rtm_host_free(void *p);
 
 #ifdef __cplusplus
 }
