@@ -141,6 +141,9 @@ def run_gpu(args):
     eng = BatchRTM(c["nz"], c["nx"], c["nt"], c["dx"], c["dt"], c["fp"], c["abc"], rho, lam, mu, x0, nxs, xsrc, zs,
                    zr, comp_mask=c["comp_mask"], group_max=args.group, nsource=c["nsource"])
     groups = eng.groups()
+    # autotuner: tile width per pass, timed on the widest group (untimed)
+    widest = max(groups, key=lambda g: int(eng.nxs[g[0]:g[0] + g[1]].sum()))
+    tune = eng.autotune(widest[0], widest[1], steps=args.tune_steps)
     # shard groups over ranks (shots are independent)
     mine = groups[rank::world]
     tmax = max(eng.trace_count(s, n) for s, n in groups)
@@ -244,6 +247,9 @@ def run_gpu(args):
                                "dt=0.5 ms, nt=6000, 64 shots on 600-2000-cell subgrids; one step = one group of "
                                f"{args.group} shots (forward + adjoint with imaging); FP16 source snapshots",
                    "group_shots": args.group, "inputs_vs_l2": "inputs larger than L2 (snapshots ~150 GB)",
+                   "tile": {"forward_tx": tune["tile_x"], "adjoint_tx": tune["tile_x_adj"], "tz": 128,
+                            "autotune_ms_per_launch_fwd_8_16_32": [round(x, 4) for x in tune["tune_ms_fwd"]],
+                            "autotune_ms_per_launch_adj_8_16_32": [round(x, 4) for x in tune["tune_ms_adj"]]},
                    "shots_per_s": round(shots_all / t_dev, 3),
                    "wall_s": round(wall, 3),
                    "fwd_ms_per_step": round(fwd_ms / args.steps, 2),
@@ -337,6 +343,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--group", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--tune-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--nt", type=int, default=None, help="override nt (profiling captures only)")
     ap.add_argument("--shots", type=int, default=None, help="override the shot count (profiling captures only)")

@@ -20,6 +20,7 @@ SIGNATURES = {
     "rtm_last_error": (ctypes.c_char_p, []),
     "rtm_last_status": (_c_int, []),
     "rtm_set_exact": (None, [_c_int]),
+    "rtm_set_kernel_version": (None, [_c_int]),
     "rtm_op3_c_": (None, [_c_int] * 4 + [_P] * 10),
     "rtm_gpu_init": (None, [_c_int] * 3),
     "rtm_gpu_copy_in": (None, [_c_int] * 3 + [_P] * 10),
@@ -43,7 +44,8 @@ SIGNATURES = {
                          + [_P] * 3 + [_c_int] + [_P] * 5 + [_c_int, _c_int, _c_int]),
     "rtm_batch_migrate": (_c_int, [_P, _c_int, _c_int, _P, _c_int, _P, _c_int]),
     "rtm_batch_stats": (_c_int, [_P, _P]),
-    "rtm_batch_set": (_c_int, [_P, _c_int]),
+    "rtm_batch_autotune": (_c_int, [_P, _c_int, _c_int, _c_int]),
+    "rtm_batch_set": (_c_int, [_P, _c_int, _c_int]),
     "rtm_batch_destroy": (None, [_P]),
     "rtm_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "rtm_host_free": (None, [_P]),

@@ -43,13 +43,24 @@ class BatchRTM:
                                        int(image_on_device)))
 
     def stats(self):
-        out = np.zeros(8, np.float64)
+        out = np.zeros(16, np.float64)
         check(load().rtm_batch_stats(self.h, ptr(out)))
         return dict(fwd_ms=out[0], adj_ms=out[1], cells=int(out[2]), kernels=int(out[3]), total_ms=out[4],
-                    tile_x=int(out[5]), work_items=int(out[6]))
+                    tile_x=int(out[5]), work_items=int(out[6]), tile_x_adj=int(out[7]),
+                    tune_ms_fwd=list(out[8:11]), tune_ms_adj=list(out[11:14]))
 
-    def set_graph(self, use_graph):
-        check(load().rtm_batch_set(self.h, 1 if use_graph else 0))
+    def autotune(self, shot0=0, nshot=None, steps=20):
+        """Pick the fastest tile width per pass on the geometry of a group."""
+        nshot = self.group_max if nshot is None else nshot
+        check(load().rtm_batch_autotune(self.h, shot0, nshot, steps))
+        return self.stats()
+
+    def set_graph(self, use_graph, tile_x=0):
+        check(load().rtm_batch_set(self.h, 1 if use_graph else 0, tile_x))
+        self._graph = use_graph
+
+    def set_tile(self, tile_x):
+        check(load().rtm_batch_set(self.h, 1 if getattr(self, "_graph", True) else 0, tile_x))
 
     def close(self):
         if getattr(self, "h", None):

@@ -84,13 +84,17 @@ struct rtm_batch {
     DevBuf<float> model, coefraw, coef, F, A, zero, img, filt, maxes, traces, tstage, full;
     DevBuf<__half> snaps;
     DevBuf<int> dx0;
-    ShotTable tab;
+    ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
+    ShotTable tab_a;  // adjoint pass work items
+    int tx_f = 0, tx_a = 0;          // tile widths chosen by the autotuner (0 = heuristic)
+    double tune_ms[2][3] = {{0}};    // measured ms per step, [pass][tx 8,16,32]
     std::vector<float> dtsrc;
     cudaStream_t st = nullptr;
     double last_fwd_ms = 0, last_adj_ms = 0, last_total_ms = 0;
     long long last_cells = 0;
     int kernels_last = 0;
     bool use_graph = true;
+    int tile_x = 0;  // 0 = automatic
 
     ~rtm_batch()
     {
@@ -100,7 +104,8 @@ struct rtm_batch {
 
 namespace {
 
-int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_dev, float *image, int image_dev)
+int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_dev, float *image, int image_dev,
+                int tune_steps = 0)
 {
     RTM_CHECK_ARG(s0 >= 0 && ns >= 1 && s0 + ns <= (int)b->x0.size() && ns <= b->group_max, "bad shot range");
     {
@@ -137,7 +142,19 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     }
     RTM_CHECK_ARG(col <= b->cap_cols, "group wider than the batch capacity");
     b->tab.ldz = ld;
-    TRY(b->tab.build(pick_tile_width((long long)nz, col)));
+    const int tz = kernel_version() == 1 ? TZ_TILE : TZ_TILE2;  // batch planes are always v2-aligned
+    {
+        const int heur = pick_tile_width((long long)nz, col, tz);
+        int heur_a = heur;
+        while (tz == TZ_TILE2 && heur_a > 8 && !v2_fits(true, false, heur_a)) heur_a /= 2;
+        const int txf = b->tile_x > 0 ? b->tile_x : (b->tx_f > 0 ? b->tx_f : heur);
+        int txa = b->tile_x > 0 ? b->tile_x : (b->tx_a > 0 ? b->tx_a : heur_a);
+        while (tz == TZ_TILE2 && txa > 8 && !v2_fits(true, false, txa)) txa /= 2;
+        TRY(b->tab.build(txf, tz));
+        b->tab_a.shots = b->tab.shots;
+        b->tab_a.ldz = ld;
+        TRY(b->tab_a.build(txa, tz));
+    }
     RTM_CUDA(cudaMemcpyAsync(b->dx0.p, x0g.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
     const long long gp = b->gplane;
     // ---- coefficients of every shot's subgrid
@@ -179,13 +196,14 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     auto mx = [&](int L) { return b->maxes.p + (size_t)L * b->group_max * 2; };
     const float inv_dt = 1.0f / b->dt, inv_dx = 1.0f / b->dx;
 
-    auto base_args = [&]() {
+    auto base_args = [&](bool adj) {
+        const ShotTable &tb = adj ? b->tab_a : b->tab;
         Step2DArgs<float> a;
         memset(&a, 0, sizeof a);
         for (int k = 0; k < 5; k++) a.coef[k] = b->coef.p + k * gp;
-        a.shots = b->tab.d_geom;
+        a.shots = tb.d_geom;
         a.nshots = ns;
-        a.ntiles = b->tab.ntiles;
+        a.ntiles = tb.ntiles;
         a.ldz = ld;
         a.filt = b->filt.p;
         a.abc2 = b->abc + 5;
@@ -195,11 +213,67 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     };
     // initialise launch configuration outside any capture
     {
-        Step2DArgs<float> a = base_args();
+        Step2DArgs<float> a = base_args(false);
         a.ntiles = 0;
-        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st));
+        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz));
         a.img[0] = b->img.p;
-        TRY(launch_step<float>(a, true, false, b->tab.tx, 0, st));
+        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz));
+    }
+
+    if (tune_steps > 0) {
+        // Autotuner: time `tune_steps` launches of each pass for every tile
+        // width on this group's geometry and keep the fastest per pass.
+        cudaEvent_t t0, t1;
+        RTM_CUDA(cudaEventCreate(&t0));
+        RTM_CUDA(cudaEventCreate(&t1));
+        const int cand[3] = {8, 16, 32};
+        for (int pass = 0; pass < 2; pass++) {
+            double best = 1e30;
+            int bx = cand[0];
+            for (int ci = 0; ci < 3; ci++) {
+                if (tz == TZ_TILE2 && !v2_fits(pass == 1, false, cand[ci])) {
+                    b->tune_ms[pass][ci] = -1;  // does not fit in shared memory
+                    continue;
+                }
+                ShotTable &tb = pass ? b->tab_a : b->tab;
+                TRY(tb.build(cand[ci], tz));
+                for (int rep = 0; rep < 2; rep++) {  // first round warms up
+                    RTM_CUDA(cudaEventRecord(t0, st));
+                    for (int k = 0; k < tune_steps; k++) {
+                        const int L = 3 + (k & 1);
+                        Step2DArgs<float> a = base_args(pass == 1);
+                        for (int f = 0; f < 5; f++) {
+                            a.out[f] = pass ? ab(L & 1, f) : fb(L & 1, f);
+                            a.own2[f] = a.out[f];
+                            a.nb[f] = pass ? ab((L + 1) & 1, f) : fb((L + 1) & 1, f);
+                        }
+                        if (!pass) {
+                            a.sponge = 1;
+                            a.snap_out[0] = snap(1, 0);
+                            a.snap_out[1] = snap(1, 1);
+                            a.snap_max_in = mx(1);
+                            a.snap_max_out = mx(2);
+                        } else {
+                            a.rec = b->traces.p; a.comp_mask = b->comp_mask; a.ncomp = b->ncomp; a.it = 0;
+                            a.isnap0[0] = snap(1, 0); a.isnap0[1] = snap(1, 1); a.imax0 = mx(1);
+                            a.isnap1[0] = snap(2, 0); a.isnap1[1] = snap(2, 1); a.imax1 = mx(2);
+                            for (int i = 0; i < 3; i++) { a.img[i] = b->img.p + i * gp; a.imgc[i] = b->img.p + (3 + i) * gp; }
+                        }
+                        TRY(launch_step<float>(a, pass == 1, false, tb.tx, 0, st, tb.tz));
+                    }
+                    RTM_CUDA(cudaEventRecord(t1, st));
+                    RTM_CUDA(cudaEventSynchronize(t1));
+                }
+                float ms = 0;
+                RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+                b->tune_ms[pass][ci] = ms / tune_steps;
+                if (ms < best) { best = ms; bx = cand[ci]; }
+            }
+            if (pass) b->tx_a = bx; else b->tx_f = bx;
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        return RTM_OK;
     }
 
     cudaEvent_t e0, e1, e2;
@@ -211,7 +285,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     // of the last level
     auto record_fwd = [&]() -> int {
         for (int L = 2; L <= nt; L++) {
-            Step2DArgs<float> a = base_args();
+            Step2DArgs<float> a = base_args(false);
             for (int f = 0; f < 5; f++) {
                 a.out[f] = fb(L & 1, f);
                 a.own2[f] = fb(L & 1, f);
@@ -224,7 +298,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.snap_out[1] = snap(L - 1, 1);
             a.snap_max_in = mx(L - 1);
             a.snap_max_out = mx(L);
-            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st));
+            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz));
             nkern++;
         }
         dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
@@ -236,7 +310,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     // ---- adjoint pass with the imaging condition: levels nt..1
     auto record_adj = [&]() -> int {
         for (int L = nt; L >= 1; L--) {
-            Step2DArgs<float> a = base_args();
+            Step2DArgs<float> a = base_args(true);
             for (int f = 0; f < 5; f++) {
                 a.out[f] = ab(L & 1, f);
                 a.own2[f] = L + 2 <= nt ? ab(L & 1, f) : b->zero.p;
@@ -258,7 +332,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                 a.img[i] = b->img.p + i * gp;
                 a.imgc[i] = b->img.p + (3 + i) * gp;
             }
-            TRY(launch_step<float>(a, true, false, b->tab.tx, 0, st));
+            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz));
             nkern++;
         }
         return RTM_OK;
@@ -469,15 +543,32 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[2] = (double)b->last_cells;
     out[3] = (double)b->kernels_last;
     out[4] = b->last_total_ms;
-    out[5] = (double)b->tab.tx;
+    out[5] = (double)(b->tx_f > 0 ? b->tx_f : b->tab.tx);
     out[6] = (double)b->tab.ntiles;
+    out[7] = (double)(b->tx_a > 0 ? b->tx_a : b->tab_a.tx);
+    for (int p = 0; p < 2; p++)
+        for (int i = 0; i < 3; i++) out[8 + 3 * p + i] = b->tune_ms[p][i];
     return RTM_OK;
 }
 
-extern "C" int rtm_batch_set(rtm_batch *b, int use_graph)
+extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
 {
     RTM_CHECK_ARG(b, "null argument");
+    RTM_CHECK_ARG(tile_x == 0 || tile_x == 8 || tile_x == 16 || tile_x == 32, "tile_x must be 0, 8, 16 or 32");
     b->use_graph = use_graph != 0;
+    b->tile_x = tile_x;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
+{
+    RTM_CHECK_ARG(b && steps > 0, "bad arguments");
+    TRY(ensure_device());
+    b->tx_f = b->tx_a = 0;
+    // traces are not read during tuning beyond the receiver row; use the
+    // staging buffer content as is
+    TRY(batch_group(b, shot0, nshot, b->tstage.p, 1, b->full.p, 1, steps));
+    RTM_CUDA(cudaStreamSynchronize(b->st));
     return RTM_OK;
 }
 

@@ -17,10 +17,13 @@ enum RtmStatus {
 
 void rtm_set_error(const char *fmt, ...);
 
+// On failure the runtime's last-error slot is cleared as well, so that one
+// failed call is reported once and not again by the next check.
 #define RTM_CUDA(call)                                                                     \
     do {                                                                                   \
         cudaError_t e_ = (call);                                                           \
         if (e_ != cudaSuccess) {                                                           \
+            cudaGetLastError();                                                            \
             rtm_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
             return RTM_ERR_CUDA;                                                           \
         }                                                                                  \

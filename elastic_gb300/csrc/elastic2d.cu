@@ -3,11 +3,14 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <cstdint>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/elastic_rtm.h"
 #include "elastic2d.cuh"
 #include "elastic2d_aux.cuh"
+#include "elastic2d_v2.cuh"
 #include "engine.h"
 
 using namespace eg;
@@ -27,6 +30,9 @@ void rtm_set_error(const char *fmt, ...)
 extern "C" const char *rtm_last_error(void) { return g_err; }
 extern "C" int rtm_last_status(void) { return g_last_status; }
 extern "C" void rtm_set_exact(int exact) { g_exact = exact ? 1 : 0; }
+static int g_kernel_version = 0;
+extern "C" void rtm_set_kernel_version(int v) { g_kernel_version = (v == 1 || v == 2) ? v : 0; }
+int eg::kernel_version() { return g_kernel_version; }
 
 namespace eg {
 
@@ -87,19 +93,107 @@ static int launch_step_e(const Step2DArgs<T> &a, int tx, int grid_cap, cudaStrea
     }
 }
 
-template <typename T>
-int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st)
+int max_smem_optin()
 {
+    static int v = 0;
+    if (!v) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (v <= 0) v = 48 * 1024;
+    }
+    return v;
+}
+
+bool v2_fits(bool adj, bool exact, int tx)
+{
+    size_t need = 0;
+    switch (tx) {
+    case 8: need = adj ? (exact ? v2_smem<true, true, 8>(true) : v2_smem<true, false, 8>(true)) : v2_smem<false, false, 8>(false); break;
+    case 16: need = adj ? (exact ? v2_smem<true, true, 16>(true) : v2_smem<true, false, 16>(true)) : v2_smem<false, false, 16>(false); break;
+    case 32: need = adj ? (exact ? v2_smem<true, true, 32>(true) : v2_smem<true, false, 32>(true)) : v2_smem<false, false, 32>(false); break;
+    default: return false;
+    }
+    return need <= (size_t)max_smem_optin();
+}
+
+template <bool EXACT, bool ADJ, int TX>
+static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t st)
+{
+    auto kern = k_step2d_v2<EXACT, ADJ, TX>;
+    const bool img = ADJ && a.img[0] != nullptr;
+    const size_t smem = v2_smem<ADJ, EXACT, TX>(img);
+    RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX), "tile width %d needs more shared memory than a block can use", TX);
+    static int grid_max[2] = {0, 0};
+    if (!grid_max[img]) {
+        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v2_smem<ADJ, EXACT, TX>(true)));
+        int nb = 0;
+        RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
+        grid_max[img] = (nb > 0 ? nb : 1) * device_sm_count();
+    }
+    int grid = a.ntiles < grid_max[img] ? a.ntiles : grid_max[img];
+    if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
+    if (grid <= 0) return RTM_OK;
+    kern<<<grid, 256, smem, st>>>(a);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+template <bool EXACT, bool ADJ>
+static int launch_v2(const Step2DArgs<float> &a, int tx, int grid_cap, cudaStream_t st)
+{
+    switch (tx) {
+    case 8: return launch_v2_tx<EXACT, ADJ, 8>(a, grid_cap, st);
+    case 16: return launch_v2_tx<EXACT, ADJ, 16>(a, grid_cap, st);
+    case 32: return launch_v2_tx<EXACT, ADJ, 32>(a, grid_cap, st);
+    default: rtm_set_error("unsupported tile width %d", tx); return RTM_ERR_ARG;
+    }
+}
+
+// v2 needs float planes whose columns start on 16-byte boundaries.
+static bool v2_layout_ok(const Step2DArgs<float> &a)
+{
+    if (a.ldz % 4) return false;
+    auto al = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+    for (int f = 0; f < 5; f++) {
+        if (!al(a.out[f]) || !al(a.own2[f]) || !al(a.nb[f]) || !al(a.coef[f])) return false;
+        if (a.inplane[f] && !al(a.inplane[f])) return false;
+    }
+    return true;
+}
+
+bool v2_usable(bool is_float, int ldz, const void *const *ptrs, int n)
+{
+    if (!is_float || kernel_version() == 1 || ldz % 4) return false;
+    for (int i = 0; i < n; i++)
+        if (ptrs[i] && ((uintptr_t)ptrs[i] & 15u)) return false;
+    return true;
+}
+
+template <typename T>
+int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        if (tz == TZ_TILE2) {
+            if (!v2_layout_ok(a)) {
+                rtm_set_error("v2 step launched on an unaligned layout");
+                return RTM_ERR_ARG;
+            }
+            if (adj) return exact ? launch_v2<true, true>(a, tx, grid_cap, st) : launch_v2<false, true>(a, tx, grid_cap, st);
+            return exact ? launch_v2<true, false>(a, tx, grid_cap, st) : launch_v2<false, false>(a, tx, grid_cap, st);
+        }
+    }
     if (adj) return exact ? launch_step_e<T, true, true>(a, tx, grid_cap, st) : launch_step_e<T, false, true>(a, tx, grid_cap, st);
     return exact ? launch_step_e<T, true, false>(a, tx, grid_cap, st) : launch_step_e<T, false, false>(a, tx, grid_cap, st);
 }
-template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t);
-template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t);
+template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t, int);
+template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t, int);
 
 // ------------------------------------------------------------- batch table
-int ShotTable::build(int tx_)
+int ShotTable::build(int tx_, int tz_)
 {
     tx = tx_;
+    tz = tz_;
     std::vector<ShotGeom> g(shots.size());
     int t = 0;
     for (size_t s = 0; s < shots.size(); s++) {
@@ -112,7 +206,7 @@ int ShotTable::build(int tx_)
         g[s].src_ix = h.src_ix;
         g[s].rec_iz = h.rec_iz;
         g[s].tile0 = t;
-        g[s].ntz = ceil_div(h.nz, TZ_TILE);
+        g[s].ntz = ceil_div(h.nz, tz);
         g[s].pad = 0;
         t += g[s].ntz * ceil_div(h.nx, tx);
     }
@@ -231,7 +325,13 @@ struct Hist {
         RTM_CUDA(cudaMemset(zero.p, 0, plane * sizeof(T)));
         tab.shots.assign(1, HostShot{0, 0, nz, nx, -1, -1, -1});
         tab.ldz = nz;
-        TRY(tab.build(pick_tile_width(nz, nx)));
+        // v2 when every level of every history starts on a 16-byte boundary
+        // (cudaMalloc bases, plane = nz*nx floats)
+        const bool v2 = kernel_version() != 1 && std::is_same<T, float>::value && nz % 4 == 0 && (plane % 4) == 0;
+        const int tz = v2 ? TZ_TILE2 : TZ_TILE;
+        int tx = pick_tile_width(nz, nx, tz);
+        while (v2 && tx > 8 && !v2_fits(true, exact, tx)) tx /= 2;
+        TRY(tab.build(tx, tz));
         return RTM_OK;
     }
     // coefficient planes (unmasked, device) -> masked planes
@@ -276,7 +376,7 @@ struct Hist {
         return a;
     }
     T *lev(T *h, int L) const { return h + (size_t)(L - 1) * plane; }  // 1-based level
-    int step(const Step2DArgs<T> &a, bool adj) { return launch_step<T>(a, adj, exact, tab.tx, 0, st); }
+    int step(const Step2DArgs<T> &a, bool adj) { return launch_step<T>(a, adj, exact, tab.tx, 0, st, tab.tz); }
 
     // Source wavefield, W/rtm-mod-adj.f90:178-261.  src[] = dt*source(it).
     int forward(T *const H[5], const std::vector<T> &dtsrc, int zsrc0, int xsrc0)
@@ -285,7 +385,7 @@ struct Hist {
         ShotTable &tb = tab;
         tb.shots[0].src_iz = zsrc0;
         tb.shots[0].src_ix = xsrc0;
-        TRY(tb.build(tb.tx));
+        TRY(tb.build(tb.tx, tb.tz));
         for (int L = 2; L <= nt; L++) {
             Step2DArgs<T> a = args();
             for (int f = 0; f < 5; f++) {
@@ -299,7 +399,7 @@ struct Hist {
             TRY(step(a, false));
         }
         tb.shots[0].src_iz = tb.shots[0].src_ix = -1;
-        return tb.build(tb.tx);
+        return tb.build(tb.tx, tb.tz);
     }
 
     // Born scattered loop (W/rtm-mod-adj.f90:291-357) on histories already
@@ -309,7 +409,7 @@ struct Hist {
     {
         tab.shots[0].rec_iz = zrec0;
         tab.shots[0].doff = 0;
-        TRY(tab.build(tab.tx));
+        TRY(tab.build(tab.tx, tab.tz));
         for (int L = 1; L <= nt; L++) {
             Step2DArgs<T> a = args();
             for (int f = 0; f < 5; f++) {
@@ -326,7 +426,7 @@ struct Hist {
             TRY(step(a, false));
         }
         tab.shots[0].rec_iz = -1;
-        return tab.build(tab.tx);
+        return tab.build(tab.tx, tab.tz);
     }
 
     // rtm_op3 (W/rtmlib-mod.f90:72-196) + the C recursion: H holds the
@@ -778,7 +878,13 @@ int dropin_run(int it_max, int nt, int nz, int nx, int ldz, size_t pstride, floa
     TRY(ensure_device());
     h.tab.shots.assign(1, HostShot{0, 0, nz, nx, -1, -1, -1});
     h.tab.ldz = ldz;
-    TRY(h.tab.build(pick_tile_width(nz, nx)));
+    const void *ptrs[10];
+    for (int f = 0; f < 5; f++) { ptrs[f] = base[f]; ptrs[5 + f] = cm[f]; }
+    const bool v2 = v2_usable(true, ldz, ptrs, 10) && (pstride % 4) == 0;
+    const int tz = v2 ? TZ_TILE2 : TZ_TILE;
+    int tx = pick_tile_width(nz, nx, tz);
+    while (v2 && tx > 8 && !v2_fits(true, h.exact, tx)) tx /= 2;
+    TRY(h.tab.build(tx, tz));
     for (int i = 0; i < 5; i++) h.cmp[i] = cm[i];
     cudaEvent_t e0, e1;
     RTM_CUDA(cudaEventCreate(&e0));

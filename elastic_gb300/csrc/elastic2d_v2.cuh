@@ -1,0 +1,504 @@
+// Fused 2D elastic step, version 2 (float, 16-byte aligned layouts).
+//
+// Same per-cell arithmetic as k_step2d (elastic2d.cuh) -- in EXACT mode the
+// results are bit-identical -- with a staging and compute layout built for
+// sm_103a's memory system:
+//  * a tile is 128 z-rows x TX columns; its neighbour level (and, for the
+//    adjoint, the coefficients and the FP16 source snapshots) is staged with
+//    an 8-row aligned z halo and a 5-column x halo by cp.async (16-byte
+//    chunks, hardware zero-fill outside the shot), so every byte of the tile
+//    is in flight at once instead of being loaded through registers;
+//  * each thread owns 4 consecutive z cells of TX/8 columns: x-stencils read
+//    one 128-bit shared word per tap, z-stencils read a 20-value window in
+//    five 128-bit words, own/coefficient/output traffic is float4.
+// Requirements (checked by the launcher): ldz % 4 == 0, 16-byte aligned
+// planes, rows [nz, ldz) of staged planes zero.
+#pragma once
+#include "elastic2d.cuh"
+
+namespace eg {
+
+constexpr int V2_TZ = 128;              // tile rows (32 lanes x 4)
+constexpr int V2_ZH = 8;                // aligned z halo
+constexpr int V2_LZ = V2_TZ + 2 * V2_ZH;  // staged rows per column (144)
+
+template <int TX>
+struct V2 {
+    static constexpr int LX = TX + 2 * HALO;        // staged columns
+    static constexpr int SIZE = V2_LZ * LX;         // floats per staged array
+    static constexpr int CHUNKS = (V2_LZ / 4) * LX; // 16-byte chunks per array
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem, bool valid)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = valid ? 8 : 0;
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
+// 4 consecutive floats of array `arr` at local column x (tile coords, may be
+// -5..TX+4) and local row z (multiple of 4, may be -8..V2_TZ+4).
+template <int TX>
+__device__ __forceinline__ float4 lds4(const float *sm, int arr, int x, int z)
+{
+    return *reinterpret_cast<const float4 *>(sm + arr * V2<TX>::SIZE + (x + HALO) * V2_LZ + (z + V2_ZH));
+}
+__device__ __forceinline__ float f4(const float4 &v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+
+// 20-value z window rows z-8 .. z+11 of array `arr` at column x.
+template <int TX>
+__device__ __forceinline__ void zwin(const float *sm, int arr, int x, int z, float w[20])
+{
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+        const float4 v = lds4<TX>(sm, arr, x, z - 8 + 4 * q);
+        w[4 * q] = v.x; w[4 * q + 1] = v.y; w[4 * q + 2] = v.z; w[4 * q + 3] = v.w;
+    }
+}
+
+// Forward staggered difference for 4 outputs (rows z..z+3) at column x.
+// Along x: taps are float4 reads at columns x+hi / x+lo.  Along z: from the
+// window w (w[8+j+o] is the value at row z+j+o).
+template <bool EXACT, int TX, bool PTYPE>
+__device__ __forceinline__ void fwd_poly_x4(const float *sm, int arr, int x, int z, float p[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int hi = PTYPE ? 5 - k : 4 - k, lo = PTYPE ? -4 + k : -5 + k;
+        const float4 va = lds4<TX>(sm, arr, x + hi, z), vb = lds4<TX>(sm, arr, x + lo, z);
+        const float c = StagCoef<float>::c(k);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float t = Ar<EXACT>::mul(c, Ar<EXACT>::sub(f4(va, j), f4(vb, j)));
+            p[j] = k == 0 ? t : Ar<EXACT>::add(p[j], t);
+        }
+    }
+}
+template <bool EXACT, bool PTYPE>
+__device__ __forceinline__ void fwd_poly_z4(const float w[20], float p[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int hi = PTYPE ? 5 - k : 4 - k, lo = PTYPE ? -4 + k : -5 + k;
+        const float c = StagCoef<float>::c(k);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float t = Ar<EXACT>::mul(c, Ar<EXACT>::sub(w[8 + j + hi], w[8 + j + lo]));
+            p[j] = k == 0 ? t : Ar<EXACT>::add(p[j], t);
+        }
+    }
+}
+
+// Adjoint gathers for 4 outputs.  Exact: terms (coef*c_k)*field in the
+// reference order (M5: +c_k at -5+k for k=0..4, then -c_k at +4-k for
+// k=4..0; P5: +c_k at -4+k, then -c_k at +5-k).  Fast: products array.
+template <int TX, bool PTYPE>
+__device__ __forceinline__ void adj_exact_x4(const float *sm, int ca, int fa, int x, int z, float v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int o = PTYPE ? -4 + k : -5 + k;
+        const float4 c4 = lds4<TX>(sm, ca, x + o, z), f = lds4<TX>(sm, fa, x + o, z);
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = add_rn(v[j], mul_rn(mul_rn(f4(c4, j), StagCoef<float>::c(k)), f4(f, j)));
+    }
+#pragma unroll
+    for (int k = 4; k >= 0; k--) {
+        const int o = PTYPE ? 5 - k : 4 - k;
+        const float4 c4 = lds4<TX>(sm, ca, x + o, z), f = lds4<TX>(sm, fa, x + o, z);
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = sub_rn(v[j], mul_rn(mul_rn(f4(c4, j), StagCoef<float>::c(k)), f4(f, j)));
+    }
+}
+template <bool PTYPE>
+__device__ __forceinline__ void adj_exact_z4(const float cw[20], const float fw[20], float v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int o = PTYPE ? -4 + k : -5 + k;
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = add_rn(v[j], mul_rn(mul_rn(cw[8 + j + o], StagCoef<float>::c(k)), fw[8 + j + o]));
+    }
+#pragma unroll
+    for (int k = 4; k >= 0; k--) {
+        const int o = PTYPE ? 5 - k : 4 - k;
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = sub_rn(v[j], mul_rn(mul_rn(cw[8 + j + o], StagCoef<float>::c(k)), fw[8 + j + o]));
+    }
+}
+template <int TX, bool PTYPE>
+__device__ __forceinline__ void adj_fast_x4(const float *sm, int pa, int x, int z, float v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int op = PTYPE ? -4 + k : -5 + k, om = PTYPE ? 5 - k : 4 - k;
+        const float4 a = lds4<TX>(sm, pa, x + op, z), b = lds4<TX>(sm, pa, x + om, z);
+        const float c = StagCoef<float>::c(k);
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = v[j] + c * (f4(a, j) - f4(b, j));
+    }
+}
+template <bool PTYPE>
+__device__ __forceinline__ void adj_fast_z4(const float w[20], float v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int op = PTYPE ? -4 + k : -5 + k, om = PTYPE ? 5 - k : 4 - k;
+        const float c = StagCoef<float>::c(k);
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = v[j] + c * (w[8 + j + op] - w[8 + j + om]);
+    }
+}
+
+template <bool ADJ, bool EXACT>
+struct V2Arr {
+    static constexpr int NRAW = ADJ ? 10 : 5;  // staged float arrays
+};
+
+// Shared memory of a v2 launch: NRAW float arrays (+ 2 FP16 snapshot arrays
+// for fused imaging, stored as halves).
+template <bool ADJ, bool EXACT, int TX>
+constexpr size_t v2_smem(bool img)
+{
+    return (size_t)V2Arr<ADJ, EXACT>::NRAW * V2<TX>::SIZE * sizeof(float) +
+           (ADJ && img ? (size_t)2 * V2<TX>::SIZE * sizeof(__half) : 0);
+}
+
+template <typename V>
+__device__ __forceinline__ float4 ld_f4(const V *p) { return *reinterpret_cast<const float4 *>(p); }
+
+template <bool EXACT, bool ADJ, int TX>
+__global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2DArgs<float> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *sm = reinterpret_cast<float *>(smem_raw);
+    constexpr int NRAW = V2Arr<ADJ, EXACT>::NRAW;
+    constexpr int SZ = V2<TX>::SIZE;
+    constexpr int CW = TX / 8;  // columns per warp
+    __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool img = ADJ && a.img[0] != nullptr;
+
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int s = find_shot<float>(a.shots, a.nshots, t);
+        const ShotGeom g = a.shots[s];
+        const int lt = t - g.tile0;
+        const int tz0 = (lt % g.ntz) * V2_TZ, tx0 = (lt / g.ntz) * TX;
+        const long long off = g.off;
+        const int nz = g.nz, nx = g.nx, ldz = a.ldz;
+
+        __syncthreads();  // previous tile consumed
+        // ---- asynchronous staging
+        for (int c = threadIdx.x; c < V2<TX>::CHUNKS; c += blockDim.x) {
+            const int col = c / (V2_LZ / 4), zc = c - col * (V2_LZ / 4);
+            const int gx = tx0 - HALO + col, gz = tz0 - V2_ZH + 4 * zc;
+            const bool ok = (gx >= 0) & (gx < nx) & (gz >= 0) & (gz < ldz);
+            const long long o = ok ? off + (long long)gx * ldz + gz : 0;
+            const int so = col * V2_LZ + 4 * zc;
+#pragma unroll
+            for (int f = 0; f < 5; f++) cp_async16(sm + f * SZ + so, a.nb[f] + o, ok);
+            if (ADJ) {
+#pragma unroll
+                for (int f = 0; f < 5; f++) cp_async16(sm + (5 + f) * SZ + so, a.coef[f] + o, ok);
+                if (img) {
+                    const bool oks = ok & (gz < nz);
+                    cp_async8(smh + so, a.isnap0[0] + o, oks);
+                    cp_async8(smh + SZ + so, a.isnap0[1] + o, oks);
+                }
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        if (ADJ && !EXACT) {
+            // products coef*field in place (slots 0..6 of the 10 raw arrays)
+            for (int e = threadIdx.x; e < SZ; e += blockDim.x) {
+                float fv[5], cv[5];
+#pragma unroll
+                for (int f = 0; f < 5; f++) { fv[f] = sm[f * SZ + e]; cv[f] = sm[(5 + f) * SZ + e]; }
+                sm[P_A23XX * SZ + e] = cv[A23] * fv[SXX];
+                sm[P_A2ZZ * SZ + e] = cv[A2] * fv[SZZ];
+                sm[P_A3XZ * SZ + e] = cv[A3] * fv[SXZ];
+                sm[P_A2XX * SZ + e] = cv[A2] * fv[SXX];
+                sm[P_A23ZZ * SZ + e] = cv[A23] * fv[SZZ];
+                sm[P_M1XVX * SZ + e] = cv[M1X] * fv[VX];
+                sm[P_M1ZVZ * SZ + e] = cv[M1Z] * fv[VZ];
+            }
+            __syncthreads();
+        }
+
+        float wmax0 = 0.f, wmax1 = 0.f;
+        const int z = 4 * lane;  // local row of this thread's 4 cells
+        const int gz = tz0 + z;
+#pragma unroll 1
+        for (int r = 0; r < CW; r++) {
+            const int x = warp * CW + r, gx = tx0 + x;
+            if (gx >= nx || gz >= nz) continue;
+            const long long o = off + (long long)gx * ldz + gz;
+            const int nval = min(4, nz - gz);  // rows of this group inside the shot
+            float v[5][4];
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                const float4 b = ld_f4(a.own2[f] + o);
+                v[f][0] = b.x; v[f][1] = b.y; v[f][2] = b.z; v[f][3] = b.w;
+                if (a.inplane[f]) {
+                    const float4 q = ld_f4(a.inplane[f] + o);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) v[f][j] = Ar<EXACT>::add(f4(q, j), v[f][j]);
+                }
+            }
+            if (!ADJ) {
+                if (a.has_src && gx == g.src_ix && g.src_iz >= gz && g.src_iz < gz + 4) {
+                    const int j = g.src_iz - gz;
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++)
+                        if (jj == j) {
+                            v[SXX][jj] = Ar<EXACT>::add(v[SXX][jj], a.srcval);
+                            v[SZZ][jj] = Ar<EXACT>::add(v[SZZ][jj], a.srcval);
+                        }
+                }
+                const float4 cm1x = __ldg(reinterpret_cast<const float4 *>(a.coef[M1X] + o));
+                const float4 cm1z = __ldg(reinterpret_cast<const float4 *>(a.coef[M1Z] + o));
+                const float4 ca2 = __ldg(reinterpret_cast<const float4 *>(a.coef[A2] + o));
+                const float4 ca3 = __ldg(reinterpret_cast<const float4 *>(a.coef[A3] + o));
+                const float4 ca23 = __ldg(reinterpret_cast<const float4 *>(a.coef[A23] + o));
+                float p[4], w[20];
+                // Vx: Ax (x, M, sxx) then Bx (z, P, sxz)
+                fwd_poly_x4<EXACT, TX, false>(sm, SXX, x, z, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[VX][j] = Ar<EXACT>::add(v[VX][j], Ar<EXACT>::mul(f4(cm1x, j), p[j]));
+                zwin<TX>(sm, SXZ, x, z, w);
+                fwd_poly_z4<EXACT, true>(w, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[VX][j] = Ar<EXACT>::add(v[VX][j], Ar<EXACT>::mul(f4(cm1x, j), p[j]));
+                // Vz: Az (x, P, sxz) then Bz (z, M, szz)
+                fwd_poly_x4<EXACT, TX, true>(sm, SXZ, x, z, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[VZ][j] = Ar<EXACT>::add(v[VZ][j], Ar<EXACT>::mul(f4(cm1z, j), p[j]));
+                zwin<TX>(sm, SZZ, x, z, w);
+                fwd_poly_z4<EXACT, false>(w, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[VZ][j] = Ar<EXACT>::add(v[VZ][j], Ar<EXACT>::mul(f4(cm1z, j), p[j]));
+                // sxx: D (x, P, vx) with a23, szz: F (same poly) with a2
+                fwd_poly_x4<EXACT, TX, true>(sm, VX, x, z, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    v[SXX][j] = Ar<EXACT>::add(v[SXX][j], Ar<EXACT>::mul(f4(ca23, j), p[j]));
+                    v[SZZ][j] = Ar<EXACT>::add(v[SZZ][j], Ar<EXACT>::mul(f4(ca2, j), p[j]));
+                }
+                // sxx: E (z, P, vz) with a2, szz: G (same poly) with a23
+                zwin<TX>(sm, VZ, x, z, w);
+                fwd_poly_z4<EXACT, true>(w, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    v[SXX][j] = Ar<EXACT>::add(v[SXX][j], Ar<EXACT>::mul(f4(ca2, j), p[j]));
+                    v[SZZ][j] = Ar<EXACT>::add(v[SZZ][j], Ar<EXACT>::mul(f4(ca23, j), p[j]));
+                }
+                // sxz: H (z, M, vx) then J (x, M, vz), both with a3
+                zwin<TX>(sm, VX, x, z, w);
+                fwd_poly_z4<EXACT, false>(w, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[SXZ][j] = Ar<EXACT>::add(v[SXZ][j], Ar<EXACT>::mul(f4(ca3, j), p[j]));
+                fwd_poly_x4<EXACT, TX, false>(sm, VZ, x, z, p);
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[SXZ][j] = Ar<EXACT>::add(v[SXZ][j], Ar<EXACT>::mul(f4(ca3, j), p[j]));
+            } else {
+                if (a.rec && g.rec_iz >= gz && g.rec_iz < gz + 4) {
+                    const int j = g.rec_iz - gz;
+                    int slot = 0;
+#pragma unroll
+                    for (int f = 0; f < 5; f++)
+                        if (a.comp_mask & (1 << f)) {
+                            const float d = a.rec[g.doff + ((long long)a.it * a.ncomp + slot) * nx + gx];
+#pragma unroll
+                            for (int jj = 0; jj < 4; jj++)
+                                if (jj == j) v[f][jj] = Ar<EXACT>::add(d, v[f][jj]);
+                            slot++;
+                        }
+                }
+                if (EXACT) {
+                    float cw[20], fw[20];
+                    adj_exact_x4<TX, false>(sm, 5 + A23, SXX, x, z, v[VX]);
+                    adj_exact_x4<TX, false>(sm, 5 + A2, SZZ, x, z, v[VX]);
+                    zwin<TX>(sm, 5 + A3, x, z, cw); zwin<TX>(sm, SXZ, x, z, fw);
+                    adj_exact_z4<true>(cw, fw, v[VX]);
+                    zwin<TX>(sm, 5 + A2, x, z, cw); zwin<TX>(sm, SXX, x, z, fw);
+                    adj_exact_z4<false>(cw, fw, v[VZ]);
+                    zwin<TX>(sm, 5 + A23, x, z, cw); zwin<TX>(sm, SZZ, x, z, fw);
+                    adj_exact_z4<false>(cw, fw, v[VZ]);
+                    adj_exact_x4<TX, true>(sm, 5 + A3, SXZ, x, z, v[VZ]);
+                    adj_exact_x4<TX, true>(sm, 5 + M1X, VX, x, z, v[SXX]);
+                    zwin<TX>(sm, 5 + M1Z, x, z, cw); zwin<TX>(sm, VZ, x, z, fw);
+                    adj_exact_z4<true>(cw, fw, v[SZZ]);
+                    zwin<TX>(sm, 5 + M1X, x, z, cw); zwin<TX>(sm, VX, x, z, fw);
+                    adj_exact_z4<false>(cw, fw, v[SXZ]);
+                    adj_exact_x4<TX, false>(sm, 5 + M1Z, VZ, x, z, v[SXZ]);
+                } else {
+                    float w[20];
+                    adj_fast_x4<TX, false>(sm, P_A23XX, x, z, v[VX]);
+                    adj_fast_x4<TX, false>(sm, P_A2ZZ, x, z, v[VX]);
+                    zwin<TX>(sm, P_A3XZ, x, z, w);
+                    adj_fast_z4<true>(w, v[VX]);
+                    adj_fast_x4<TX, true>(sm, P_A3XZ, x, z, v[VZ]);
+                    zwin<TX>(sm, P_A2XX, x, z, w);
+                    adj_fast_z4<false>(w, v[VZ]);
+                    zwin<TX>(sm, P_A23ZZ, x, z, w);
+                    adj_fast_z4<false>(w, v[VZ]);
+                    adj_fast_x4<TX, true>(sm, P_M1XVX, x, z, v[SXX]);
+                    zwin<TX>(sm, P_M1ZVZ, x, z, w);
+                    adj_fast_z4<true>(w, v[SZZ]);
+                    zwin<TX>(sm, P_M1XVX, x, z, w);
+                    adj_fast_z4<false>(w, v[SXZ]);
+                    adj_fast_x4<TX, false>(sm, P_M1ZVZ, x, z, v[SXZ]);
+                }
+            }
+            if (a.sponge) {
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) v[f][j] = sponge_cell<EXACT>(v[f][j], gz + j, gx, nz, nx, a.filt, a.abc2);
+            }
+            // ---- stores (rows >= nz are never written)
+            if (nval == 4) {
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    *reinterpret_cast<float4 *>(a.out[f] + o) = make_float4(v[f][0], v[f][1], v[f][2], v[f][3]);
+            } else {
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    for (int j = 0; j < nval; j++) a.out[f][o + j] = v[f][j];
+            }
+            if (!ADJ && a.rec && g.rec_iz >= gz && g.rec_iz < gz + 4) {
+                const int j = g.rec_iz - gz;
+                int slot = 0;
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    if (a.comp_mask & (1 << f)) {
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++)
+                            if (jj == j) a.rec[g.doff + ((long long)a.it * a.ncomp + slot) * nx + gx] = v[f][jj];
+                        slot++;
+                    }
+            }
+            if (!ADJ && a.snap_out[0]) {
+                const float m0 = a.snap_max_in[2 * s], m1 = a.snap_max_in[2 * s + 1];
+                const float q0 = m0 > 0.f ? SNAP_Q / m0 : 0.f, q1 = m1 > 0.f ? SNAP_Q / m1 : 0.f;
+                const float4 c0 = lds4<TX>(sm, VX, x, z), c1 = lds4<TX>(sm, VZ, x, z);
+                __half2 h[4];
+                h[0] = __floats2half2_rn(c0.x * q0, c0.y * q0);
+                h[1] = __floats2half2_rn(c0.z * q0, c0.w * q0);
+                h[2] = __floats2half2_rn(c1.x * q1, c1.y * q1);
+                h[3] = __floats2half2_rn(c1.z * q1, c1.w * q1);
+                if (nval == 4) {
+                    *reinterpret_cast<uint2 *>(a.snap_out[0] + o) = make_uint2(*reinterpret_cast<unsigned *>(&h[0]), *reinterpret_cast<unsigned *>(&h[1]));
+                    *reinterpret_cast<uint2 *>(a.snap_out[1] + o) = make_uint2(*reinterpret_cast<unsigned *>(&h[2]), *reinterpret_cast<unsigned *>(&h[3]));
+                } else {
+                    const float cv0[4] = {c0.x, c0.y, c0.z, c0.w}, cv1[4] = {c1.x, c1.y, c1.z, c1.w};
+                    for (int j = 0; j < nval; j++) {
+                        a.snap_out[0][o + j] = __float2half_rn(cv0[j] * q0);
+                        a.snap_out[1][o + j] = __float2half_rn(cv1[j] * q1);
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (j < nval) {
+                        wmax0 = fmaxf(wmax0, fabsf(v[VX][j]));
+                        wmax1 = fmaxf(wmax1, fabsf(v[VZ][j]));
+                    }
+            }
+            if (img) {
+                // imaging condition of level it (W/image-mod-rtm.f90:146-162)
+                const float d0 = a.imax0[2 * s] * (1.0f / SNAP_Q), d1 = a.imax0[2 * s + 1] * (1.0f / SNAP_Q);
+                auto SV = [&](int arr, int dx_, int dz_) {
+                    return __half2float(smh[arr * SZ + (x + dx_ + HALO) * V2_LZ + (z + dz_ + V2_ZH)]);
+                };
+                float s1[4], s2[4], s4[4], s5[4], s6[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    s1[j] = s2[j] = s4[j] = s5[j] = s6[j] = 0.f;
+                    const int cz = gz + j;
+                    if (!a.ilast) {
+                        const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
+                        s1[j] = a.inv_dt * (__half2float(a.isnap1[0][o + j]) * e0 - SV(0, 0, j) * d0);
+                        s2[j] = a.inv_dt * (__half2float(a.isnap1[1][o + j]) * e1 - SV(1, 0, j) * d1);
+                    }
+                    if (cz >= 4 && cz <= nz - 6 && gx >= 4 && gx <= nx - 6) {
+                        float p4 = 0.f, p5 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 5; k++) {
+                            p4 += StagCoef<float>::c(k) * (SV(0, 5 - k, j) - SV(0, -4 + k, j));
+                            p5 += StagCoef<float>::c(k) * (SV(1, 0, j + 5 - k) - SV(1, 0, j - 4 + k));
+                        }
+                        s4[j] = p4 * d0 * a.inv_dx;
+                        s5[j] = p5 * d1 * a.inv_dx;
+                    }
+                    if (cz >= 5 && cz <= nz - 6 && gx >= 5 && gx <= nx - 6) {
+                        float p6 = 0.f, p7 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 5; k++) {
+                            p6 += StagCoef<float>::c(k) * (SV(0, 0, j + 4 - k) - SV(0, 0, j - 5 + k));
+                            p7 += StagCoef<float>::c(k) * (SV(1, 4 - k, j) - SV(1, -5 + k, j));
+                        }
+                        s6[j] = (p6 * d0 + p7 * d1) * a.inv_dx;
+                    }
+                }
+                float tt[3][4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float s3 = s4[j] + s5[j];
+                    tt[0][j] = v[VX][j] * s1[j] + v[VZ][j] * s2[j];
+                    tt[1][j] = -(v[SXX][j] + v[SZZ][j]) * s3;
+                    tt[2][j] = -(2.f * v[SXX][j] * s4[j] + 2.f * v[SZZ][j] * s5[j] + v[SXZ][j] * s6[j]);
+                }
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    if (nval == 4) {
+                        float4 sv = ld_f4(a.img[i] + o), cv = ld_f4(a.imgc[i] + o);
+                        float sa[4] = {sv.x, sv.y, sv.z, sv.w}, ca[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const float y = tt[i][j] - ca[j];
+                            const float tsum = sa[j] + y;
+                            ca[j] = (tsum - sa[j]) - y;
+                            sa[j] = tsum;
+                        }
+                        *reinterpret_cast<float4 *>(a.img[i] + o) = make_float4(sa[0], sa[1], sa[2], sa[3]);
+                        *reinterpret_cast<float4 *>(a.imgc[i] + o) = make_float4(ca[0], ca[1], ca[2], ca[3]);
+                    } else {
+                        for (int j = 0; j < nval; j++) {
+                            float sj = a.img[i][o + j], cj = a.imgc[i][o + j];
+                            const float y = tt[i][j] - cj;
+                            const float tsum = sj + y;
+                            cj = (tsum - sj) - y;
+                            a.img[i][o + j] = tsum;
+                            a.imgc[i][o + j] = cj;
+                        }
+                    }
+                }
+            }
+        }
+        if (!ADJ && a.snap_out[0]) {
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) {
+                wmax0 = fmaxf(wmax0, __shfl_xor_sync(0xffffffffu, wmax0, d));
+                wmax1 = fmaxf(wmax1, __shfl_xor_sync(0xffffffffu, wmax1, d));
+            }
+            if (lane == 0) {
+                atomic_max_abs(a.snap_max_out + 2 * s, wmax0);
+                atomic_max_abs(a.snap_max_out + 2 * s + 1, wmax1);
+            }
+        }
+    }
+}
+
+}  // namespace eg

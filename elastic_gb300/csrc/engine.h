@@ -13,7 +13,12 @@
 
 namespace eg {
 
-constexpr int TZ_TILE = 32;  // tile height (one warp along z)
+constexpr int TZ_TILE = 32;   // v1 tile height (one warp along z)
+constexpr int TZ_TILE2 = 128; // v2 tile height (32 lanes x 4 cells)
+
+// Kernel version: 0 = automatic (v2 where the layout allows), 1 or 2 forced
+// (a forced v2 on an unaligned layout runs v1).
+int kernel_version();
 
 int ensure_device();
 int device_sm_count();
@@ -64,26 +69,33 @@ struct ShotTable {
     std::vector<HostShot> shots;
     int ldz = 0;
     int tx = 16;
+    int tz = TZ_TILE;
     int ntiles = 0;
     ShotGeom *d_geom = nullptr;
     ShotTable() = default;
     ShotTable(const ShotTable &) = delete;
     ShotTable &operator=(const ShotTable &) = delete;
     ~ShotTable();
-    int build(int tx);
+    int build(int tx, int tz = TZ_TILE);
 };
 
 // Tile width giving at least two work items per SM when the grid allows.
-inline int pick_tile_width(long long cells_z, long long cells_x)
+inline int pick_tile_width(long long cells_z, long long cells_x, int tz = TZ_TILE)
 {
-    const long long ntz = (cells_z + TZ_TILE - 1) / TZ_TILE;
+    const long long ntz = (cells_z + tz - 1) / tz;
     const long long want = 2LL * device_sm_count();
     for (int tx : {32, 16}) if (ntz * ((cells_x + tx - 1) / tx) >= want) return tx;
     return 8;
 }
 
 template <typename T>
-int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st);
+int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz = TZ_TILE);
+
+// True when a float step on planes with pitch ldz starting at `ptrs` can use v2.
+bool v2_usable(bool is_float, int ldz, const void *const *ptrs, int n);
+// True when the v2 kernel of this flavour and tile width fits in shared memory.
+bool v2_fits(bool adj, bool exact, int tx);
+int max_smem_optin();
 
 template <typename T>
 int model_coefs(int nz, int nx, T dx, T dt, const T *d_rho, const T *d_lam, const T *d_mu, int ldin, T *m1x, T *m1z,

@@ -32,6 +32,11 @@ def set_exact(exact=True):
     load().rtm_set_exact(1 if exact else 0)
 
 
+def set_kernel_version(version=0):
+    """0 automatic, 1 shared-memory tile kernel, 2 cp.async-staged kernel."""
+    load().rtm_set_kernel_version(int(version))
+
+
 # ----------------------------------------------------------------- a1..a4
 def model_op(rho, lam, mu, dx, dt):
     """model_op + rtmmod_init + aux_*_c.  Returns (m1_x, m1_z, aux_m2_c,

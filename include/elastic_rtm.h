@@ -37,6 +37,10 @@ const char *rtm_last_error(void);
 int rtm_last_status(void);
 /* Select exact (1, default) or fast (0) arithmetic for the drop-in calls. */
 void rtm_set_exact(int exact);
+/* Step-kernel generation: 0 automatic (default), 1 the shared-memory tile
+ * kernel, 2 the cp.async-staged kernel (used only where planes are 16-byte
+ * aligned with a pitch that is a multiple of 4 floats; otherwise 1). */
+void rtm_set_kernel_version(int version);
 
 /* ------------------------------------------------- drop-in replacements */
 /* Adjoint recursion for levels nt-3 .. 0 (0-based) on full histories, in
@@ -163,11 +167,18 @@ rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp
  * host pointers. */
 int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device, float *image,
                       int image_on_device);
-/* out[0..6]: forward ms, adjoint ms, cells of the last group, kernels
- * launched, total ms of the last call, tile width, work items. */
+/* out[0..13]: forward ms, adjoint ms, cells of the last group, kernels
+ * launched, total ms of the last call, forward tile width, forward work
+ * items, adjoint tile width, then the autotuner's ms per step for tile
+ * widths 8, 16, 32 (forward, then adjoint). */
 int rtm_batch_stats(const rtm_batch *b, double *out);
-/* use_graph=0 launches the time loop kernel by kernel. */
-int rtm_batch_set(rtm_batch *b, int use_graph);
+/* Autotuner: times `steps` launches of each pass for every tile width on the
+ * geometry of shots [shot0, shot0+nshot) and keeps the fastest per pass for
+ * the following rtm_batch_migrate calls. */
+int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps);
+/* use_graph=0 launches the time loop kernel by kernel; tile_x selects the
+ * tile width of the step kernel (8, 16 or 32; 0 = automatic). */
+int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */
 void *rtm_host_alloc(size_t bytes);

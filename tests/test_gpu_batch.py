@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from elastic_gb300 import rtm as R
 from elastic_gb300 import synth
 from elastic_gb300.batch import BatchRTM
 
@@ -44,11 +45,14 @@ def oracle_stack(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, ab
     return img
 
 
-def run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group, graph=True):
+def run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group, graph=True,
+              tile_x=0, tune=False):
     n = len(nxs)
     eng = BatchRTM(nz, nx, nt, dx, dt, fp, abc, rho, lam, mu, x0, nxs, xsrc, np.full(n, zs), np.full(n, zr),
                    comp_mask=3, group_max=group, nsource=ns)
-    eng.set_graph(graph)
+    if tune:
+        eng.autotune(0, group, steps=4)
+    eng.set_graph(graph, tile_x)
     image = np.zeros(3 * nz * nx, np.float32)
     for s0, k in eng.groups():
         flat = np.concatenate([np.concatenate([traces[s][c].ravel() for c in range(2)]) for s in range(s0, s0 + k)])
@@ -58,7 +62,9 @@ def run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, 
     return image.reshape(3, nx, nz), st
 
 
-def test_batch_matches_oracle_stack():
+@pytest.mark.parametrize("version", [1, 2])
+def test_batch_matches_oracle_stack(version):
+    R.set_kernel_version(version)
     nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 48, 200, 160, 10.0, 1e-3, 30.0, 12, 6, 6, 40
     rho, lam, mu, x0, nxs, xsrc, traces = survey(nz=nz, nx=nx, nt=nt)
     img, st = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=2)
@@ -67,6 +73,7 @@ def test_batch_matches_oracle_stack():
     errs32 = [rel_l2(img[i], ref32[i]) for i in range(3)]
     errs64 = [rel_l2(img[i], ref64[i]) for i in range(3)]
     print("batch vs FP32 oracle", errs32, "vs FP64 oracle", errs64, st)
+    R.set_kernel_version(0)
     assert max(errs32) < RTOL_SNAP
     assert max(errs64) < RTOL_SNAP
     assert st["kernels"] == 2 * nt
@@ -79,3 +86,22 @@ def test_batch_graph_and_grouping_are_bit_identical():
     b, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=1,
                      graph=False)
     np.testing.assert_array_equal(a, b)
+
+
+def test_batch_tile_widths_and_autotuner_are_bit_identical():
+    """The tile width (chosen by hand or by the autotuner) does not change
+    the arithmetic of any cell."""
+    nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 40, 180, 60, 10.0, 1e-3, 30.0, 10, 6, 6, 40
+    rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=5)
+    ref, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3, tile_x=8)
+    for tx in (16,):
+        img, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
+                           tile_x=tx)
+        np.testing.assert_array_equal(img, ref)
+    img, st = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
+                        tune=True)
+    np.testing.assert_array_equal(img, ref)
+    assert st["tile_x"] in (8, 16, 32) and st["tile_x_adj"] in (8, 16, 32)
+    # -1 marks a tile width that does not fit in shared memory
+    assert all(t > 0 or t == -1 for t in st["tune_ms_fwd"] + st["tune_ms_adj"])
+    assert max(st["tune_ms_fwd"]) > 0 and max(st["tune_ms_adj"]) > 0

@@ -38,11 +38,15 @@ def model(nz, nx, seed=0, dtype=np.float32):
     return rho.astype(dtype), lam.astype(dtype), mu.astype(dtype)
 
 
-@pytest.fixture(autouse=True)
-def exact_mode():
+@pytest.fixture(autouse=True, params=[1, 2], ids=["v1", "v2"])
+def exact_mode(request):
+    """Every test runs with both step-kernel generations (v2 applies where the
+    planes are 16-byte aligned, e.g. nz % 4 == 0; elsewhere both run v1)."""
     R.set_exact(True)
+    R.set_kernel_version(request.param)
     yield
     R.set_exact(True)
+    R.set_kernel_version(0)
 
 
 def test_rtm_op3_c_matches_reference_golden_vectors():
