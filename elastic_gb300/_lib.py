@@ -22,6 +22,7 @@ SIGNATURES = {
     "rtm_set_exact": (None, [_c_int]),
     "rtm_set_kernel_version": (None, [_c_int]),
     "rtm_op3_c_": (None, [_c_int] * 4 + [_P] * 10),
+    "rtm_op3_dev_noalloc": (_c_int, [_c_int] * 3 + [_P] * 11),
     "rtm_gpu_init": (None, [_c_int] * 3),
     "rtm_gpu_copy_in": (None, [_c_int] * 3 + [_P] * 10),
     "rtm_gpu_copy_out": (None, [_c_int] * 3 + [_P] * 5),

@@ -52,6 +52,25 @@ void rtm_set_kernel_version(int version);
 void rtm_op3_c_(int nt, int nz, int nx, int zrec, float *Vx0, float *Vz0, float *sigmaxx0, float *sigmazz0,
                 float *sigmaxz0, float *m1_x, float *m1_z, float *aux_m2_c, float *aux_m3_c, float *aux_m2m3_c);
 
+/* Allocation-free variant of rtm_op3_c_ (no counterpart in the reference):
+ * the same adjoint recursion, exact arithmetic, on caller-owned DEVICE
+ * buffers -- five (nz,nx,nt) histories updated in place and five unmasked
+ * (nz,nx) coefficient planes -- for callers that cannot allocate device
+ * memory at that point (their allocator owns the device heap, or an
+ * allocation there would synchronise or fail).  It never calls cudaMalloc or
+ * cudaFree: its scratch (masked coefficients, work-item table) is a fixed
+ * 10 MiB device array of this library, so nz*nx must not exceed
+ * RTM_NOALLOC_MAX_CELLS (larger grids are rejected with status 1).  The
+ * first call on each device looks the scratch up (cudaGetSymbolAddress);
+ * make it before any stream capture.  Calls whose GPU work overlaps race on
+ * the shared scratch.  stream: a cudaStream_t, or NULL for the default
+ * stream; returns after the work has finished. */
+#define RTM_NOALLOC_MAX_CELLS 524288
+int rtm_op3_dev_noalloc(int nt, int nz, int nx, float *Vx0_dev, float *Vz0_dev, float *sigmaxx0_dev,
+                        float *sigmazz0_dev, float *sigmaxz0_dev, const float *m1_x_dev, const float *m1_z_dev,
+                        const float *aux_m2_c_dev, const float *aux_m3_c_dev, const float *aux_m2m3_c_dev,
+                        void *stream);
+
 /* The reference's internal C<->CUDA layer (W/rtmlib-modC-gpu.cu:35,77,100,
  * 115,425), same arguments and padded layout: arrays (nz+10,nx+10[,nt+10])
  * with a 5-cell offset on every axis (W/gpu.h:9,13), masked coefficients.
