@@ -50,6 +50,11 @@ SIGNATURES = {
     "rtm_batch_destroy": (None, [_P]),
     "rtm_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "rtm_host_free": (None, [_P]),
+    "acoustic3d_fwd_c_": (_c_int, [_c_int] * 4 + [_c_float] * 3 + [_P, _c_int, _c_float, _c_int, _c_int, _c_int, _P,
+                                   _c_int, _P, _P, _P, _c_int, _P]),
+    "acoustic3d_rtm_c_": (_c_int, [_c_int] * 4 + [_c_float] * 3 + [_P, _c_int, _c_float, _c_int, _c_int, _c_int, _P,
+                                   _c_int, _P, _c_int, _P, _c_int, _P]),
+    "acoustic3d_set": (_c_int, [_c_int, _c_int]),
 }
 
 _lib = None

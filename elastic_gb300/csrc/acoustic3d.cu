@@ -1,0 +1,596 @@
+// Single-domain 3D acoustic propagator, 10th order in space, 2nd in time,
+// and 3D RTM with reverse-time restart of the source wavefield (sm_103a).
+//
+// Reference (lgan/elastic, W = 2d_rtm_restart/Src_working), raised from its
+// 8th-order stencil to 10th order:
+//   W/wave_fkernel.3d8o.cu:31-106   p2 = vel*L(p1) + p1 + p1 - p0, vel = v^2 dt^2
+//   W/wave_fkernel.3d8o.cu:183-210  sponge p0, p1 *= exp(-b(a-edge)) before each step
+//   W/gpu_funcs_3d.cu:64-131        source injection, receiver extraction, imaging
+//   W/gpu_funcs_3d.cu:509-712       adjoint with the source wavefield restarted
+//                                   backwards from its last two slices
+//
+// Layout: p[(iy*n2 + ix)*n1 + iz], iz fastest; interior cells [5, n-5) on
+// every axis are updated, the 5-cell rim stays zero.
+//
+// Kernel (2.5-D): a CTA covers 128 z-rows x TX columns and marches along y.
+// Each thread owns 4 consecutive z cells of one column: an 11-slice register
+// queue of float4 gives the y taps; the current slice with its x and z halo
+// sits in shared memory for the x and z taps.  DRAM traffic per cell-update
+// is p1 + p0 + vel read, p2 written (16 B).
+//
+// Sponge, fused: planes are stored pre-damped.  The reference damps p1 and
+// p0 in place before each step, so every stored level is multiplied by the
+// factor once as "p1" and once more as "p0".  Writing f*p2 and reading
+// f*p0 reproduces that exactly (same products, same rounding).  Receivers see
+// the undamped level, as in the reference (they record before the next
+// step's damping).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "../../include/elastic_rtm.h"
+#include "common.cuh"
+#include "engine.h"
+
+using namespace eg;
+
+namespace {
+
+constexpr int AR = 5;            // stencil radius
+constexpr int A_TZ = 128;        // tile rows (32 lanes x 4)
+constexpr int A_ZH = 8;          // aligned z halo
+constexpr int A_LZ = A_TZ + 2 * A_ZH;
+
+struct Ac3DArgs {
+    const float *p0;   // level t-1 (stored, pre-damped)
+    const float *p1;   // level t   (stored, pre-damped)
+    float *p2;         // level t+1 output (may alias p0)
+    const float *vel;  // v^2 dt^2
+    int n1, n2, n3;
+    float coef[16];    // C0, then (z, x, y) per offset 1..5
+    const float *damp; // factor per edge distance, damp_a entries (nullable)
+    int damp_a;
+    long long src_o;   // linear offset of the source cell, -1 none
+    float src_val;     // added to the raw p2 at the source cell
+    int zr;            // receiver plane (0-based), -1 none
+    float *rec_out;    // record raw p2 at iz=zr into rec_out[iy*n2+ix]
+    const float *rec_in;  // add rec_in[iy*n2+ix] to p2 at iz=zr
+    float *img;        // img += (1e-6*p2_raw)*simg  (nullable)
+    const float *simg;
+    int y0, y1;        // y range of the march handled by a CTA chunk: [y0, y1)
+    int ychunks;       // number of y chunks
+};
+
+__device__ __forceinline__ int edge_dist(int i, int n)
+{
+    const int lo = i - AR, hi = (n - 1 - AR) - i;
+    return lo < hi ? lo : hi;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float damp_of(const Ac3DArgs &a, int iz, int ix, int iy)
+{
+    if (!a.damp) return 1.f;
+    int e = edge_dist(iz, a.n1);
+    e = min(e, edge_dist(ix, a.n2));
+    e = min(e, edge_dist(iy, a.n3));
+    if (e >= 0 && e < a.damp_a) {
+        const float t = __ldg(a.damp + e);
+        return t < 1.f ? t : 1.f;
+    }
+    return 1.f;
+}
+
+template <bool EXACT>
+__device__ __forceinline__ float fm(float x, float y) { return EXACT ? __fmul_rn(x, y) : x * y; }
+template <bool EXACT>
+__device__ __forceinline__ float fa(float x, float y) { return EXACT ? __fadd_rn(x, y) : x + y; }
+template <bool EXACT>
+__device__ __forceinline__ float fs(float x, float y) { return EXACT ? __fsub_rn(x, y) : x - y; }
+
+__device__ __forceinline__ float e4(const float4 &v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
+
+template <bool EXACT, int TX>
+__global__ void __launch_bounds__(TX * 32) k_acoustic3d(const __grid_constant__ Ac3DArgs a)
+{
+    __shared__ __align__(16) float sl[(TX + 2 * AR) * A_LZ];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // warp = column in tile
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3;
+    const int ntz = (n1 - 2 * AR + A_TZ - 1) / A_TZ;
+    const int ntx = (n2 - 2 * AR + TX - 1) / TX;
+    int b = blockIdx.x;
+    const int yc = b % a.ychunks;
+    b /= a.ychunks;
+    const int tzi = b % ntz, txi = b / ntz;
+    const int z0 = AR + tzi * A_TZ, x0 = AR + txi * TX;
+    const int ylen = (n3 - 2 * AR + a.ychunks - 1) / a.ychunks;
+    const int ya = AR + yc * ylen, yb = min(n3 - AR, ya + ylen);
+    if (ya >= yb) return;
+    const int z = z0 + 4 * lane, x = x0 + warp;  // this thread's cells z..z+3 at column x
+    const bool colok = x < n2 - AR;
+    const long long s2 = n1, s3 = (long long)n1 * n2;
+    // Interior rows start at 5, so the 4 cells of a thread are not 16-byte
+    // aligned: the queue and the own-cell loads are scalar.
+    // Queue q[k] = p1 at (z..z+3, x, y-5+k).
+    float q[11][4];
+#pragma unroll
+    for (int k = 0; k < 11; k++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) q[k][j] = 0.f;  // columns beyond the interior stay zero
+    auto ld4 = [&](const float *p, long long o, float out[4]) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) out[j] = (z + j < n1 - AR) ? __ldg(p + o + j) : 0.f;
+    };
+    const long long ocol = (long long)x * s2 + z;
+    if (colok)
+#pragma unroll
+        for (int k = 0; k < 10; k++) ld4(a.p1, ocol + (long long)(ya - 5 + k) * s3, q[k + 1]);
+    const float *coef = a.coef;
+    for (int y = ya; y < yb; y++) {
+        // advance the queue: q[0..9] <- q[1..10], q[10] <- p1(y+5)
+#pragma unroll
+        for (int k = 0; k < 10; k++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) q[k][j] = q[k + 1][j];
+        if (colok) ld4(a.p1, ocol + (long long)(y + 5) * s3, q[10]);
+        __syncthreads();  // previous slice consumed
+        // centre of the slice from the queue
+        {
+            float *d = sl + (warp + AR) * A_LZ + (4 * lane + A_ZH);
+#pragma unroll
+            for (int j = 0; j < 4; j++) d[j] = q[5][j];
+        }
+        // z halo (rows z0-8..z0-1 and z0+128..z0+135) and x halo (5 columns each side)
+        {
+            const long long sy = (long long)y * s3;
+            for (int e = threadIdx.x; e < TX * 2 * A_ZH; e += blockDim.x) {
+                const int c = e / (2 * A_ZH), r = e % (2 * A_ZH);
+                const int zz = r < A_ZH ? z0 - A_ZH + r : z0 + A_TZ + (r - A_ZH);
+                const int xx = x0 + c;
+                const float v = (zz >= 0 && zz < n1 && xx < n2) ? __ldg(a.p1 + sy + (long long)xx * s2 + zz) : 0.f;
+                sl[(c + AR) * A_LZ + (zz - z0 + A_ZH)] = v;
+            }
+            for (int e = threadIdx.x; e < 2 * AR * A_LZ; e += blockDim.x) {
+                const int c = e / A_LZ, r = e % A_LZ;
+                const int xx = c < AR ? x0 - AR + c : x0 + TX + (c - AR);
+                const int zz = z0 - A_ZH + r;
+                const float v = (zz >= 0 && zz < n1 && xx >= 0 && xx < n2) ? __ldg(a.p1 + sy + (long long)xx * s2 + zz) : 0.f;
+                sl[(c < AR ? c : TX + c) * A_LZ + r] = v;
+            }
+        }
+        __syncthreads();
+        if (!colok) continue;
+        const long long o = ocol + (long long)y * s3;
+        float vel4[4], p04[4];
+        ld4(a.vel, o, vel4);
+        ld4(a.p0, o, p04);
+        float w[20];  // z window rows z-8..z+11 at column x
+        {
+            const float *c = sl + (warp + AR) * A_LZ + (4 * lane + A_ZH) - 8;
+#pragma unroll
+            for (int i = 0; i < 20; i++) w[i] = c[i];
+        }
+        float outv[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float p = q[5][j];
+            float acc = fm<EXACT>(coef[0], p);
+#pragma unroll
+            for (int k = 1; k <= 5; k++) {
+                const float zp = fa<EXACT>(w[8 + j + k], w[8 + j - k]);
+                const float xp = fa<EXACT>(sl[(warp + AR + k) * A_LZ + (4 * lane + A_ZH + j)],
+                                           sl[(warp + AR - k) * A_LZ + (4 * lane + A_ZH + j)]);
+                const float yp = fa<EXACT>(q[5 + k][j], q[5 - k][j]);
+                acc = fa<EXACT>(acc, fm<EXACT>(coef[1 + 3 * (k - 1)], zp));
+                acc = fa<EXACT>(acc, fm<EXACT>(coef[2 + 3 * (k - 1)], xp));
+                acc = fa<EXACT>(acc, fm<EXACT>(coef[3 + 3 * (k - 1)], yp));
+            }
+            const int zz = z + j;
+            const float f = damp_of<EXACT>(a, zz, x, y);
+            const float p0d = f == 1.f ? p04[j] : fm<EXACT>(f, p04[j]);
+            float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(vel4[j], acc), p), p), p0d);
+            const long long oj = o + j;
+            if (oj == a.src_o) v = fa<EXACT>(v, a.src_val);
+            if (zz == a.zr) {
+                const long long ri = (long long)y * n2 + x;
+                if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
+                if (a.rec_out) a.rec_out[ri] = v;
+            }
+            if (a.img && zz < n1 - AR) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
+            outv[j] = f == 1.f ? v : fm<EXACT>(f, v);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if (z + j < n1 - AR) a.p2[o + j] = outv[j];
+    }
+}
+
+// Pipelined 2.5-D kernel for n1 % 4 == 0 (16-byte aligned columns).  Tiles
+// start at row 4 + 128k so that every thread's 4 cells form one aligned
+// float4; rows outside the interior are computed as zero and stay zero.
+// Per y slice: the x/z halo of the NEXT slice is staged by cp.async into the
+// other half of a double buffer and the next queue / p0 / vel values are
+// loaded into registers while the current slice is computed; one barrier
+// per slice.
+__device__ __forceinline__ void acp16(float *smem, const float *gmem, bool ok)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(ok ? 16 : 0));
+}
+
+template <bool EXACT, int TX>
+__global__ void __launch_bounds__(TX * 32, TX == 8 ? 2 : 1) k_acoustic3d_p(const __grid_constant__ Ac3DArgs a)
+{
+    __shared__ __align__(16) float buf[2][(TX + 2 * AR) * A_LZ];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3;
+    const int ntz = (n1 - 9 + A_TZ - 1) / A_TZ;  // rows 4 .. n1-6 (interior plus row 4)
+    const int ntx = (n2 - 2 * AR + TX - 1) / TX;
+    int b = blockIdx.x;
+    const int yc = b % a.ychunks;
+    b /= a.ychunks;
+    const int tzi = b % ntz, txi = b / ntz;
+    const int z0 = 4 + tzi * A_TZ, x0 = AR + txi * TX;
+    const int ylen = (n3 - 2 * AR + a.ychunks - 1) / a.ychunks;
+    const int ya = AR + yc * ylen, yb = min(n3 - AR, ya + ylen);
+    if (ya >= yb) return;
+    const int z = z0 + 4 * lane, x = x0 + warp;
+    const bool colok = x < n2 - AR;
+    const bool grp = colok && z < n1;  // this thread's float4 exists
+    const long long s2 = n1, s3 = (long long)n1 * n2;
+    const long long ocol = (long long)x * s2 + z;
+    auto L4 = [&](const float *p, long long o) -> float4 {
+        return grp ? __ldg(reinterpret_cast<const float4 *>(p + o)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    // halo staging of slice y into buffer h (z halo rows of the tile columns,
+    // x halo columns over all 144 rows), 16-byte chunks
+    auto stage = [&](int y, float *h) {
+        const long long sy = (long long)y * s3;
+        constexpr int ZCH = 4 * TX, XCH = 2 * AR * (A_LZ / 4);
+        for (int e = threadIdx.x; e < ZCH + XCH; e += blockDim.x) {
+            int col, r4;
+            if (e < ZCH) {
+                col = AR + e / 4;
+                const int q = e % 4;
+                r4 = q < 2 ? 4 * q : A_ZH + A_TZ + 4 * (q - 2);
+            } else {
+                const int f = e - ZCH;
+                const int c = f / (A_LZ / 4);
+                col = c < AR ? c : TX + c;
+                r4 = 4 * (f % (A_LZ / 4));
+            }
+            const int xx = x0 - AR + col, zz = z0 - A_ZH + r4;
+            const bool ok = xx >= 0 && xx < n2 && zz >= 0 && zz < n1;
+            acp16(h + col * A_LZ + r4, a.p1 + (ok ? sy + (long long)xx * s2 + zz : 0), ok);
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    };
+    float4 q[11];
+#pragma unroll
+    for (int k = 0; k < 11; k++) q[k] = L4(a.p1, ocol + (long long)(ya - 5 + k) * s3);
+    stage(ya, buf[ya & 1]);
+    // every column writes its centre (zero outside the interior): the
+    // x taps of edge cells read these slots
+    *reinterpret_cast<float4 *>(buf[ya & 1] + (warp + AR) * A_LZ + (4 * lane + A_ZH)) = q[5];
+    float4 p0c = L4(a.p0, ocol + (long long)ya * s3), velc = L4(a.vel, ocol + (long long)ya * s3);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncthreads();
+    const float *coef = a.coef;
+    for (int y = ya; y < yb; y++) {
+        const bool more = y + 1 < yb;
+        float4 qn = make_float4(0.f, 0.f, 0.f, 0.f), p0n = qn, veln = qn;
+        if (more) {
+            stage(y + 1, buf[(y + 1) & 1]);
+            qn = L4(a.p1, ocol + (long long)(y + 6) * s3);
+            p0n = L4(a.p0, ocol + (long long)(y + 1) * s3);
+            veln = L4(a.vel, ocol + (long long)(y + 1) * s3);
+        }
+        if (grp) {
+            const float *sl = buf[y & 1];
+            const float *cz = sl + (warp + AR) * A_LZ + (4 * lane + A_ZH);
+            float w[20];
+#pragma unroll
+            for (int i = 0; i < 20; i += 4) {
+                const float4 t = *reinterpret_cast<const float4 *>(cz - 8 + i);
+                w[i] = t.x; w[i + 1] = t.y; w[i + 2] = t.z; w[i + 3] = t.w;
+            }
+            const long long o = ocol + (long long)y * s3;
+            // offset-outer, cell-inner: each cell's sum keeps the order
+            // C0, then (z, x, y) for offsets 1..5
+            float accv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) accv[j] = fm<EXACT>(coef[0], e4(q[5], j));
+#pragma unroll
+            for (int k = 1; k <= 5; k++) {
+                const float4 xm = *reinterpret_cast<const float4 *>(cz - k * A_LZ);
+                const float4 xp = *reinterpret_cast<const float4 *>(cz + k * A_LZ);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float zp = fa<EXACT>(w[8 + j + k], w[8 + j - k]);
+                    const float xq = fa<EXACT>(e4(xp, j), e4(xm, j));
+                    const float yp = fa<EXACT>(e4(q[5 + k], j), e4(q[5 - k], j));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[1 + 3 * (k - 1)], zp));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[2 + 3 * (k - 1)], xq));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[3 + 3 * (k - 1)], yp));
+                }
+            }
+            float out[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int zz = z + j;
+                const float p = e4(q[5], j);
+                const float acc = accv[j];
+                const bool inside = zz >= AR && zz < n1 - AR;
+                const float f = damp_of<EXACT>(a, zz, x, y);
+                const float p0v = e4(p0c, j);
+                const float p0d = f == 1.f ? p0v : fm<EXACT>(f, p0v);
+                float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), acc), p), p), p0d);
+                const long long oj = o + j;
+                if (oj == a.src_o) v = fa<EXACT>(v, a.src_val);
+                if (inside && zz == a.zr) {
+                    const long long ri = (long long)y * n2 + x;
+                    if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
+                    if (a.rec_out) a.rec_out[ri] = v;
+                }
+                if (inside && a.img) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
+                out[j] = inside ? (f == 1.f ? v : fm<EXACT>(f, v)) : 0.f;
+            }
+            *reinterpret_cast<float4 *>(a.p2 + o) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+        if (more) *reinterpret_cast<float4 *>(buf[(y + 1) & 1] + (warp + AR) * A_LZ + (4 * lane + A_ZH)) = q[6];
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 10; k++) q[k] = q[k + 1];
+        q[10] = qn;
+        p0c = p0n;
+        velc = veln;
+    }
+}
+
+// wavelet injection on a stored plane (used for the reverse restart:
+// S(t) - w(t) delta before the backward step)
+__global__ void k_inject(float *p, long long o, float v)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) p[o] = p[o] + v;
+}
+
+template <bool EXACT>
+int launch_ac(const Ac3DArgs &a0, int tx, int ychunks, cudaStream_t st)
+{
+    Ac3DArgs a = a0;
+    a.ychunks = ychunks;
+    const int ntx = (a.n2 - 2 * AR + tx - 1) / tx;
+    if (a.n1 % 4 == 0) {
+        const int ntz = (a.n1 - 9 + A_TZ - 1) / A_TZ;
+        const int grid = ntz * ntx * ychunks;
+        switch (tx) {
+        case 8: k_acoustic3d_p<EXACT, 8><<<grid, 8 * 32, 0, st>>>(a); break;
+        case 16: k_acoustic3d_p<EXACT, 16><<<grid, 16 * 32, 0, st>>>(a); break;
+        default: rtm_set_error("unsupported 3D tile width %d", tx); return RTM_ERR_ARG;
+        }
+    } else {
+        const int ntz = (a.n1 - 2 * AR + A_TZ - 1) / A_TZ;
+        const int grid = ntz * ntx * ychunks;
+        switch (tx) {
+        case 8: k_acoustic3d<EXACT, 8><<<grid, 8 * 32, 0, st>>>(a); break;
+        case 16: k_acoustic3d<EXACT, 16><<<grid, 16 * 32, 0, st>>>(a); break;
+        default: rtm_set_error("unsupported 3D tile width %d", tx); return RTM_ERR_ARG;
+        }
+    }
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+struct Ac3D {
+    int n1, n2, n3, nt;
+    size_t vol;
+    DevBuf<float> vel, buf, damp, rec, img;
+    float coef[16];
+    int damp_a = 0;
+    int tx = 16, ych = 2;
+    bool exact = false;
+    cudaStream_t st = 0;
+
+    int step(const float *p0, const float *p1, float *p2, bool damped, long long src_o, float src_val, int zr,
+             float *rec_out, const float *rec_in, float *img, const float *simg)
+    {
+        Ac3DArgs a;
+        memset(&a, 0, sizeof a);
+        a.p0 = p0; a.p1 = p1; a.p2 = p2; a.vel = vel.p;
+        a.n1 = n1; a.n2 = n2; a.n3 = n3;
+        memcpy(a.coef, coef, sizeof coef);
+        a.damp = damped && damp_a > 0 ? damp.p : nullptr;
+        a.damp_a = damp_a;
+        a.src_o = src_o; a.src_val = src_val;
+        a.zr = zr; a.rec_out = rec_out; a.rec_in = rec_in;
+        a.img = img; a.simg = simg;
+        return exact ? launch_ac<true>(a, tx, ych, st) : launch_ac<false>(a, tx, ych, st);
+    }
+};
+
+void host_coeffs(double d1, double d2, double d3, float *coef)
+{
+    const double c[6] = {-5269.0 / 1800.0, 5.0 / 3.0, -5.0 / 21.0, 5.0 / 126.0, -5.0 / 1008.0, 1.0 / 3150.0};
+    const double i1 = 1.0 / (d1 * d1), i2 = 1.0 / (d2 * d2), i3 = 1.0 / (d3 * d3);
+    coef[0] = (float)(c[0] * (i1 + i2 + i3));
+    for (int k = 1; k <= 5; k++) {
+        coef[1 + 3 * (k - 1) + 0] = (float)(c[k] * i1);
+        coef[1 + 3 * (k - 1) + 1] = (float)(c[k] * i2);
+        coef[1 + 3 * (k - 1) + 2] = (float)(c[k] * i3);
+    }
+}
+
+int ac_setup(Ac3D &m, int n1, int n2, int n3, int nt, float d1, float d2, float d3, const float *vel2, int vel_dev,
+             int damp_a, float damp_b)
+{
+    RTM_CHECK_ARG(n1 >= 2 * AR + 1 && n2 >= 2 * AR + 1 && n3 >= 2 * AR + 1 && nt >= 2, "3D grid too small");
+    TRY(ensure_device());
+    m.n1 = n1; m.n2 = n2; m.n3 = n3; m.nt = nt;
+    m.vol = (size_t)n1 * n2 * n3;
+    host_coeffs(d1, d2, d3, m.coef);
+    TRY(m.vel.alloc(m.vol));
+    RTM_CUDA(cudaMemcpy(m.vel.p, vel2, m.vol * sizeof(float), vel_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    m.damp_a = damp_a;
+    if (damp_a > 0) {
+        std::vector<float> t(damp_a);
+        for (int e = 0; e < damp_a; e++) t[e] = expf(-damp_b * (float)(damp_a - e));
+        TRY(m.damp.alloc(damp_a));
+        RTM_CUDA(cudaMemcpy(m.damp.p, t.data(), damp_a * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    const char *e = getenv("ELASTIC_RTM_EXACT3D");
+    m.exact = e && atoi(e) == 1;
+    return RTM_OK;
+}
+
+int g_ac_tx = 16, g_ac_ych = 0;  // tile width and y chunks (0: chosen from the SM count)
+
+int pick_ychunks(int n1, int n2, int tx)
+{
+    if (g_ac_ych > 0) return g_ac_ych;
+    const int ntz = n1 % 4 == 0 ? (n1 - 9 + A_TZ - 1) / A_TZ : (n1 - 2 * AR + A_TZ - 1) / A_TZ;
+    const int ntx = (n2 - 2 * AR + tx - 1) / tx;
+    const int nsm = device_sm_count() * (tx == 8 ? 2 : 1);
+    int best = 1;
+    double best_eff = 0;
+    for (int c = 1; c <= 8; c++) {
+        const int g = ntz * ntx * c;
+        const double waves = (double)g / nsm;
+        const double eff = waves / std::ceil(waves) * (1.0 - 0.01 * c);  // chunks re-read 10 slices
+        if (eff > best_eff) { best_eff = eff; best = c; }
+    }
+    return best;
+}
+
+// Forward modelling from rest (W/gpu_funcs_3d.cu:133-315 with the sponge of
+// damp_kernel): returns the raw traces d[it][iy][ix] and the last two
+// stored levels.
+int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, float dir, int zr, float *d_dev,
+               float **last0, float **last1)
+{
+    m.tx = g_ac_tx;
+    m.ych = pick_ychunks(m.n1, m.n2, m.tx);
+    TRY(m.buf.alloc(2 * m.vol));
+    float *A = m.buf.p, *B = m.buf.p + m.vol;
+    RTM_CUDA(cudaMemsetAsync(m.buf.p, 0, 2 * m.vol * sizeof(float), m.st));
+    for (int it = 0; it < m.nt; it++) {
+        // A = level it-2 (older), B = level it-1; the new level goes over A
+        TRY(m.step(A, B, A, damped, src_o, dir * wavelet[it], zr, d_dev ? d_dev + (size_t)it * m.n2 * m.n3 : nullptr,
+                   nullptr, nullptr, nullptr));
+        std::swap(A, B);
+    }
+    *last0 = A;  // level nt-2
+    *last1 = B;  // level nt-1
+    return RTM_OK;
+}
+
+}  // namespace
+
+extern "C" int acoustic3d_set(int tile_x, int ychunks)
+{
+    RTM_CHECK_ARG(tile_x == 8 || tile_x == 16, "tile_x must be 8 or 16");
+    RTM_CHECK_ARG(ychunks >= 0 && ychunks <= 64, "ychunks must be 0..64");
+    g_ac_tx = tile_x;
+    g_ac_ych = ychunks;
+    return RTM_OK;
+}
+
+extern "C" int acoustic3d_fwd_c_(int n1, int n2, int n3, int nt, float d1, float d2, float d3, const float *vel2,
+                                 int damp_a, float damp_b, int zs, int xs, int ys, const float *wavelet, int zr,
+                                 float *data, float *p_last0, float *p_last1, int on_device, double *ms)
+{
+    Ac3D m;
+    TRY(ac_setup(m, n1, n2, n3, nt, d1, d2, d3, vel2, on_device, damp_a, damp_b));
+    RTM_CHECK_ARG(zs >= 1 && zs <= n1 && xs >= 1 && xs <= n2 && ys >= 1 && ys <= n3, "source outside the grid");
+    RTM_CHECK_ARG(zr == 0 || (zr >= 1 && zr <= n1), "receiver plane outside the grid");
+    const long long so = ((long long)(ys - 1) * n2 + (xs - 1)) * n1 + (zs - 1);
+    const size_t dn = (size_t)nt * n2 * n3;
+    DevBuf<float> d;
+    float *dd = nullptr;
+    if (zr > 0 && data) {
+        if (on_device) dd = data;
+        else { TRY(d.alloc(dn)); dd = d.p; }
+        RTM_CUDA(cudaMemsetAsync(dd, 0, dn * sizeof(float), m.st));
+    }
+    cudaEvent_t e0, e1;
+    RTM_CUDA(cudaEventCreate(&e0));
+    RTM_CUDA(cudaEventCreate(&e1));
+    RTM_CUDA(cudaEventRecord(e0, m.st));
+    float *l0, *l1;
+    TRY(ac_forward(m, true, so, wavelet, 1.f, zr - 1, dd, &l0, &l1));
+    RTM_CUDA(cudaEventRecord(e1, m.st));
+    RTM_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    RTM_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    if (ms) *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (dd && !on_device) RTM_CUDA(cudaMemcpy(data, dd, dn * sizeof(float), k));
+    if (p_last0) RTM_CUDA(cudaMemcpy(p_last0, l0, m.vol * sizeof(float), k));
+    if (p_last1) RTM_CUDA(cudaMemcpy(p_last1, l1, m.vol * sizeof(float), k));
+    RTM_CUDA(cudaDeviceSynchronize());
+    return RTM_OK;
+}
+
+// 3D RTM (W/gpu_funcs_3d.cu:509-712): source propagated forward undamped,
+// only its last two levels kept; backwards: the receiver field (damped) takes
+// the traces at the receiver plane, the source field is rebuilt from its last
+// two levels (reverse-time restart: S(t-2) = L-step(S(t-1), S(t) - w(t)
+// delta)), and every jt-th level adds (1e-6*R)*S to the image.
+extern "C" int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float d2, float d3, const float *vel2,
+                                 int damp_a, float damp_b, int zs, int xs, int ys, const float *wavelet, int zr,
+                                 const float *data, int jt, float *img, int on_device, double *ms)
+{
+    Ac3D m;
+    TRY(ac_setup(m, n1, n2, n3, nt, d1, d2, d3, vel2, on_device, damp_a, damp_b));
+    RTM_CHECK_ARG(zs >= 1 && zs <= n1 && xs >= 1 && xs <= n2 && ys >= 1 && ys <= n3, "source outside the grid");
+    RTM_CHECK_ARG(zr >= 1 && zr <= n1 && jt >= 1, "bad receiver plane or imaging interval");
+    const long long so = ((long long)(ys - 1) * n2 + (xs - 1)) * n1 + (zs - 1);
+    const size_t dn = (size_t)nt * n2 * n3;
+    DevBuf<float> d, rbuf, ib;
+    const float *dd = data;
+    if (!on_device) {
+        TRY(d.alloc(dn));
+        RTM_CUDA(cudaMemcpy(d.p, data, dn * sizeof(float), cudaMemcpyHostToDevice));
+        dd = d.p;
+    }
+    TRY(ib.alloc(m.vol));
+    RTM_CUDA(cudaMemsetAsync(ib.p, 0, m.vol * sizeof(float), m.st));
+    TRY(rbuf.alloc(2 * m.vol));
+    RTM_CUDA(cudaMemsetAsync(rbuf.p, 0, 2 * m.vol * sizeof(float), m.st));
+    cudaEvent_t e0, e1;
+    RTM_CUDA(cudaEventCreate(&e0));
+    RTM_CUDA(cudaEventCreate(&e1));
+    RTM_CUDA(cudaEventRecord(e0, m.st));
+    float *X, *Y;  // X = S(nt-2), Y = S(nt-1)
+    TRY(ac_forward(m, false, so, wavelet, 1.f, -1, nullptr, &X, &Y));
+    float *r0 = rbuf.p, *r1 = rbuf.p + m.vol;
+    for (int it = nt - 1; it >= 0; it--) {
+        // source level it: S(nt-1) = Y, S(nt-2) = X, else rebuilt
+        const float *S;
+        if (it == nt - 1) S = Y;
+        else if (it == nt - 2) S = X;
+        else {
+            k_inject<<<1, 32, 0, m.st>>>(Y, so, -wavelet[it + 2]);
+            RTM_CUDA(cudaGetLastError());
+            TRY(m.step(Y, X, Y, false, -1, 0.f, -1, nullptr, nullptr, nullptr, nullptr));
+            std::swap(X, Y);  // X = S(it), Y = S(it+1)
+            S = X;
+        }
+        // receiver field level it (+ traces), imaging with S(it)
+        TRY(m.step(r0, r1, r0, true, -1, 0.f, zr - 1, nullptr, dd + (size_t)it * n2 * n3,
+                   it % jt == 0 ? ib.p : nullptr, S));
+        std::swap(r0, r1);
+    }
+    RTM_CUDA(cudaEventRecord(e1, m.st));
+    RTM_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    RTM_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    if (ms) *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    RTM_CUDA(cudaMemcpy(img, ib.p, m.vol * sizeof(float), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+    RTM_CUDA(cudaDeviceSynchronize());
+    return RTM_OK;
+}

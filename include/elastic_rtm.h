@@ -163,6 +163,29 @@ int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, i
               double *dlambda, double *dmu, double *Vx, double *Vz, double *sigmaxx, double *sigmazz,
               double *sigmaxz, int linear, int exact_adjoint);
 
+/* ------------------------------------------------- 3D acoustic (a14, a15)
+ * Single-domain 3D acoustic propagator, 10th order in space (the
+ * reference's W/wave_fkernel.3d8o.cu:31-106 is 8th order), sponge of
+ * W/wave_fkernel.3d8o.cu:183-210 with factor expf(-damp_b*(damp_a-edge)) for
+ * edge distances below damp_a, point source added after each update,
+ * receivers on the plane iz=zr (1-based; 0 = none) recorded into
+ * data[it][iy][ix].  Layout p[(iy*n2+ix)*n1+iz]; vel2 = v^2 dt^2.  Only the
+ * interior [5, n-5) of every axis is updated.  on_device selects device
+ * pointers; *ms receives the device time of the propagation.
+ * acoustic3d_fwd_c_ returns the traces and the last two levels (the state
+ * the reverse-time restart starts from); acoustic3d_rtm_c_ propagates the
+ * source undamped, restarts it backwards from its last two levels
+ * (W/gpu_funcs_3d.cu:509-712) and images every jt-th level. */
+int acoustic3d_fwd_c_(int n1, int n2, int n3, int nt, float d1, float d2, float d3, const float *vel2, int damp_a,
+                      float damp_b, int zs, int xs, int ys, const float *wavelet, int zr, float *data,
+                      float *p_last0, float *p_last1, int on_device, double *ms);
+int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float d2, float d3, const float *vel2, int damp_a,
+                      float damp_b, int zs, int xs, int ys, const float *wavelet, int zr, const float *data, int jt,
+                      float *img, int on_device, double *ms);
+/* Kernel shape of the 3D propagator: tile width 8 or 16 columns and the
+ * number of chunks the y march is split into (0 = chosen from the SM count). */
+int acoustic3d_set(int tile_x, int ychunks);
+
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
  * shots of a survey, each on its own subgrid [x0, x0+nxs) of the full model

@@ -163,8 +163,10 @@ void ora3d_rtm(int n1, int n2, int n3, int nt, int jt, const float *vel, const f
     for (it = nt - 1; it >= 0; it--) {
         if (damp_a > 0) ora3d_damp(n1, n2, n3, damp_a, damp_table, r0, r1);
         ora3d_step(n1, n2, n3, r0, r1, r0, vel, coef);
-        for (iy = 0; iy < n3; iy++)
-            for (ix = 0; ix < n2; ix++)
+        /* traces enter at interior receivers only (rim cells are never
+           updated, so injecting there would accumulate) */
+        for (iy = RAD; iy < n3 - RAD; iy++)
+            for (ix = RAD; ix < n2 - RAD; ix++)
                 r0[A3(zr, ix, iy)] = r0[A3(zr, ix, iy)] + d[(size_t)it * n2 * n3 + (size_t)iy * n2 + ix];
         tmp = r0; r0 = r1; r1 = tmp; /* r1 = R(it) */
         if (it == nt - 1)
@@ -182,4 +184,44 @@ void ora3d_rtm(int n1, int n2, int n3, int nt, int jt, const float *vel, const f
             for (i = 0; i < tot; i++) img[i] = img[i] + (1e-6f * r1[i]) * S[i];
     }
     free(X); free(Y); free(r0); free(r1);
+}
+
+/* Forward modelling keeping every level: hist[it] = level it (as stored by
+   ora3d_forward before the next damping).  Test helper for the reverse-time
+   restart property. */
+void ora3d_forward_history(int n1, int n2, int n3, int nt, const float *vel, const float *coef, const float *src,
+                           int zs, int xs, int ys, float *hist)
+{
+    size_t tot = (size_t)n1 * n2 * n3;
+    float *a = (float *)calloc(tot, sizeof(float)), *b = (float *)calloc(tot, sizeof(float)), *tmp;
+    int it;
+    for (it = 0; it < nt; it++) {
+        ora3d_step(n1, n2, n3, a, b, a, vel, coef);
+        a[A3(zs, xs, ys)] = a[A3(zs, xs, ys)] + src[it];
+        memcpy(hist + (size_t)it * tot, a, tot * sizeof(float));
+        tmp = a; a = b; b = tmp;
+    }
+    free(a); free(b);
+}
+
+/* 3D RTM imaging with the source field read from a stored history instead
+   of the reverse-time restart (same receiver side as ora3d_rtm). */
+void ora3d_rtm_stored(int n1, int n2, int n3, int nt, int jt, const float *vel, const float *coef, int damp_a,
+                      const float *damp_table, const float *hist, int zr, const float *d, float *img)
+{
+    size_t tot = (size_t)n1 * n2 * n3, i;
+    float *r0 = (float *)calloc(tot, sizeof(float)), *r1 = (float *)calloc(tot, sizeof(float)), *tmp;
+    int it, ix, iy;
+    memset(img, 0, tot * sizeof(float));
+    for (it = nt - 1; it >= 0; it--) {
+        if (damp_a > 0) ora3d_damp(n1, n2, n3, damp_a, damp_table, r0, r1);
+        ora3d_step(n1, n2, n3, r0, r1, r0, vel, coef);
+        for (iy = RAD; iy < n3 - RAD; iy++)
+            for (ix = RAD; ix < n2 - RAD; ix++)
+                r0[A3(zr, ix, iy)] = r0[A3(zr, ix, iy)] + d[(size_t)it * n2 * n3 + (size_t)iy * n2 + ix];
+        tmp = r0; r0 = r1; r1 = tmp;
+        if (it % jt == 0)
+            for (i = 0; i < tot; i++) img[i] = img[i] + (1e-6f * r1[i]) * hist[(size_t)it * tot + i];
+    }
+    free(r0); free(r1);
 }

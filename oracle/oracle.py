@@ -258,3 +258,21 @@ def acoustic_rtm(vel2, coef, damp_a, table, src_pos, wavelet, zr, d, jt):
     lib().ora3d_rtm(n1, n2, n3, nt, jt, _p(vel2), _p(coef), damp_a, _p(table), zs, xs, ys, _p(wavelet), zr,
                     _p(np.ascontiguousarray(d)), _p(img))
     return img
+
+
+def acoustic_forward_history(vel2, coef, src_pos, wavelet):
+    n3, n2, n1 = vel2.shape
+    nt = wavelet.shape[0]
+    h = np.zeros((nt, n3, n2, n1), np.float32)
+    zs, xs, ys = src_pos
+    lib().ora3d_forward_history(n1, n2, n3, nt, _p(vel2), _p(coef), _p(wavelet), zs, xs, ys, _p(h))
+    return h
+
+
+def acoustic_rtm_stored(vel2, coef, damp_a, table, hist, zr, d, jt):
+    n3, n2, n1 = vel2.shape
+    nt = hist.shape[0]
+    img = np.zeros_like(vel2)
+    lib().ora3d_rtm_stored(n1, n2, n3, nt, jt, _p(vel2), _p(coef), damp_a, _p(table), _p(np.ascontiguousarray(hist)),
+                           zr, _p(np.ascontiguousarray(d)), _p(img))
+    return img
