@@ -72,6 +72,32 @@ __global__ void k_stack(const ShotGeom *shots, int shot, int ld, int nz, long lo
     for (int i = 0; i < 3; i++) full[i * plane_full + f] += img[i * gplane + o] - cmp[i * gplane + o];
 }
 
+// Blocked compensated imaging: totals (sum, compensation) += partial planes
+// with Kahan's update, then the partials restart from zero.  The three image
+// planes of a group are contiguous, so one launch covers n4 float4 words.
+__global__ void k_fold(long long n4, float4 *sum, float4 *cmp, float4 *part)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+        const float4 p = part[i];
+        float4 sv = sum[i], cv = cmp[i];
+        float *sa = &sv.x, *ca = &cv.x;
+        const float pa[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float y = pa[j] - ca[j];
+            const float t = sa[j] + y;
+            ca[j] = (t - sa[j]) - y;
+            sa[j] = t;
+        }
+        sum[i] = sv;
+        cmp[i] = cv;
+        part[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// levels accumulated in FP32 partial planes between two folds
+constexpr int IMG_FOLD = 32;
+
 }  // namespace
 
 struct rtm_batch {
@@ -87,7 +113,8 @@ struct rtm_batch {
     ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
     ShotTable tab_a;  // adjoint pass work items
     int tx_f = 0, tx_a = 0;          // tile widths chosen by the autotuner (0 = heuristic)
-    double tune_ms[2][3] = {{0}};    // measured ms per step, [pass][tx 8,16,32]
+    int st_f = 1, st_a = 1;          // staging buffers per CTA chosen by the autotuner
+    double tune_ms[2][3][2] = {};    // measured ms per step, [pass][tx 8,16,32][stages 1,2]
     std::vector<float> dtsrc;
     cudaStream_t st = nullptr;
     double last_fwd_ms = 0, last_adj_ms = 0, last_total_ms = 0;
@@ -143,6 +170,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     RTM_CHECK_ARG(col <= b->cap_cols, "group wider than the batch capacity");
     b->tab.ldz = ld;
     const int tz = kernel_version() == 1 ? TZ_TILE : TZ_TILE2;  // batch planes are always v2-aligned
+    int stf = 1, sta = 1;  // staging buffers per CTA of the two passes
     {
         const int heur = pick_tile_width((long long)nz, col, tz);
         int heur_a = heur;
@@ -154,6 +182,8 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         b->tab_a.shots = b->tab.shots;
         b->tab_a.ldz = ld;
         TRY(b->tab_a.build(txa, tz));
+        if (tz == TZ_TILE2 && v2_fits(false, false, txf, b->st_f)) stf = b->st_f;
+        if (tz == TZ_TILE2 && v2_fits(true, false, txa, b->st_a)) sta = b->st_a;
     }
     RTM_CUDA(cudaMemcpyAsync(b->dx0.p, x0g.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
     const long long gp = b->gplane;
@@ -187,11 +217,28 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     // ---- state
     RTM_CUDA(cudaMemsetAsync(b->F.p, 0, 10 * gp * sizeof(float), st));
     RTM_CUDA(cudaMemsetAsync(b->A.p, 0, 10 * gp * sizeof(float), st));
-    RTM_CUDA(cudaMemsetAsync(b->img.p, 0, 6 * gp * sizeof(float), st));
+    RTM_CUDA(cudaMemsetAsync(b->img.p, 0, 9 * gp * sizeof(float), st));
     RTM_CUDA(cudaMemsetAsync(b->maxes.p, 0, (size_t)(nt + 2) * b->group_max * 2 * sizeof(float), st));
 
     auto fb = [&](int par, int f) { return b->F.p + (par * 5 + f) * gp; };
     auto ab = [&](int par, int f) { return b->A.p + (par * 5 + f) * gp; };
+    // v2 images: FP32 partial planes folded every IMG_FOLD levels; the v1
+    // kernel keeps per-level Kahan updates of the totals
+    const bool blocked = tz == TZ_TILE2;
+    auto set_img = [&](Step2DArgs<float> &a) {
+        for (int i = 0; i < 3; i++) {
+            a.img[i] = b->img.p + (blocked ? 6 + i : i) * gp;
+            a.imgc[i] = blocked ? nullptr : b->img.p + (3 + i) * gp;
+        }
+    };
+    auto fold = [&]() -> int {
+        const long long n4 = 3 * gp / 4;
+        const int grid = (int)std::min<long long>(ceil_div((int)std::min<long long>(n4, 1LL << 30), 256), 8LL * device_sm_count());
+        k_fold<<<grid, 256, 0, st>>>(n4, reinterpret_cast<float4 *>(b->img.p), reinterpret_cast<float4 *>(b->img.p + 3 * gp),
+                                    reinterpret_cast<float4 *>(b->img.p + 6 * gp));
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    };
     auto snap = [&](int L, int f) { return b->snaps.p + ((size_t)(L - 1) * 2 + f) * gp; };  // level L (1-based)
     auto mx = [&](int L) { return b->maxes.p + (size_t)L * b->group_max * 2; };
     const float inv_dt = 1.0f / b->dt, inv_dx = 1.0f / b->dx;
@@ -215,9 +262,9 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     {
         Step2DArgs<float> a = base_args(false);
         a.ntiles = 0;
-        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz));
+        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf));
         a.img[0] = b->img.p;
-        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz));
+        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta));
     }
 
     if (tune_steps > 0) {
@@ -229,46 +276,48 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         const int cand[3] = {8, 16, 32};
         for (int pass = 0; pass < 2; pass++) {
             double best = 1e30;
-            int bx = cand[0];
-            for (int ci = 0; ci < 3; ci++) {
-                if (tz == TZ_TILE2 && !v2_fits(pass == 1, false, cand[ci])) {
-                    b->tune_ms[pass][ci] = -1;  // does not fit in shared memory
-                    continue;
-                }
-                ShotTable &tb = pass ? b->tab_a : b->tab;
-                TRY(tb.build(cand[ci], tz));
-                for (int rep = 0; rep < 2; rep++) {  // first round warms up
-                    RTM_CUDA(cudaEventRecord(t0, st));
-                    for (int k = 0; k < tune_steps; k++) {
-                        const int L = 3 + (k & 1);
-                        Step2DArgs<float> a = base_args(pass == 1);
-                        for (int f = 0; f < 5; f++) {
-                            a.out[f] = pass ? ab(L & 1, f) : fb(L & 1, f);
-                            a.own2[f] = a.out[f];
-                            a.nb[f] = pass ? ab((L + 1) & 1, f) : fb((L + 1) & 1, f);
-                        }
-                        if (!pass) {
-                            a.sponge = 1;
-                            a.snap_out[0] = snap(1, 0);
-                            a.snap_out[1] = snap(1, 1);
-                            a.snap_max_in = mx(1);
-                            a.snap_max_out = mx(2);
-                        } else {
-                            a.rec = b->traces.p; a.comp_mask = b->comp_mask; a.ncomp = b->ncomp; a.it = 0;
-                            a.isnap0[0] = snap(1, 0); a.isnap0[1] = snap(1, 1); a.imax0 = mx(1);
-                            a.isnap1[0] = snap(2, 0); a.isnap1[1] = snap(2, 1); a.imax1 = mx(2);
-                            for (int i = 0; i < 3; i++) { a.img[i] = b->img.p + i * gp; a.imgc[i] = b->img.p + (3 + i) * gp; }
-                        }
-                        TRY(launch_step<float>(a, pass == 1, false, tb.tx, 0, st, tb.tz));
+            int bx = cand[0], bs = 1;
+            for (int ci = 0; ci < 3; ci++)
+                for (int ns_ = 1; ns_ <= 2; ns_++) {
+                    if (tz != TZ_TILE2 ? ns_ > 1 : !v2_fits(pass == 1, false, cand[ci], ns_)) {
+                        b->tune_ms[pass][ci][ns_ - 1] = -1;  // does not fit in shared memory
+                        continue;
                     }
-                    RTM_CUDA(cudaEventRecord(t1, st));
-                    RTM_CUDA(cudaEventSynchronize(t1));
+                    ShotTable &tb = pass ? b->tab_a : b->tab;
+                    TRY(tb.build(cand[ci], tz));
+                    for (int rep = 0; rep < 2; rep++) {  // first round warms up
+                        RTM_CUDA(cudaEventRecord(t0, st));
+                        for (int k = 0; k < tune_steps; k++) {
+                            const int L = 3 + (k & 1);
+                            Step2DArgs<float> a = base_args(pass == 1);
+                            for (int f = 0; f < 5; f++) {
+                                a.out[f] = pass ? ab(L & 1, f) : fb(L & 1, f);
+                                a.own2[f] = a.out[f];
+                                a.nb[f] = pass ? ab((L + 1) & 1, f) : fb((L + 1) & 1, f);
+                            }
+                            if (!pass) {
+                                a.sponge = 1;
+                                a.snap_out[0] = snap(1, 0);
+                                a.snap_out[1] = snap(1, 1);
+                                a.snap_max_in = mx(1);
+                                a.snap_max_out = mx(2);
+                            } else {
+                                a.rec = b->traces.p; a.comp_mask = b->comp_mask; a.ncomp = b->ncomp; a.it = 0;
+                                a.isnap0[0] = snap(1, 0); a.isnap0[1] = snap(1, 1); a.imax0 = mx(1);
+                                a.isnap1[0] = snap(2, 0); a.isnap1[1] = snap(2, 1); a.imax1 = mx(2);
+                                set_img(a);
+                            }
+                            TRY(launch_step<float>(a, pass == 1, false, tb.tx, 0, st, tb.tz, ns_));
+                        }
+                        RTM_CUDA(cudaEventRecord(t1, st));
+                        RTM_CUDA(cudaEventSynchronize(t1));
+                    }
+                    float ms = 0;
+                    RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+                    b->tune_ms[pass][ci][ns_ - 1] = ms / tune_steps;
+                    if (ms < best) { best = ms; bx = cand[ci]; bs = ns_; }
                 }
-                float ms = 0;
-                RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-                b->tune_ms[pass][ci] = ms / tune_steps;
-                if (ms < best) { best = ms; bx = cand[ci]; }
-            }
+            if (pass) b->st_a = bs; else b->st_f = bs;
             if (pass) b->tx_a = bx; else b->tx_f = bx;
         }
         cudaEventDestroy(t0);
@@ -298,7 +347,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.snap_out[1] = snap(L - 1, 1);
             a.snap_max_in = mx(L - 1);
             a.snap_max_out = mx(L);
-            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz));
+            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf));
             nkern++;
         }
         dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
@@ -328,12 +377,13 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.isnap1[0] = L < nt ? snap(L + 1, 0) : snap(L, 0);
             a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
             a.imax1 = L < nt ? mx(L + 1) : mx(L);
-            for (int i = 0; i < 3; i++) {
-                a.img[i] = b->img.p + i * gp;
-                a.imgc[i] = b->img.p + (3 + i) * gp;
-            }
-            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz));
+            set_img(a);
+            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta));
             nkern++;
+            if (blocked && ((nt - L + 1) % IMG_FOLD == 0 || L == 1)) {
+                TRY(fold());
+                nkern++;
+            }
         }
         return RTM_OK;
     };
@@ -465,7 +515,7 @@ extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float d
     if (!s) s = b->F.alloc(10 * gp);
     if (!s) s = b->A.alloc(10 * gp);
     if (!s) s = b->zero.alloc(gp);
-    if (!s) s = b->img.alloc(6 * gp);
+    if (!s) s = b->img.alloc(9 * gp);  // sums, compensations, partials
     if (!s) s = b->filt.alloc(abc + 5);
     if (!s) s = b->maxes.alloc((size_t)(nt + 2) * b->group_max * 2);
     if (!s) s = b->traces.alloc((size_t)tcap);
@@ -547,7 +597,14 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[6] = (double)b->tab.ntiles;
     out[7] = (double)(b->tx_a > 0 ? b->tx_a : b->tab_a.tx);
     for (int p = 0; p < 2; p++)
-        for (int i = 0; i < 3; i++) out[8 + 3 * p + i] = b->tune_ms[p][i];
+        for (int i = 0; i < 3; i++) {
+            const double m1 = b->tune_ms[p][i][0], m2 = b->tune_ms[p][i][1];
+            out[8 + 3 * p + i] = m1 < 0 ? m2 : (m2 < 0 ? m1 : std::min(m1, m2));
+            out[16 + 6 * p + 2 * i] = m1;
+            out[17 + 6 * p + 2 * i] = m2;
+        }
+    out[14] = b->st_f;
+    out[15] = b->st_a;
     return RTM_OK;
 }
 
@@ -560,11 +617,21 @@ extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
     return RTM_OK;
 }
 
+extern "C" int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj)
+{
+    RTM_CHECK_ARG(b, "null argument");
+    RTM_CHECK_ARG(fwd >= 1 && fwd <= 2 && adj >= 1 && adj <= 2, "stages must be 1 or 2");
+    b->st_f = fwd;
+    b->st_a = adj;
+    return RTM_OK;
+}
+
 extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
 {
     RTM_CHECK_ARG(b && steps > 0, "bad arguments");
     TRY(ensure_device());
     b->tx_f = b->tx_a = 0;
+    b->st_f = b->st_a = 1;
     // traces are not read during tuning beyond the receiver row; use the
     // staging buffer content as is
     TRY(batch_group(b, shot0, nshot, b->tstage.p, 1, b->full.p, 1, steps));

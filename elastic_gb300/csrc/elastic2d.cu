@@ -117,21 +117,43 @@ bool v2_fits(bool adj, bool exact, int tx)
     return need <= (size_t)max_smem_optin();
 }
 
+bool v2_fits(bool adj, bool exact, int tx, int stages)
+{
+    return stages >= 1 && stages <= 2 && v2_fits(adj, exact, tx) &&
+           (size_t)stages * v2_stage_bytes(adj, exact, tx) <= (size_t)max_smem_optin();
+}
+
+size_t v2_stage_bytes(bool adj, bool exact, int tx)
+{
+    switch (tx) {
+    case 8: return adj ? (exact ? v2_smem<true, true, 8>(true) : v2_smem<true, false, 8>(true)) : v2_smem<false, false, 8>(false);
+    case 16: return adj ? (exact ? v2_smem<true, true, 16>(true) : v2_smem<true, false, 16>(true)) : v2_smem<false, false, 16>(false);
+    case 32: return adj ? (exact ? v2_smem<true, true, 32>(true) : v2_smem<true, false, 32>(true)) : v2_smem<false, false, 32>(false);
+    default: return 0;
+    }
+}
+
 template <bool EXACT, bool ADJ, int TX>
-static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t st)
+static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t st, int stages)
 {
     auto kern = k_step2d_v2<EXACT, ADJ, TX>;
     const bool img = ADJ && a.img[0] != nullptr;
-    const size_t smem = v2_smem<ADJ, EXACT, TX>(img);
-    RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX), "tile width %d needs more shared memory than a block can use", TX);
-    static int grid_max[2] = {0, 0};
-    if (!grid_max[img]) {
-        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v2_smem<ADJ, EXACT, TX>(true)));
+    RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX, stages), "tile width %d with %d stages needs more shared memory than a block can use",
+                  TX, stages);
+    const size_t smem = (size_t)stages * v2_smem<ADJ, EXACT, TX>(img);
+    static bool attr_set = false;
+    static int grid_max[2][2] = {{0, 0}, {0, 0}};
+    if (!attr_set) {
+        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin()));
+        attr_set = true;
+    }
+    int &gm = grid_max[img][stages - 1];
+    if (!gm) {
         int nb = 0;
         RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
-        grid_max[img] = (nb > 0 ? nb : 1) * device_sm_count();
+        gm = (nb > 0 ? nb : 1) * device_sm_count();
     }
-    int grid = a.ntiles < grid_max[img] ? a.ntiles : grid_max[img];
+    int grid = a.ntiles < gm ? a.ntiles : gm;
     if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
     if (grid <= 0) return RTM_OK;
     kern<<<grid, 256, smem, st>>>(a);
@@ -140,12 +162,12 @@ static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t s
 }
 
 template <bool EXACT, bool ADJ>
-static int launch_v2(const Step2DArgs<float> &a, int tx, int grid_cap, cudaStream_t st)
+static int launch_v2(const Step2DArgs<float> &a, int tx, int grid_cap, cudaStream_t st, int stages)
 {
     switch (tx) {
-    case 8: return launch_v2_tx<EXACT, ADJ, 8>(a, grid_cap, st);
-    case 16: return launch_v2_tx<EXACT, ADJ, 16>(a, grid_cap, st);
-    case 32: return launch_v2_tx<EXACT, ADJ, 32>(a, grid_cap, st);
+    case 8: return launch_v2_tx<EXACT, ADJ, 8>(a, grid_cap, st, stages);
+    case 16: return launch_v2_tx<EXACT, ADJ, 16>(a, grid_cap, st, stages);
+    case 32: return launch_v2_tx<EXACT, ADJ, 32>(a, grid_cap, st, stages);
     default: rtm_set_error("unsupported tile width %d", tx); return RTM_ERR_ARG;
     }
 }
@@ -171,7 +193,7 @@ bool v2_usable(bool is_float, int ldz, const void *const *ptrs, int n)
 }
 
 template <typename T>
-int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz)
+int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz, int stages)
 {
     if constexpr (std::is_same<T, float>::value) {
         if (tz == TZ_TILE2) {
@@ -179,15 +201,15 @@ int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_c
                 rtm_set_error("v2 step launched on an unaligned layout");
                 return RTM_ERR_ARG;
             }
-            if (adj) return exact ? launch_v2<true, true>(a, tx, grid_cap, st) : launch_v2<false, true>(a, tx, grid_cap, st);
-            return exact ? launch_v2<true, false>(a, tx, grid_cap, st) : launch_v2<false, false>(a, tx, grid_cap, st);
+            if (adj) return exact ? launch_v2<true, true>(a, tx, grid_cap, st, stages) : launch_v2<false, true>(a, tx, grid_cap, st, stages);
+            return exact ? launch_v2<true, false>(a, tx, grid_cap, st, stages) : launch_v2<false, false>(a, tx, grid_cap, st, stages);
         }
     }
     if (adj) return exact ? launch_step_e<T, true, true>(a, tx, grid_cap, st) : launch_step_e<T, false, true>(a, tx, grid_cap, st);
     return exact ? launch_step_e<T, true, false>(a, tx, grid_cap, st) : launch_step_e<T, false, false>(a, tx, grid_cap, st);
 }
-template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t, int);
-template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t, int);
+template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t, int, int);
+template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t, int, int);
 
 // ------------------------------------------------------------- batch table
 int ShotTable::build(int tx_, int tz_)

@@ -10,7 +10,13 @@
 //    is in flight at once instead of being loaded through registers;
 //  * each thread owns 4 consecutive z cells of TX/8 columns: x-stencils read
 //    one 128-bit shared word per tap, z-stencils read a 20-value window in
-//    five 128-bit words, own/coefficient/output traffic is float4.
+//    five 128-bit words, own/coefficient/output traffic is float4;
+//  * with twice the stage size of dynamic shared memory the CTA stages its
+//    next work item while it computes the current one (two stages);
+//  * fused imaging reads the FP16 snapshots as 4-half words and adds the
+//    level's image terms either with per-level Kahan compensation (imgc set)
+//    or into FP32 partial planes that the caller folds into compensated
+//    totals every few levels (imgc null).
 // Requirements (checked by the launcher): ldz % 4 == 0, 16-byte aligned
 // planes, rows [nz, ldz) of staged planes zero.
 #pragma once
@@ -169,7 +175,7 @@ struct V2Arr {
 // Shared memory of a v2 launch: NRAW float arrays (+ 2 FP16 snapshot arrays
 // for fused imaging, stored as halves).
 template <bool ADJ, bool EXACT, int TX>
-constexpr size_t v2_smem(bool img)
+__host__ __device__ constexpr size_t v2_smem(bool img)
 {
     return (size_t)V2Arr<ADJ, EXACT>::NRAW * V2<TX>::SIZE * sizeof(float) +
            (ADJ && img ? (size_t)2 * V2<TX>::SIZE * sizeof(__half) : 0);
@@ -178,48 +184,88 @@ constexpr size_t v2_smem(bool img)
 template <typename V>
 __device__ __forceinline__ float4 ld_f4(const V *p) { return *reinterpret_cast<const float4 *>(p); }
 
+// 4 halves at (column x, rows z..z+3) of FP16 array `arr` (z multiple of 4).
+template <int TX>
+__device__ __forceinline__ float4 ldh4(const __half *smh, int arr, int x, int z)
+{
+    const uint2 u = *reinterpret_cast<const uint2 *>(smh + arr * V2<TX>::SIZE + (x + HALO) * V2_LZ + (z + V2_ZH));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// Issue the cp.async staging of work item t into the stage at `sm`.
+template <bool ADJ, int TX>
+__device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, float *sm, bool img)
+{
+    constexpr int NRAW = V2Arr<ADJ, false>::NRAW;
+    constexpr int SZ = V2<TX>::SIZE;
+    __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
+    const int s = find_shot<float>(a.shots, a.nshots, t);
+    const ShotGeom &g = a.shots[s];
+    const int lt = t - g.tile0;
+    const int tz0 = (lt % g.ntz) * V2_TZ, tx0 = (lt / g.ntz) * TX;
+    const int nz = g.nz, nx = g.nx, ldz = a.ldz;
+    for (int c = threadIdx.x; c < V2<TX>::CHUNKS; c += blockDim.x) {
+        const int col = c / (V2_LZ / 4), zc = c - col * (V2_LZ / 4);
+        const int gx = tx0 - HALO + col, gz = tz0 - V2_ZH + 4 * zc;
+        const bool ok = (gx >= 0) & (gx < nx) & (gz >= 0) & (gz < ldz);
+        const long long o = ok ? g.off + (long long)gx * ldz + gz : 0;
+        const int so = col * V2_LZ + 4 * zc;
+#pragma unroll
+        for (int f = 0; f < 5; f++) cp_async16(sm + f * SZ + so, a.nb[f] + o, ok);
+        if (ADJ) {
+#pragma unroll
+            for (int f = 0; f < 5; f++) cp_async16(sm + (5 + f) * SZ + so, a.coef[f] + o, ok);
+            if (img) {
+                const bool oks = ok & (gz < nz);
+                cp_async8(smh + so, a.isnap0[0] + o, oks);
+                cp_async8(smh + SZ + so, a.isnap0[1] + o, oks);
+            }
+        }
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+}
+
 template <bool EXACT, bool ADJ, int TX>
 __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2DArgs<float> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *sm = reinterpret_cast<float *>(smem_raw);
     constexpr int NRAW = V2Arr<ADJ, EXACT>::NRAW;
     constexpr int SZ = V2<TX>::SIZE;
     constexpr int CW = TX / 8;  // columns per warp
-    __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool img = ADJ && a.img[0] != nullptr;
+    // one or two stages, depending on the shared memory this launch received
+    unsigned dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    const size_t stage_bytes = v2_smem<ADJ, EXACT, TX>(img);
+    const bool dbuf = dyn >= 2 * stage_bytes;
+    auto stage = [&](int k) { return reinterpret_cast<float *>(smem_raw + (k ? stage_bytes : 0)); };
 
+    int cur = 0;
+    if (blockIdx.x < a.ntiles) v2_stage<ADJ, TX>(a, blockIdx.x, stage(0), img);
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        float *sm = stage(cur);
+        __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
+        if (dbuf) {
+            if (tn < a.ntiles) {
+                v2_stage<ADJ, TX>(a, tn, stage(cur ^ 1), img);
+                asm volatile("cp.async.wait_group 1;\n" ::);
+            } else {
+                asm volatile("cp.async.wait_group 0;\n" ::);
+            }
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+        }
+        __syncthreads();
         const int s = find_shot<float>(a.shots, a.nshots, t);
         const ShotGeom g = a.shots[s];
         const int lt = t - g.tile0;
         const int tz0 = (lt % g.ntz) * V2_TZ, tx0 = (lt / g.ntz) * TX;
         const long long off = g.off;
         const int nz = g.nz, nx = g.nx, ldz = a.ldz;
-
-        __syncthreads();  // previous tile consumed
-        // ---- asynchronous staging
-        for (int c = threadIdx.x; c < V2<TX>::CHUNKS; c += blockDim.x) {
-            const int col = c / (V2_LZ / 4), zc = c - col * (V2_LZ / 4);
-            const int gx = tx0 - HALO + col, gz = tz0 - V2_ZH + 4 * zc;
-            const bool ok = (gx >= 0) & (gx < nx) & (gz >= 0) & (gz < ldz);
-            const long long o = ok ? off + (long long)gx * ldz + gz : 0;
-            const int so = col * V2_LZ + 4 * zc;
-#pragma unroll
-            for (int f = 0; f < 5; f++) cp_async16(sm + f * SZ + so, a.nb[f] + o, ok);
-            if (ADJ) {
-#pragma unroll
-                for (int f = 0; f < 5; f++) cp_async16(sm + (5 + f) * SZ + so, a.coef[f] + o, ok);
-                if (img) {
-                    const bool oks = ok & (gz < nz);
-                    cp_async8(smh + so, a.isnap0[0] + o, oks);
-                    cp_async8(smh + SZ + so, a.isnap0[1] + o, oks);
-                }
-            }
-        }
-        cp_async_wait_all();
-        __syncthreads();
         if (ADJ && !EXACT) {
             // products coef*field in place (slots 0..6 of the 10 raw arrays)
             for (int e = threadIdx.x; e < SZ; e += blockDim.x) {
@@ -418,51 +464,71 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
             }
             if (img) {
                 // imaging condition of level it (W/image-mod-rtm.f90:146-162)
+                // on the dequantised source snapshots: x taps are 8-byte
+                // reads of 4 halves, z taps come from a 20-row window
                 const float d0 = a.imax0[2 * s] * (1.0f / SNAP_Q), d1 = a.imax0[2 * s + 1] * (1.0f / SNAP_Q);
-                auto SV = [&](int arr, int dx_, int dz_) {
-                    return __half2float(smh[arr * SZ + (x + dx_ + HALO) * V2_LZ + (z + dz_ + V2_ZH)]);
-                };
-                float s1[4], s2[4], s4[4], s5[4], s6[4];
+                float wx[20], wz[20];  // z windows of source Vx and Vz, rows z-8..z+11 (raw halves)
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    s1[j] = s2[j] = s4[j] = s5[j] = s6[j] = 0.f;
-                    const int cz = gz + j;
-                    if (!a.ilast) {
-                        const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
-                        s1[j] = a.inv_dt * (__half2float(a.isnap1[0][o + j]) * e0 - SV(0, 0, j) * d0);
-                        s2[j] = a.inv_dt * (__half2float(a.isnap1[1][o + j]) * e1 - SV(1, 0, j) * d1);
+                for (int q = 0; q < 5; q++) {
+                    const float4 tx_ = ldh4<TX>(smh, 0, x, z - 8 + 4 * q), tz_ = ldh4<TX>(smh, 1, x, z - 8 + 4 * q);
+                    wx[4 * q] = tx_.x; wx[4 * q + 1] = tx_.y; wx[4 * q + 2] = tx_.z; wx[4 * q + 3] = tx_.w;
+                    wz[4 * q] = tz_.x; wz[4 * q + 1] = tz_.y; wz[4 * q + 2] = tz_.z; wz[4 * q + 3] = tz_.w;
+                }
+                float p4[4] = {0.f, 0.f, 0.f, 0.f}, p7[4] = {0.f, 0.f, 0.f, 0.f};  // x taps: Vx (P), Vz (M)
+#pragma unroll
+                for (int k = 0; k < 5; k++) {
+                    const float c = StagCoef<float>::c(k);
+                    const float4 ap = ldh4<TX>(smh, 0, x + 5 - k, z), am = ldh4<TX>(smh, 0, x - 4 + k, z);
+                    const float4 bp = ldh4<TX>(smh, 1, x + 4 - k, z), bm = ldh4<TX>(smh, 1, x - 5 + k, z);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        p4[j] += c * (f4(ap, j) - f4(am, j));
+                        p7[j] += c * (f4(bp, j) - f4(bm, j));
                     }
-                    if (cz >= 4 && cz <= nz - 6 && gx >= 4 && gx <= nx - 6) {
-                        float p4 = 0.f, p5 = 0.f;
+                }
+                float s1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f};
+                if (!a.ilast) {
+                    const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
+                    const uint2 u0 = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
+                    const uint2 u1 = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
+                    const float2 a0 = __half22float2(*reinterpret_cast<const __half2 *>(&u0.x));
+                    const float2 a1 = __half22float2(*reinterpret_cast<const __half2 *>(&u0.y));
+                    const float2 b0 = __half22float2(*reinterpret_cast<const __half2 *>(&u1.x));
+                    const float2 b1 = __half22float2(*reinterpret_cast<const __half2 *>(&u1.y));
+                    const float nx4[4] = {a0.x, a0.y, a1.x, a1.y}, nz4[4] = {b0.x, b0.y, b1.x, b1.y};
 #pragma unroll
-                        for (int k = 0; k < 5; k++) {
-                            p4 += StagCoef<float>::c(k) * (SV(0, 5 - k, j) - SV(0, -4 + k, j));
-                            p5 += StagCoef<float>::c(k) * (SV(1, 0, j + 5 - k) - SV(1, 0, j - 4 + k));
-                        }
-                        s4[j] = p4 * d0 * a.inv_dx;
-                        s5[j] = p5 * d1 * a.inv_dx;
-                    }
-                    if (cz >= 5 && cz <= nz - 6 && gx >= 5 && gx <= nx - 6) {
-                        float p6 = 0.f, p7 = 0.f;
-#pragma unroll
-                        for (int k = 0; k < 5; k++) {
-                            p6 += StagCoef<float>::c(k) * (SV(0, 0, j + 4 - k) - SV(0, 0, j - 5 + k));
-                            p7 += StagCoef<float>::c(k) * (SV(1, 4 - k, j) - SV(1, -5 + k, j));
-                        }
-                        s6[j] = (p6 * d0 + p7 * d1) * a.inv_dx;
+                    for (int j = 0; j < 4; j++) {
+                        s1[j] = a.inv_dt * (nx4[j] * e0 - wx[8 + j] * d0);
+                        s2[j] = a.inv_dt * (nz4[j] * e1 - wz[8 + j] * d1);
                     }
                 }
                 float tt[3][4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
-                    const float s3 = s4[j] + s5[j];
+                    const int cz = gz + j;
+                    float s4 = 0.f, s5 = 0.f, s6 = 0.f;
+                    if (cz >= 4 && cz <= nz - 6 && gx >= 4 && gx <= nx - 6) {
+                        float p5 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 5; k++) p5 += StagCoef<float>::c(k) * (wz[8 + j + 5 - k] - wz[8 + j - 4 + k]);
+                        s4 = p4[j] * d0 * a.inv_dx;
+                        s5 = p5 * d1 * a.inv_dx;
+                    }
+                    if (cz >= 5 && cz <= nz - 6 && gx >= 5 && gx <= nx - 6) {
+                        float p6 = 0.f;
+#pragma unroll
+                        for (int k = 0; k < 5; k++) p6 += StagCoef<float>::c(k) * (wx[8 + j + 4 - k] - wx[8 + j - 5 + k]);
+                        s6 = (p6 * d0 + p7[j] * d1) * a.inv_dx;
+                    }
+                    const float s3 = s4 + s5;
                     tt[0][j] = v[VX][j] * s1[j] + v[VZ][j] * s2[j];
                     tt[1][j] = -(v[SXX][j] + v[SZZ][j]) * s3;
-                    tt[2][j] = -(2.f * v[SXX][j] * s4[j] + 2.f * v[SZZ][j] * s5[j] + v[SXZ][j] * s6[j]);
+                    tt[2][j] = -(2.f * v[SXX][j] * s4 + 2.f * v[SZZ][j] * s5 + v[SXZ][j] * s6);
                 }
 #pragma unroll
                 for (int i = 0; i < 3; i++) {
-                    if (nval == 4) {
+                    if (a.imgc[i] && nval == 4) {
+                        // per-level Kahan compensation
                         float4 sv = ld_f4(a.img[i] + o), cv = ld_f4(a.imgc[i] + o);
                         float sa[4] = {sv.x, sv.y, sv.z, sv.w}, ca[4] = {cv.x, cv.y, cv.z, cv.w};
 #pragma unroll
@@ -474,7 +540,7 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
                         }
                         *reinterpret_cast<float4 *>(a.img[i] + o) = make_float4(sa[0], sa[1], sa[2], sa[3]);
                         *reinterpret_cast<float4 *>(a.imgc[i] + o) = make_float4(ca[0], ca[1], ca[2], ca[3]);
-                    } else {
+                    } else if (a.imgc[i]) {
                         for (int j = 0; j < nval; j++) {
                             float sj = a.img[i][o + j], cj = a.imgc[i][o + j];
                             const float y = tt[i][j] - cj;
@@ -483,6 +549,14 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
                             a.img[i][o + j] = tsum;
                             a.imgc[i][o + j] = cj;
                         }
+                    } else if (nval == 4) {
+                        // FP32 partial sums, folded into compensated totals
+                        // by the caller every few levels
+                        float4 sv = ld_f4(a.img[i] + o);
+                        sv.x += tt[i][0]; sv.y += tt[i][1]; sv.z += tt[i][2]; sv.w += tt[i][3];
+                        *reinterpret_cast<float4 *>(a.img[i] + o) = sv;
+                    } else {
+                        for (int j = 0; j < nval; j++) a.img[i][o + j] += tt[i][j];
                     }
                 }
             }
@@ -498,6 +572,9 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
                 atomic_max_abs(a.snap_max_out + 2 * s + 1, wmax1);
             }
         }
+        __syncthreads();  // the stage is free for the prefetch of the next iteration
+        cur ^= dbuf ? 1 : 0;
+        if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img);
     }
 }
 
