@@ -249,10 +249,11 @@ def run_gpu(args):
                    "group_shots": args.group, "inputs_vs_l2": "inputs larger than L2 (snapshots ~150 GB)",
                    "tile": {"forward_tx": tune["tile_x"], "adjoint_tx": tune["tile_x_adj"], "tz": 128,
                             "forward_stages": tune["stages"], "adjoint_stages": tune["stages_adj"],
-                            "autotune_ms_per_launch_fwd_8_16_32_x_stages_1_2":
-                                [[round(x, 4) for x in r] for r in tune["tune_ms_fwd_stages"]],
-                            "autotune_ms_per_launch_adj_8_16_32_x_stages_1_2":
-                                [[round(x, 4) for x in r] for r in tune["tune_ms_adj_stages"]]},
+                            "forward_threads": tune["threads"], "adjoint_threads": tune["threads_adj"],
+                            "autotune_ms_per_launch_fwd_tx8_16_32_x_s1t256_s2t256_s1t512_s2t512":
+                                [[round(x, 4) for x in r] for r in tune["tune_ms_fwd_variants"]],
+                            "autotune_ms_per_launch_adj_tx8_16_32_x_s1t256_s2t256_s1t512_s2t512":
+                                [[round(x, 4) for x in r] for r in tune["tune_ms_adj_variants"]]},
                    "shots_per_s": round(shots_all / t_dev, 3),
                    "wall_s": round(wall, 3),
                    "fwd_ms_per_step": round(fwd_ms / args.steps, 2),

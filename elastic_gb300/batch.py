@@ -43,14 +43,15 @@ class BatchRTM:
                                        int(image_on_device)))
 
     def stats(self):
-        out = np.zeros(28, np.float64)
+        out = np.zeros(48, np.float64)
         check(load().rtm_batch_stats(self.h, ptr(out)))
         return dict(fwd_ms=out[0], adj_ms=out[1], cells=int(out[2]), kernels=int(out[3]), total_ms=out[4],
                     tile_x=int(out[5]), work_items=int(out[6]), tile_x_adj=int(out[7]),
                     tune_ms_fwd=list(out[8:11]), tune_ms_adj=list(out[11:14]),
-                    stages=int(out[14]), stages_adj=int(out[15]),
-                    tune_ms_fwd_stages=[list(out[16 + 2 * i:18 + 2 * i]) for i in range(3)],
-                    tune_ms_adj_stages=[list(out[22 + 2 * i:24 + 2 * i]) for i in range(3)])
+                    stages=int(out[14]), stages_adj=int(out[15]), threads=int(out[40]), threads_adj=int(out[41]),
+                    # per tile width 8, 16, 32: [1 stage, 2 stages, 1 stage 512 threads, 2 stages 512 threads]
+                    tune_ms_fwd_variants=[list(out[16 + 4 * i:20 + 4 * i]) for i in range(3)],
+                    tune_ms_adj_variants=[list(out[28 + 4 * i:32 + 4 * i]) for i in range(3)])
 
     def autotune(self, shot0=0, nshot=None, steps=20):
         """Pick the fastest tile width per pass on the geometry of a group."""
@@ -65,9 +66,10 @@ class BatchRTM:
     def set_tile(self, tile_x):
         check(load().rtm_batch_set(self.h, 1 if getattr(self, "_graph", True) else 0, tile_x))
 
-    def set_stages(self, fwd, adj):
-        """Staging buffers per CTA (1 or 2) of the forward and adjoint step."""
-        check(load().rtm_batch_set_stages(self.h, fwd, adj))
+    def set_stages(self, fwd, adj, threads_fwd=256, threads_adj=256):
+        """Staging buffers per CTA (1 or 2) and threads per CTA (256, or 512
+        at tile widths >= 16) of the forward and adjoint step."""
+        check(load().rtm_batch_set_stages(self.h, fwd, adj, threads_fwd, threads_adj))
 
     def close(self):
         if getattr(self, "h", None):

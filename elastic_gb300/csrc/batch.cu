@@ -114,7 +114,9 @@ struct rtm_batch {
     ShotTable tab_a;  // adjoint pass work items
     int tx_f = 0, tx_a = 0;          // tile widths chosen by the autotuner (0 = heuristic)
     int st_f = 1, st_a = 1;          // staging buffers per CTA chosen by the autotuner
-    double tune_ms[2][3][2] = {};    // measured ms per step, [pass][tx 8,16,32][stages 1,2]
+    int th_f = 256, th_a = 256;      // threads per CTA chosen by the autotuner
+    // measured ms per step, [pass][tx 8,16,32][variant: stages 1/2 x threads 256/512]
+    double tune_ms[2][3][4] = {};
     std::vector<float> dtsrc;
     cudaStream_t st = nullptr;
     double last_fwd_ms = 0, last_adj_ms = 0, last_total_ms = 0;
@@ -170,7 +172,8 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     RTM_CHECK_ARG(col <= b->cap_cols, "group wider than the batch capacity");
     b->tab.ldz = ld;
     const int tz = kernel_version() == 1 ? TZ_TILE : TZ_TILE2;  // batch planes are always v2-aligned
-    int stf = 1, sta = 1;  // staging buffers per CTA of the two passes
+    int stf = 1, sta = 1;      // staging buffers per CTA of the two passes
+    int thf = 256, tha = 256;  // threads per CTA of the two passes
     {
         const int heur = pick_tile_width((long long)nz, col, tz);
         int heur_a = heur;
@@ -182,8 +185,8 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         b->tab_a.shots = b->tab.shots;
         b->tab_a.ldz = ld;
         TRY(b->tab_a.build(txa, tz));
-        if (tz == TZ_TILE2 && v2_fits(false, false, txf, b->st_f)) stf = b->st_f;
-        if (tz == TZ_TILE2 && v2_fits(true, false, txa, b->st_a)) sta = b->st_a;
+        if (tz == TZ_TILE2 && v2_fits(false, false, txf, b->st_f, b->th_f)) { stf = b->st_f; thf = b->th_f; }
+        if (tz == TZ_TILE2 && v2_fits(true, false, txa, b->st_a, b->th_a)) { sta = b->st_a; tha = b->th_a; }
     }
     RTM_CUDA(cudaMemcpyAsync(b->dx0.p, x0g.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
     const long long gp = b->gplane;
@@ -262,9 +265,9 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     {
         Step2DArgs<float> a = base_args(false);
         a.ntiles = 0;
-        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf));
+        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
         a.img[0] = b->img.p;
-        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta));
+        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
     }
 
     if (tune_steps > 0) {
@@ -276,11 +279,12 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         const int cand[3] = {8, 16, 32};
         for (int pass = 0; pass < 2; pass++) {
             double best = 1e30;
-            int bx = cand[0], bs = 1;
+            int bx = cand[0], bs = 1, bt = 256;
             for (int ci = 0; ci < 3; ci++)
-                for (int ns_ = 1; ns_ <= 2; ns_++) {
-                    if (tz != TZ_TILE2 ? ns_ > 1 : !v2_fits(pass == 1, false, cand[ci], ns_)) {
-                        b->tune_ms[pass][ci][ns_ - 1] = -1;  // does not fit in shared memory
+                for (int var = 0; var < 4; var++) {
+                    const int ns_ = 1 + (var & 1), nth = var >= 2 ? 512 : 256;
+                    if (tz != TZ_TILE2 ? var > 0 : !v2_fits(pass == 1, false, cand[ci], ns_, nth)) {
+                        b->tune_ms[pass][ci][var] = -1;  // not available or does not fit in a block
                         continue;
                     }
                     ShotTable &tb = pass ? b->tab_a : b->tab;
@@ -307,17 +311,17 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                                 a.isnap1[0] = snap(2, 0); a.isnap1[1] = snap(2, 1); a.imax1 = mx(2);
                                 set_img(a);
                             }
-                            TRY(launch_step<float>(a, pass == 1, false, tb.tx, 0, st, tb.tz, ns_));
+                            TRY(launch_step<float>(a, pass == 1, false, tb.tx, 0, st, tb.tz, ns_, nth));
                         }
                         RTM_CUDA(cudaEventRecord(t1, st));
                         RTM_CUDA(cudaEventSynchronize(t1));
                     }
                     float ms = 0;
                     RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-                    b->tune_ms[pass][ci][ns_ - 1] = ms / tune_steps;
-                    if (ms < best) { best = ms; bx = cand[ci]; bs = ns_; }
+                    b->tune_ms[pass][ci][var] = ms / tune_steps;
+                    if (ms < best) { best = ms; bx = cand[ci]; bs = ns_; bt = nth; }
                 }
-            if (pass) b->st_a = bs; else b->st_f = bs;
+            if (pass) { b->st_a = bs; b->th_a = bt; } else { b->st_f = bs; b->th_f = bt; }
             if (pass) b->tx_a = bx; else b->tx_f = bx;
         }
         cudaEventDestroy(t0);
@@ -347,7 +351,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.snap_out[1] = snap(L - 1, 1);
             a.snap_max_in = mx(L - 1);
             a.snap_max_out = mx(L);
-            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf));
+            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
             nkern++;
         }
         dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
@@ -378,7 +382,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
             a.imax1 = L < nt ? mx(L + 1) : mx(L);
             set_img(a);
-            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta));
+            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
             nkern++;
             if (blocked && ((nt - L + 1) % IMG_FOLD == 0 || L == 1)) {
                 TRY(fold());
@@ -598,13 +602,18 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[7] = (double)(b->tx_a > 0 ? b->tx_a : b->tab_a.tx);
     for (int p = 0; p < 2; p++)
         for (int i = 0; i < 3; i++) {
-            const double m1 = b->tune_ms[p][i][0], m2 = b->tune_ms[p][i][1];
-            out[8 + 3 * p + i] = m1 < 0 ? m2 : (m2 < 0 ? m1 : std::min(m1, m2));
-            out[16 + 6 * p + 2 * i] = m1;
-            out[17 + 6 * p + 2 * i] = m2;
+            double best = -1;
+            for (int v = 0; v < 4; v++) {
+                const double m = b->tune_ms[p][i][v];
+                out[16 + 12 * p + 4 * i + v] = m;
+                if (m >= 0 && (best < 0 || m < best)) best = m;
+            }
+            out[8 + 3 * p + i] = best;
         }
     out[14] = b->st_f;
     out[15] = b->st_a;
+    out[40] = b->th_f;
+    out[41] = b->th_a;
     return RTM_OK;
 }
 
@@ -617,12 +626,16 @@ extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
     return RTM_OK;
 }
 
-extern "C" int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj)
+extern "C" int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj, int threads_fwd, int threads_adj)
 {
     RTM_CHECK_ARG(b, "null argument");
     RTM_CHECK_ARG(fwd >= 1 && fwd <= 2 && adj >= 1 && adj <= 2, "stages must be 1 or 2");
+    RTM_CHECK_ARG((threads_fwd == 256 || threads_fwd == 512) && (threads_adj == 256 || threads_adj == 512),
+                  "threads must be 256 or 512");
     b->st_f = fwd;
     b->st_a = adj;
+    b->th_f = threads_fwd;
+    b->th_a = threads_adj;
     return RTM_OK;
 }
 
@@ -632,6 +645,7 @@ extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
     TRY(ensure_device());
     b->tx_f = b->tx_a = 0;
     b->st_f = b->st_a = 1;
+    b->th_f = b->th_a = 256;
     // traces are not read during tuning beyond the receiver row; use the
     // staging buffer content as is
     TRY(batch_group(b, shot0, nshot, b->tstage.p, 1, b->full.p, 1, steps));

@@ -105,69 +105,72 @@ int max_smem_optin()
     return v;
 }
 
-bool v2_fits(bool adj, bool exact, int tx)
+template <int TX>
+static size_t v2_bytes_tx(bool adj, bool exact)
 {
-    size_t need = 0;
-    switch (tx) {
-    case 8: need = adj ? (exact ? v2_smem<true, true, 8>(true) : v2_smem<true, false, 8>(true)) : v2_smem<false, false, 8>(false); break;
-    case 16: need = adj ? (exact ? v2_smem<true, true, 16>(true) : v2_smem<true, false, 16>(true)) : v2_smem<false, false, 16>(false); break;
-    case 32: need = adj ? (exact ? v2_smem<true, true, 32>(true) : v2_smem<true, false, 32>(true)) : v2_smem<false, false, 32>(false); break;
-    default: return false;
-    }
-    return need <= (size_t)max_smem_optin();
-}
-
-bool v2_fits(bool adj, bool exact, int tx, int stages)
-{
-    return stages >= 1 && stages <= 2 && v2_fits(adj, exact, tx) &&
-           (size_t)stages * v2_stage_bytes(adj, exact, tx) <= (size_t)max_smem_optin();
+    if (adj) return exact ? v2_smem<true, true, TX>(true) : v2_smem<true, false, TX>(true);
+    return exact ? v2_smem<false, true, TX>(false) : v2_smem<false, false, TX>(false);
 }
 
 size_t v2_stage_bytes(bool adj, bool exact, int tx)
 {
     switch (tx) {
-    case 8: return adj ? (exact ? v2_smem<true, true, 8>(true) : v2_smem<true, false, 8>(true)) : v2_smem<false, false, 8>(false);
-    case 16: return adj ? (exact ? v2_smem<true, true, 16>(true) : v2_smem<true, false, 16>(true)) : v2_smem<false, false, 16>(false);
-    case 32: return adj ? (exact ? v2_smem<true, true, 32>(true) : v2_smem<true, false, 32>(true)) : v2_smem<false, false, 32>(false);
+    case 8: return v2_bytes_tx<8>(adj, exact);
+    case 16: return v2_bytes_tx<16>(adj, exact);
+    case 32: return v2_bytes_tx<32>(adj, exact);
     default: return 0;
     }
 }
 
+bool v2_fits(bool adj, bool exact, int tx) { return v2_fits(adj, exact, tx, 1); }
+
+bool v2_threads_ok(bool exact, int tx, int threads)
+{
+    return threads == 256 || (threads == 512 && !exact && tx >= 16);
+}
+
+bool v2_fits(bool adj, bool exact, int tx, int stages, int threads)
+{
+    if (stages < 1 || stages > 2 || !v2_threads_ok(exact, tx, threads)) return false;
+    const size_t b = v2_stage_bytes(adj, exact, tx);
+    return b > 0 && (size_t)stages * b <= (size_t)max_smem_optin();
+}
+
 template <bool EXACT, bool ADJ, int TX>
-static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t st, int stages)
+static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t st, int stages, int threads)
 {
     auto kern = k_step2d_v2<EXACT, ADJ, TX>;
     const bool img = ADJ && a.img[0] != nullptr;
-    RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX, stages), "tile width %d with %d stages needs more shared memory than a block can use",
-                  TX, stages);
+    RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX, stages, threads),
+                  "tile width %d with %d stages and %d threads does not fit in a block", TX, stages, threads);
     const size_t smem = (size_t)stages * v2_smem<ADJ, EXACT, TX>(img);
     static bool attr_set = false;
-    static int grid_max[2][2] = {{0, 0}, {0, 0}};
+    static int grid_max[2][2][2] = {};
     if (!attr_set) {
         RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin()));
         attr_set = true;
     }
-    int &gm = grid_max[img][stages - 1];
+    int &gm = grid_max[img][stages - 1][threads == 512];
     if (!gm) {
         int nb = 0;
-        RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
+        RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem));
         gm = (nb > 0 ? nb : 1) * device_sm_count();
     }
     int grid = a.ntiles < gm ? a.ntiles : gm;
     if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
     if (grid <= 0) return RTM_OK;
-    kern<<<grid, 256, smem, st>>>(a);
+    kern<<<grid, threads, smem, st>>>(a);
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }
 
 template <bool EXACT, bool ADJ>
-static int launch_v2(const Step2DArgs<float> &a, int tx, int grid_cap, cudaStream_t st, int stages)
+static int launch_v2(const Step2DArgs<float> &a, int tx, int grid_cap, cudaStream_t st, int stages, int threads)
 {
     switch (tx) {
-    case 8: return launch_v2_tx<EXACT, ADJ, 8>(a, grid_cap, st, stages);
-    case 16: return launch_v2_tx<EXACT, ADJ, 16>(a, grid_cap, st, stages);
-    case 32: return launch_v2_tx<EXACT, ADJ, 32>(a, grid_cap, st, stages);
+    case 8: return launch_v2_tx<EXACT, ADJ, 8>(a, grid_cap, st, stages, threads);
+    case 16: return launch_v2_tx<EXACT, ADJ, 16>(a, grid_cap, st, stages, threads);
+    case 32: return launch_v2_tx<EXACT, ADJ, 32>(a, grid_cap, st, stages, threads);
     default: rtm_set_error("unsupported tile width %d", tx); return RTM_ERR_ARG;
     }
 }
@@ -193,7 +196,8 @@ bool v2_usable(bool is_float, int ldz, const void *const *ptrs, int n)
 }
 
 template <typename T>
-int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz, int stages)
+int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz, int stages,
+                int threads)
 {
     if constexpr (std::is_same<T, float>::value) {
         if (tz == TZ_TILE2) {
@@ -201,15 +205,18 @@ int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_c
                 rtm_set_error("v2 step launched on an unaligned layout");
                 return RTM_ERR_ARG;
             }
-            if (adj) return exact ? launch_v2<true, true>(a, tx, grid_cap, st, stages) : launch_v2<false, true>(a, tx, grid_cap, st, stages);
-            return exact ? launch_v2<true, false>(a, tx, grid_cap, st, stages) : launch_v2<false, false>(a, tx, grid_cap, st, stages);
+            if (adj)
+                return exact ? launch_v2<true, true>(a, tx, grid_cap, st, stages, threads)
+                             : launch_v2<false, true>(a, tx, grid_cap, st, stages, threads);
+            return exact ? launch_v2<true, false>(a, tx, grid_cap, st, stages, threads)
+                         : launch_v2<false, false>(a, tx, grid_cap, st, stages, threads);
         }
     }
     if (adj) return exact ? launch_step_e<T, true, true>(a, tx, grid_cap, st) : launch_step_e<T, false, true>(a, tx, grid_cap, st);
     return exact ? launch_step_e<T, true, false>(a, tx, grid_cap, st) : launch_step_e<T, false, false>(a, tx, grid_cap, st);
 }
-template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t, int, int);
-template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t, int, int);
+template int launch_step<float>(const Step2DArgs<float> &, bool, bool, int, int, cudaStream_t, int, int, int);
+template int launch_step<double>(const Step2DArgs<double> &, bool, bool, int, int, cudaStream_t, int, int, int);
 
 // ------------------------------------------------------------- batch table
 int ShotTable::build(int tx_, int tz_)

@@ -47,6 +47,28 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem, bool val
     const int n = valid ? 8 : 0;
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
 }
+// L2 eviction-priority policy for the coefficient planes, which every time
+// level reads again: evict_last.
+__device__ __forceinline__ unsigned long long l2_evict_last()
+{
+    unsigned long long p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void cp_async16_pol(void *smem, const void *gmem, bool valid, unsigned long long pol)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int n = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2, %3;\n" ::"r"(s), "l"(gmem), "r"(n), "l"(pol));
+}
+__device__ __forceinline__ float4 ldg4_pol(const float *p, unsigned long long pol)
+{
+    float4 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;\n"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
 __device__ __forceinline__ void cp_async_wait_all()
 {
     asm volatile("cp.async.commit_group;\n" ::);
@@ -167,13 +189,17 @@ __device__ __forceinline__ void adj_fast_z4(const float w[20], float v[4])
     }
 }
 
+// Threads per CTA: 256, or 512 for the fast kernels with TX >= 16 (one
+// column per warp at TX = 16).
+__host__ __device__ constexpr int v2_max_threads(bool exact) { return exact ? 256 : 512; }
+
 template <bool ADJ, bool EXACT>
 struct V2Arr {
     static constexpr int NRAW = ADJ ? 10 : 5;  // staged float arrays
 };
 
-// Shared memory of a v2 launch: NRAW float arrays (+ 2 FP16 snapshot arrays
-// for fused imaging, stored as halves).
+// Shared memory of one stage of a v2 launch: NRAW float arrays (+ 2 FP16
+// snapshot arrays for fused imaging, stored as halves).
 template <bool ADJ, bool EXACT, int TX>
 __host__ __device__ constexpr size_t v2_smem(bool img)
 {
@@ -196,7 +222,7 @@ __device__ __forceinline__ float4 ldh4(const __half *smh, int arr, int x, int z)
 
 // Issue the cp.async staging of work item t into the stage at `sm`.
 template <bool ADJ, int TX>
-__device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, float *sm, bool img)
+__device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, float *sm, bool img, unsigned long long keep)
 {
     constexpr int NRAW = V2Arr<ADJ, false>::NRAW;
     constexpr int SZ = V2<TX>::SIZE;
@@ -216,7 +242,7 @@ __device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, floa
         for (int f = 0; f < 5; f++) cp_async16(sm + f * SZ + so, a.nb[f] + o, ok);
         if (ADJ) {
 #pragma unroll
-            for (int f = 0; f < 5; f++) cp_async16(sm + (5 + f) * SZ + so, a.coef[f] + o, ok);
+            for (int f = 0; f < 5; f++) cp_async16_pol(sm + (5 + f) * SZ + so, a.coef[f] + o, ok, keep);
             if (img) {
                 const bool oks = ok & (gz < nz);
                 cp_async8(smh + so, a.isnap0[0] + o, oks);
@@ -228,44 +254,65 @@ __device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, floa
 }
 
 template <bool EXACT, bool ADJ, int TX>
-__global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2DArgs<float> a)
+__global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __grid_constant__ Step2DArgs<float> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int NRAW = V2Arr<ADJ, EXACT>::NRAW;
     constexpr int SZ = V2<TX>::SIZE;
-    constexpr int CW = TX / 8;  // columns per warp
+    const int cw = TX * 32 / (int)blockDim.x;  // columns per warp (blockDim.x = 32 * TX / cw)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool img = ADJ && a.img[0] != nullptr;
     // one or two stages, depending on the shared memory this launch received
     unsigned dyn;
     asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
     const size_t stage_bytes = v2_smem<ADJ, EXACT, TX>(img);
+    const unsigned long long keep = l2_evict_last();
     const bool dbuf = dyn >= 2 * stage_bytes;
     auto stage = [&](int k) { return reinterpret_cast<float *>(smem_raw + (k ? stage_bytes : 0)); };
 
     int cur = 0;
-    if (blockIdx.x < a.ntiles) v2_stage<ADJ, TX>(a, blockIdx.x, stage(0), img);
+    if (blockIdx.x < a.ntiles) v2_stage<ADJ, TX>(a, blockIdx.x, stage(0), img, keep);
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
         float *sm = stage(cur);
         __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
-        if (dbuf) {
-            if (tn < a.ntiles) {
-                v2_stage<ADJ, TX>(a, tn, stage(cur ^ 1), img);
-                asm volatile("cp.async.wait_group 1;\n" ::);
-            } else {
-                asm volatile("cp.async.wait_group 0;\n" ::);
-            }
-        } else {
-            asm volatile("cp.async.wait_group 0;\n" ::);
-        }
-        __syncthreads();
+        if (dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(cur ^ 1), img, keep);
         const int s = find_shot<float>(a.shots, a.nshots, t);
         const ShotGeom g = a.shots[s];
         const int lt = t - g.tile0;
         const int tz0 = (lt % g.ntz) * V2_TZ, tx0 = (lt / g.ntz) * TX;
         const long long off = g.off;
         const int nz = g.nz, nx = g.nx, ldz = a.ldz;
+        const int z = 4 * lane;  // local row of this thread's 4 cells
+        const int gz = tz0 + z;
+        // Global operands of one column (own fields; forward: coefficients;
+        // imaging: next level's snapshots).  The first column's are issued
+        // before the wait for the staged tile, so their latency overlaps it.
+        float4 gown[5], gcoef[5];
+        uint2 gsn[2];
+        auto fetch = [&](int r) {
+            const int gx = tx0 + warp * cw + r;
+            if (gx >= nx || gz >= nz) return false;
+            const long long o = off + (long long)gx * ldz + gz;
+#pragma unroll
+            for (int f = 0; f < 5; f++) gown[f] = ld_f4(a.own2[f] + o);
+            if (!ADJ) {
+#pragma unroll
+                for (int k = 0; k < 5; k++) gcoef[k] = ldg4_pol(a.coef[k] + o, keep);
+            }
+            if (ADJ && img && !a.ilast) {
+                gsn[0] = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
+                gsn[1] = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
+            }
+            return true;
+        };
+        bool have = fetch(0);
+        if (dbuf && tn < a.ntiles) {
+            asm volatile("cp.async.wait_group 1;\n" ::);
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::);
+        }
+        __syncthreads();
         if (ADJ && !EXACT) {
             // products coef*field in place (slots 0..6 of the 10 raw arrays)
             for (int e = threadIdx.x; e < SZ; e += blockDim.x) {
@@ -284,18 +331,17 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
         }
 
         float wmax0 = 0.f, wmax1 = 0.f;
-        const int z = 4 * lane;  // local row of this thread's 4 cells
-        const int gz = tz0 + z;
 #pragma unroll 1
-        for (int r = 0; r < CW; r++) {
-            const int x = warp * CW + r, gx = tx0 + x;
-            if (gx >= nx || gz >= nz) continue;
+        for (int r = 0; r < cw; r++) {
+            const int x = warp * cw + r, gx = tx0 + x;
+            if (r > 0) have = fetch(r);
+            if (!have) continue;
             const long long o = off + (long long)gx * ldz + gz;
             const int nval = min(4, nz - gz);  // rows of this group inside the shot
             float v[5][4];
 #pragma unroll
             for (int f = 0; f < 5; f++) {
-                const float4 b = ld_f4(a.own2[f] + o);
+                const float4 b = gown[f];
                 v[f][0] = b.x; v[f][1] = b.y; v[f][2] = b.z; v[f][3] = b.w;
                 if (a.inplane[f]) {
                     const float4 q = ld_f4(a.inplane[f] + o);
@@ -313,11 +359,7 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
                             v[SZZ][jj] = Ar<EXACT>::add(v[SZZ][jj], a.srcval);
                         }
                 }
-                const float4 cm1x = __ldg(reinterpret_cast<const float4 *>(a.coef[M1X] + o));
-                const float4 cm1z = __ldg(reinterpret_cast<const float4 *>(a.coef[M1Z] + o));
-                const float4 ca2 = __ldg(reinterpret_cast<const float4 *>(a.coef[A2] + o));
-                const float4 ca3 = __ldg(reinterpret_cast<const float4 *>(a.coef[A3] + o));
-                const float4 ca23 = __ldg(reinterpret_cast<const float4 *>(a.coef[A23] + o));
+                const float4 cm1x = gcoef[M1X], cm1z = gcoef[M1Z], ca2 = gcoef[A2], ca3 = gcoef[A3], ca23 = gcoef[A23];
                 float p[4], w[20];
                 // Vx: Ax (x, M, sxx) then Bx (z, P, sxz)
                 fwd_poly_x4<EXACT, TX, false>(sm, SXX, x, z, p);
@@ -489,8 +531,7 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
                 float s1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f};
                 if (!a.ilast) {
                     const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
-                    const uint2 u0 = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
-                    const uint2 u1 = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
+                    const uint2 u0 = gsn[0], u1 = gsn[1];
                     const float2 a0 = __half22float2(*reinterpret_cast<const __half2 *>(&u0.x));
                     const float2 a1 = __half22float2(*reinterpret_cast<const __half2 *>(&u0.y));
                     const float2 b0 = __half22float2(*reinterpret_cast<const __half2 *>(&u1.x));
@@ -574,7 +615,7 @@ __global__ void __launch_bounds__(256) k_step2d_v2(const __grid_constant__ Step2
         }
         __syncthreads();  // the stage is free for the prefetch of the next iteration
         cur ^= dbuf ? 1 : 0;
-        if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img);
+        if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img, keep);
     }
 }
 

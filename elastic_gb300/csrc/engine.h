@@ -90,14 +90,15 @@ inline int pick_tile_width(long long cells_z, long long cells_x, int tz = TZ_TIL
 
 template <typename T>
 int launch_step(const Step2DArgs<T> &a, bool adj, bool exact, int tx, int grid_cap, cudaStream_t st, int tz = TZ_TILE,
-                int stages = 1);
+                int stages = 1, int threads = 256);
 
 // True when a float step on planes with pitch ldz starting at `ptrs` can use v2.
 bool v2_usable(bool is_float, int ldz, const void *const *ptrs, int n);
 // True when the v2 kernel of this flavour and tile width fits in shared memory.
 bool v2_fits(bool adj, bool exact, int tx);
-// v2 tile of width tx with `stages` staging buffers (1 or 2) fits in a block
-bool v2_fits(bool adj, bool exact, int tx, int stages);
+// v2 tile of width tx with `stages` staging buffers (1 or 2) and `threads`
+// threads (256, or 512 for the fast kernels with tx >= 16) fits in a block
+bool v2_fits(bool adj, bool exact, int tx, int stages, int threads = 256);
 size_t v2_stage_bytes(bool adj, bool exact, int tx);
 int max_smem_optin();
 

@@ -209,13 +209,15 @@ rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp
  * host pointers. */
 int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device, float *image,
                       int image_on_device);
-/* out[0..27]: forward ms, adjoint ms, cells of the last group, kernels
- * launched, total ms of the last call, forward tile width, forward work
- * items, adjoint tile width; [8..13] the autotuner's best ms per step for
- * tile widths 8, 16, 32 (forward, then adjoint); [14..15] staging buffers
- * per CTA (1 or 2) of the forward and adjoint pass; [16..27] the
- * autotuner's ms per step for every (tile width, stages) pair, forward then
- * adjoint, -1 where it does not fit in shared memory. */
+/* out[0..41] (pass an array of at least 42 doubles): forward ms, adjoint
+ * ms, cells of the last group, kernels launched, total ms of the last call,
+ * forward tile width, forward work items, adjoint tile width; [8..13] the
+ * autotuner's best ms per step for tile widths 8, 16, 32 (forward, then
+ * adjoint); [14..15] staging buffers per CTA (1 or 2) of the forward and
+ * adjoint pass; [16..39] the autotuner's ms per step for every tile width
+ * (8, 16, 32) and launch shape (1 stage, 2 stages, each with 256 then 512
+ * threads), forward then adjoint, -1 where a shape does not fit in a block;
+ * [40..41] threads per CTA of the forward and adjoint pass. */
 int rtm_batch_stats(const rtm_batch *b, double *out);
 /* Autotuner: times `steps` launches of each pass for every tile width and
  * staging depth on the geometry of shots [shot0, shot0+nshot) and keeps the
@@ -224,10 +226,12 @@ int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps);
 /* use_graph=0 launches the time loop kernel by kernel; tile_x selects the
  * tile width of the step kernel (8, 16 or 32; 0 = automatic). */
 int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x);
-/* Staging buffers per CTA of the forward and adjoint step kernels: 1, or 2
- * to stage the next tile while computing the current one.  A depth that does
- * not fit in shared memory with the tile width in use falls back to 1. */
-int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj);
+/* Launch shape of the forward and adjoint step kernels: staging buffers per
+ * CTA (1, or 2 to stage the next tile while computing the current one) and
+ * threads per CTA (256, or 512 at tile widths >= 16).  A shape that does not
+ * fit in a block with the tile width in use falls back to 1 stage and 256
+ * threads. */
+int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj, int threads_fwd, int threads_adj);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */
 void *rtm_host_alloc(size_t bytes);

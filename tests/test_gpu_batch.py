@@ -22,10 +22,10 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def survey(nshots=5, nz=48, nx=200, nt=160, seed=1):
+def survey(nshots=5, nz=48, nx=200, nt=160, seed=1, spacing=24, wmin=50, wmax=96):
     vp = synth.smooth_random_model(nz, nx, 10.0, 150.0, 1800.0, 3500.0, seed=seed)
     rho, lam, mu = synth.lame_from_vp(vp)
-    x0, nxs, xsrc = synth.uneven_survey(nx, nshots, 24, 50, 96, seed=seed)
+    x0, nxs, xsrc = synth.uneven_survey(nx, nshots, spacing, wmin, wmax, seed=seed)
     rng = np.random.default_rng(seed)
     traces = [[(rng.standard_normal((w, nt))).astype(np.float32) for _ in range(2)] for w in nxs]
     return rho, lam, mu, x0, nxs, xsrc, traces
@@ -98,7 +98,7 @@ def test_batch_tile_widths_and_autotuner_are_bit_identical():
     nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 40, 180, 60, 10.0, 1e-3, 30.0, 10, 6, 6, 40
     rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=5)
     ref, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3, tile_x=8)
-    for tx, stages in ((16, None), (8, (2, 2)), (16, (2, 2))):
+    for tx, stages in ((16, None), (8, (2, 2)), (16, (2, 2)), (16, (1, 2, 512, 512)), (32, (2, 1, 512, 512))):
         # two staging buffers (next tile staged during the current one) do
         # not change the arithmetic either; where they do not fit the
         # launcher keeps one
@@ -113,4 +113,25 @@ def test_batch_tile_widths_and_autotuner_are_bit_identical():
     assert all(t > 0 or t == -1 for t in st["tune_ms_fwd"] + st["tune_ms_adj"])
     assert max(st["tune_ms_fwd"]) > 0 and max(st["tune_ms_adj"]) > 0
     assert st["stages"] in (1, 2) and st["stages_adj"] in (1, 2)
-    assert all(t > 0 or t == -1 for row in st["tune_ms_fwd_stages"] + st["tune_ms_adj_stages"] for t in row)
+    assert all(t > 0 or t == -1 for row in st["tune_ms_fwd_variants"] + st["tune_ms_adj_variants"] for t in row)
+    assert st["threads"] in (256, 512) and st["threads_adj"] in (256, 512)
+
+
+def test_batch_staging_depth_with_several_tiles_per_cta_is_bit_identical():
+    """A grid large enough that every CTA loops over several work items, so
+    the two-stage path prefetches the next tile while computing the current
+    one; one and two staging buffers give the same image, bit for bit."""
+    nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 700, 1200, 24, 10.0, 1e-3, 30.0, 20, 8, 8, 20
+    rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=7, spacing=300, wmin=300,
+                                                 wmax=400)
+    for tx in (8, 16):
+        ref, st = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
+                            tile_x=tx, stages=(1, 1))
+        assert st["work_items"] > 2 * 152  # more work items than resident CTAs
+        assert np.isfinite(ref).all() and np.abs(ref).max() > 0
+        for stages in ((2, 2), (1, 1, 512, 512), (2, 2, 512, 512)):
+            if tx == 8 and len(stages) > 2:
+                continue  # 512 threads need tile width >= 16
+            img, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
+                               tile_x=tx, stages=stages)
+            np.testing.assert_array_equal(img, ref)
