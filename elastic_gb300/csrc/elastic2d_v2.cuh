@@ -304,6 +304,12 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
                 gsn[0] = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
                 gsn[1] = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
             }
+            if (ADJ && img && (lane & 7) == 0) {
+                // the image planes are read-modified-written after the
+                // column's compute: bring their lines (one per 8 lanes) to L2
+#pragma unroll
+                for (int i = 0; i < 3; i++) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[i] + o));
+            }
             return true;
         };
         bool have = fetch(0);
