@@ -5,6 +5,9 @@
 #include <cstring>
 #include <cstdint>
 #include <type_traits>
+#include <algorithm>
+#include <cmath>
+#include <memory>
 #include <vector>
 
 #include "../../include/elastic_rtm.h"
@@ -522,107 +525,318 @@ int copy_d2h(T *h, const T *d, size_t n, cudaStream_t st) {
     return RTM_OK;
 }
 
-// Whole rtm_op2 for one shot (W/rtm-mod-adj.f90:132-496).
+// One shot of rtm_op2 (W/rtm-mod-adj.f90:132-496, lame=.true.) on the full
+// grid, with the shot's source wavefield history resident on the device:
+// born() is the Born operator (image_op2 forward, W/image-mod-rtm.f90:164-179,
+// then the scattered loop and receiver sampling, :291-375) and adjoint() the
+// RTM (rtm_op3 then image_op2 adjoint, W/image-mod-rtm.f90:146-162).  With
+// exact_adj the adjoint is the exact transpose of born() (sponge applied in
+// transposed order), which LSRTM needs.
+template <typename T>
+struct BornShot {
+    Hist<T> h;
+    DevBuf<T> S;  // source wavefield, 5 histories of nt levels
+    int nz = 0, nx = 0, nt = 0, zrec0 = 0;
+    size_t plane = 0, vol = 0;
+    T inv_dt = 0, inv_dx = 0;
+
+    // model: device planes rho, lambda, mu (raw, averaged here as model_op)
+    int init(int nz_, int nx_, int nt_, T dx, T dt, int xsrc, int zsrc, int zrec, T fp, int nsource, int abc,
+             const T *model, bool exact)
+    {
+        RTM_CHECK_ARG(nz_ >= 11 && nx_ >= 11 && nt_ >= 3, "grid too small (nz=%d nx=%d nt=%d)", nz_, nx_, nt_);
+        RTM_CHECK_ARG(zsrc >= 1 && zsrc <= nz_ && xsrc >= 1 && xsrc <= nx_ && zrec >= 1 && zrec <= nz_,
+                      "source/receiver position outside the grid");
+        nz = nz_; nx = nx_; nt = nt_; zrec0 = zrec - 1;
+        TRY(h.init(nz, nx, nt, exact));
+        TRY(h.set_abc(abc));
+        plane = h.plane;
+        vol = plane * nt;
+        DevBuf<T> raw;
+        TRY(raw.alloc(5 * plane));
+        T *r[5];
+        for (int i = 0; i < 5; i++) r[i] = raw.p + i * plane;
+        TRY(model_coefs<T>(nz, nx, dx, dt, model, model + plane, model + 2 * plane, nz, r[M1X], r[M1Z], nullptr,
+                           nullptr, r[A2], r[A3], r[A23], nz, h.st));
+        TRY(h.set_coefs_dev(r));
+        // source wavelet scaled by dt (host, as the reference)
+        std::vector<T> src(nt), dtsrc(nt);
+        host_ricker<T>(nt, dt, fp, nsource, src.data());
+        for (int i = 0; i < nt; i++) dtsrc[i] = dt * src[i];
+        TRY(S.alloc(5 * vol));
+        T *Sp[5];
+        for (int f = 0; f < 5; f++) Sp[f] = S.p + f * vol;
+        TRY(h.forward(Sp, dtsrc, zsrc - 1, xsrc - 1));
+        inv_dt = T(1) / dt;
+        inv_dx = T(1) / dx;
+        return RTM_OK;
+    }
+    T *sv(int f) const { return S.p + f * vol; }
+    size_t gather_size() const { return (size_t)nt * nx; }
+
+    // data (5 gathers of (nt,nx) in Fortran order, device) = Born(dm1..dm3).
+    // A: 5 work histories, rec: nt*5*nx work.
+    int born(const T *dm1, const T *dm2, const T *dm3, T *const A[5], T *rec, T *data)
+    {
+        for (int L = 1; L <= nt; L++) {
+            const size_t lv = (size_t)(L - 1) * plane, lv1 = L < nt ? lv + plane : lv;
+            dim3 b(128), g(ceil_div(nz, 128), nx, 1);
+            if (h.exact)
+                k_born_src<true, T><<<g, b, 0, h.st>>>(h.tab.d_geom, nz, sv(VX) + lv, sv(VZ) + lv, sv(VX) + lv1,
+                                                       sv(VZ) + lv1, L == nt, dm1, dm2, dm3, A[0] + lv, A[1] + lv,
+                                                       A[2] + lv, A[3] + lv, A[4] + lv, 1, inv_dt, inv_dx);
+            else
+                k_born_src<false, T><<<g, b, 0, h.st>>>(h.tab.d_geom, nz, sv(VX) + lv, sv(VZ) + lv, sv(VX) + lv1,
+                                                        sv(VZ) + lv1, L == nt, dm1, dm2, dm3, A[0] + lv, A[1] + lv,
+                                                        A[2] + lv, A[3] + lv, A[4] + lv, 1, inv_dt, inv_dx);
+            RTM_CUDA(cudaGetLastError());
+        }
+        TRY(h.born_scatter(A, zrec0, rec));
+        dim3 b(128), gr(ceil_div(nt, 128), nx);
+        const size_t gs = gather_size();
+        k_gather_from_rec<T><<<gr, b, 0, h.st>>>(nt, nx, rec, data, data + gs, data + 2 * gs, data + 3 * gs,
+                                                 data + 4 * gs);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    }
+
+    // img (3 planes, overwritten) = RTM(data); A: 5 work histories.
+    int adjoint(const T *data, T *const A[5], T *img, bool exact_adj)
+    {
+        for (int f = 0; f < 5; f++) RTM_CUDA(cudaMemsetAsync(A[f], 0, vol * sizeof(T), h.st));
+        const size_t gs = gather_size();
+        dim3 b(128), gr(ceil_div(nt, 128), nx);
+        k_put_rows<T><<<gr, b, 0, h.st>>>(nt, nx, nz, zrec0, data, data + gs, data + 2 * gs, data + 3 * gs,
+                                          data + 4 * gs, A[0], A[1], A[2], A[3], A[4]);
+        RTM_CUDA(cudaGetLastError());
+        TRY(h.adjoint(A, exact_adj));
+        dim3 gi(ceil_div(nz, 128), nx);
+        k_image_hist<T><<<gi, b, 0, h.st>>>(nz, nx, nt, sv(VX), sv(VZ), A[0], A[1], A[2], A[3], A[4], img,
+                                            img + plane, img + 2 * plane, inv_dt, inv_dx);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    }
+};
+
+// Whole rtm_op2 for one shot (W/rtm-mod-adj.f90:132-496), host arrays in
+// and out.
 template <typename T>
 int rtm_op_impl(int adj, int nz, int nx, int nt, T dx, T dt, int xsrc, int zsrc, int zrec, T fp, int nsource,
                 int abc, const T *rho, const T *lam, const T *mu, T *dm1, T *dm2, T *dm3, T *const D[5], int linear,
                 int exact_adj, bool exact)
 {
     RTM_CHECK_ARG(nz >= 11 && nx >= 11 && nt >= 3, "grid too small (nz=%d nx=%d nt=%d)", nz, nx, nt);
-    RTM_CHECK_ARG(zsrc >= 1 && zsrc <= nz && xsrc >= 1 && xsrc <= nx && zrec >= 1 && zrec <= nz,
-                  "source/receiver position outside the grid");
-    Hist<T> h;
-    TRY(h.init(nz, nx, nt, exact));
-    TRY(h.set_abc(abc));
-    const size_t plane = h.plane, vol = plane * nt;
-    DevBuf<T> model, raw, W;
+    TRY(ensure_device());
+    const size_t plane = (size_t)nz * nx;
+    DevBuf<T> model;
     TRY(model.alloc(3 * plane));
-    TRY(copy_h2d(model.p, rho, plane, h.st));
-    TRY(copy_h2d(model.p + plane, lam, plane, h.st));
-    TRY(copy_h2d(model.p + 2 * plane, mu, plane, h.st));
-    TRY(raw.alloc(5 * plane));
-    T *r[5];
-    for (int i = 0; i < 5; i++) r[i] = raw.p + i * plane;
-    TRY(model_coefs<T>(nz, nx, dx, dt, model.p, model.p + plane, model.p + 2 * plane, nz, r[M1X], r[M1Z], nullptr,
-                       nullptr, r[A2], r[A3], r[A23], nz, h.st));
-    TRY(h.set_coefs_dev(r));
-    // source wavelet scaled by dt (host, as the reference)
-    std::vector<T> src(nt), dtsrc(nt);
-    host_ricker<T>(nt, dt, fp, nsource, src.data());
-    for (int i = 0; i < nt; i++) dtsrc[i] = dt * src[i];
-    // 10 history volumes: source (5) and scattered / adjoint (5)
-    TRY(W.alloc(10 * vol));
-    T *S[5], *A[5];
-    for (int f = 0; f < 5; f++) { S[f] = W.p + f * vol; A[f] = W.p + (5 + f) * vol; }
-    TRY(h.forward(S, dtsrc, zsrc - 1, xsrc - 1));
-    const T inv_dt = T(1) / dt, inv_dx = T(1) / dx;
-    DevBuf<T> img;
+    RTM_CUDA(cudaMemcpy(model.p, rho, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + plane, lam, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + 2 * plane, mu, plane * sizeof(T), cudaMemcpyHostToDevice));
+    BornShot<T> sh;
+    TRY(sh.init(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, model.p, exact));
+    const size_t vol = sh.vol, gs = sh.gather_size();
+    cudaStream_t st = sh.h.st;
+    DevBuf<T> W, img, g;
+    TRY(W.alloc(5 * vol));
+    T *A[5];
+    for (int f = 0; f < 5; f++) A[f] = W.p + f * vol;
     TRY(img.alloc(3 * plane));
+    TRY(g.alloc(5 * gs));
     if (!adj) {
         // images in; Born
-        TRY(copy_h2d(img.p, dm1, plane, h.st));
-        TRY(copy_h2d(img.p + plane, dm2, plane, h.st));
-        TRY(copy_h2d(img.p + 2 * plane, dm3, plane, h.st));
+        TRY(copy_h2d(img.p, dm1, plane, st));
+        TRY(copy_h2d(img.p + plane, dm2, plane, st));
+        TRY(copy_h2d(img.p + 2 * plane, dm3, plane, st));
         T *i2 = img.p + plane, *i3 = img.p + 2 * plane;
         DevBuf<T> avg;
         if (!linear) {
             TRY(avg.alloc(2 * plane));
-            dim3 b(128), g(ceil_div(nz, 128), nx);
-            k_model_delta<T><<<g, b, 0, h.st>>>(nz, nx, i2, i3, nz, avg.p, avg.p + plane, nz);
+            dim3 b(128), gm(ceil_div(nz, 128), nx);
+            k_model_delta<T><<<gm, b, 0, st>>>(nz, nx, i2, i3, nz, avg.p, avg.p + plane, nz);
             RTM_CUDA(cudaGetLastError());
             i2 = avg.p;
             i3 = avg.p + plane;
             // the reference averages dlambda/dmu in place
-            TRY(copy_d2h(dm2, i2, plane, h.st));
-            TRY(copy_d2h(dm3, i3, plane, h.st));
-        }
-        // secondary sources of every level (image_op2 forward)
-        for (int L = 1; L <= nt; L++) {
-            const size_t lv = (size_t)(L - 1) * plane, lv1 = L < nt ? lv + plane : lv;
-            dim3 b(128), g(ceil_div(nz, 128), nx, 1);
-            if (exact)
-                k_born_src<true, T><<<g, b, 0, h.st>>>(h.tab.d_geom, nz, S[VX] + lv, S[VZ] + lv, S[VX] + lv1, S[VZ] + lv1,
-                                                       L == nt, img.p, i2, i3, A[0] + lv, A[1] + lv, A[2] + lv,
-                                                       A[3] + lv, A[4] + lv, 1, inv_dt, inv_dx);
-            else
-                k_born_src<false, T><<<g, b, 0, h.st>>>(h.tab.d_geom, nz, S[VX] + lv, S[VZ] + lv, S[VX] + lv1, S[VZ] + lv1,
-                                                        L == nt, img.p, i2, i3, A[0] + lv, A[1] + lv, A[2] + lv,
-                                                        A[3] + lv, A[4] + lv, 1, inv_dt, inv_dx);
-            RTM_CUDA(cudaGetLastError());
+            TRY(copy_d2h(dm2, i2, plane, st));
+            TRY(copy_d2h(dm3, i3, plane, st));
         }
         DevBuf<T> rec;
         TRY(rec.alloc((size_t)nt * 5 * nx));
-        TRY(h.born_scatter(A, zrec - 1, rec.p));
-        DevBuf<T> g;
-        TRY(g.alloc(5 * (size_t)nt * nx));
-        {
-            dim3 b(128), gr(ceil_div(nt, 128), nx);
-            const size_t gs = (size_t)nt * nx;
-            k_gather_from_rec<T><<<gr, b, 0, h.st>>>(nt, nx, rec.p, g.p, g.p + gs, g.p + 2 * gs, g.p + 3 * gs, g.p + 4 * gs);
-            RTM_CUDA(cudaGetLastError());
-            for (int c = 0; c < 5; c++) TRY(copy_d2h(D[c], g.p + c * gs, gs, h.st));
-        }
+        TRY(sh.born(img.p, i2, i3, A, rec.p, g.p));
+        for (int c = 0; c < 5; c++) TRY(copy_d2h(D[c], g.p + c * gs, gs, st));
     } else {
         // gathers in; RTM
-        for (int f = 0; f < 5; f++) RTM_CUDA(cudaMemsetAsync(A[f], 0, vol * sizeof(T), h.st));
-        DevBuf<T> g;
-        const size_t gs = (size_t)nt * nx;
-        TRY(g.alloc(5 * gs));
-        for (int c = 0; c < 5; c++) TRY(copy_h2d(g.p + c * gs, D[c], gs, h.st));
-        dim3 b(128), gr(ceil_div(nt, 128), nx);
-        k_put_rows<T><<<gr, b, 0, h.st>>>(nt, nx, nz, zrec - 1, g.p, g.p + gs, g.p + 2 * gs, g.p + 3 * gs, g.p + 4 * gs,
-                                          A[0], A[1], A[2], A[3], A[4]);
-        RTM_CUDA(cudaGetLastError());
-        TRY(h.adjoint(A, exact_adj != 0));
-        dim3 gi(ceil_div(nz, 128), nx);
-        k_image_hist<T><<<gi, b, 0, h.st>>>(nz, nx, nt, S[VX], S[VZ], A[0], A[1], A[2], A[3], A[4], img.p,
-                                            img.p + plane, img.p + 2 * plane, inv_dt, inv_dx);
-        RTM_CUDA(cudaGetLastError());
-        TRY(copy_d2h(dm1, img.p, plane, h.st));
-        TRY(copy_d2h(dm2, img.p + plane, plane, h.st));
-        TRY(copy_d2h(dm3, img.p + 2 * plane, plane, h.st));
+        for (int c = 0; c < 5; c++) TRY(copy_h2d(g.p + c * gs, D[c], gs, st));
+        TRY(sh.adjoint(g.p, A, img.p, exact_adj != 0));
+        TRY(copy_d2h(dm1, img.p, plane, st));
+        TRY(copy_d2h(dm2, img.p + plane, plane, st));
+        TRY(copy_d2h(dm3, img.p + 2 * plane, plane, st));
     }
-    RTM_CUDA(cudaStreamSynchronize(h.st));
+    RTM_CUDA(cudaStreamSynchronize(st));
+    return RTM_OK;
+}
+
+// ------------------------------------------------------------------ LSRTM
+// Deterministic dot product in double: per-block partial sums, then one
+// block adds the partials in order.
+template <typename T>
+__global__ void k_dot_partial(size_t n, const T *x, const T *y, double *part)
+{
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        acc += (double)x[i] * (double)y[i];
+    __shared__ double red[32];
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+__global__ void k_sum_partials(int n, const double *part, double *out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < n; i++) s += part[i];
+        *out = s;
+    }
+}
+// y += a * x
+template <typename T>
+__global__ void k_axpy(size_t n, T a, const T *x, T *y)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        y[i] += a * x[i];
+}
+// p = s + b * p
+template <typename T>
+__global__ void k_xpby(size_t n, const T *s, T b, T *p)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = s[i] + b * p[i];
+}
+
+constexpr int DOT_BLOCKS = 1024;
+
+template <typename T>
+struct Vec {
+    cudaStream_t st = 0;
+    DevBuf<double> part;
+    int init(cudaStream_t s)
+    {
+        st = s;
+        return part.alloc(DOT_BLOCKS + 1);
+    }
+    int grid(size_t n) const { return (int)std::min<size_t>(DOT_BLOCKS, std::max<size_t>(1, (n + 255) / 256)); }
+    int dot(size_t n, const T *x, const T *y, double *out)
+    {
+        const int g = grid(n);
+        k_dot_partial<T><<<g, 256, 0, st>>>(n, x, y, part.p);
+        RTM_CUDA(cudaGetLastError());
+        k_sum_partials<<<1, 32, 0, st>>>(g, part.p, part.p + DOT_BLOCKS);
+        RTM_CUDA(cudaGetLastError());
+        RTM_CUDA(cudaMemcpyAsync(out, part.p + DOT_BLOCKS, sizeof(double), cudaMemcpyDeviceToHost, st));
+        RTM_CUDA(cudaStreamSynchronize(st));
+        return RTM_OK;
+    }
+    int axpy(size_t n, double a, const T *x, T *y)
+    {
+        k_axpy<T><<<grid(n), 256, 0, st>>>(n, (T)a, x, y);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    }
+    int xpby(size_t n, const T *s, double b, T *p)
+    {
+        k_xpby<T><<<grid(n), 256, 0, st>>>(n, s, (T)b, p);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    }
+};
+
+// Least-squares RTM: niter iterations of conjugate gradients on the normal
+// equations (CGLS) for the linear Born operator L of all shots stacked,
+// min || L m - d ||^2 with m = (drho, dlambda, dmu), starting from m = 0.
+// L^T is the exact adjoint.  resid[k] = ||d - L m_k|| (k = 0..niter).
+template <typename T>
+int lsrtm_impl(int nz, int nx, int nt, T dx, T dt, T fp, int nsource, int abc, int nshots, const int *xsrc,
+               const int *zsrc, int zrec, const T *rho, const T *lam, const T *mu, const T *data, int niter, T *dm,
+               double *resid, bool exact)
+{
+    RTM_CHECK_ARG(nshots >= 1 && niter >= 0 && xsrc && zsrc && data && dm, "bad LSRTM arguments");
+    TRY(ensure_device());
+    const size_t plane = (size_t)nz * nx, nm = 3 * plane, gs = (size_t)nt * nx, nd1 = 5 * gs,
+                 nd = nd1 * (size_t)nshots;
+    DevBuf<T> model;
+    TRY(model.alloc(3 * plane));
+    RTM_CUDA(cudaMemcpy(model.p, rho, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + plane, lam, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + 2 * plane, mu, plane * sizeof(T), cudaMemcpyHostToDevice));
+    std::vector<std::unique_ptr<BornShot<T>>> shots;
+    for (int s = 0; s < nshots; s++) {
+        shots.emplace_back(new BornShot<T>());
+        TRY(shots.back()->init(nz, nx, nt, dx, dt, xsrc[s], zsrc[s], zrec, fp, nsource, abc, model.p, exact));
+    }
+    cudaStream_t st = shots[0]->h.st;
+    const size_t vol = shots[0]->vol;
+    DevBuf<T> W, rec, x, r, sv, p, q, tmp;
+    TRY(W.alloc(5 * vol));
+    T *A[5];
+    for (int f = 0; f < 5; f++) A[f] = W.p + f * vol;
+    TRY(rec.alloc((size_t)nt * 5 * nx));
+    TRY(x.alloc(nm)); TRY(sv.alloc(nm)); TRY(p.alloc(nm)); TRY(tmp.alloc(nm));
+    TRY(r.alloc(nd)); TRY(q.alloc(nd));
+    RTM_CUDA(cudaMemsetAsync(x.p, 0, nm * sizeof(T), st));
+    RTM_CUDA(cudaMemcpyAsync(r.p, data, nd * sizeof(T), cudaMemcpyHostToDevice, st));
+    Vec<T> v;
+    TRY(v.init(st));
+    // L m for all shots (data of shot s at offset s*nd1)
+    auto apply = [&](const T *m, T *out) -> int {
+        for (int s = 0; s < nshots; s++)
+            TRY(shots[s]->born(m, m + plane, m + 2 * plane, A, rec.p, out + (size_t)s * nd1));
+        return RTM_OK;
+    };
+    // L^T d summed over shots
+    auto apply_t = [&](const T *d, T *out) -> int {
+        for (int s = 0; s < nshots; s++) {
+            TRY(shots[s]->adjoint(d + (size_t)s * nd1, A, s ? tmp.p : out, true));
+            if (s) TRY(v.axpy(nm, 1.0, tmp.p, out));
+        }
+        return RTM_OK;
+    };
+    double rr = 0, gamma = 0, qq = 0;
+    TRY(v.dot(nd, r.p, r.p, &rr));
+    if (resid) resid[0] = std::sqrt(rr);
+    TRY(apply_t(r.p, sv.p));
+    TRY(v.dot(nm, sv.p, sv.p, &gamma));
+    RTM_CUDA(cudaMemcpyAsync(p.p, sv.p, nm * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    for (int k = 1; k <= niter; k++) {
+        if (gamma <= 0) {  // exact solution reached
+            if (resid) for (int j = k; j <= niter; j++) resid[j] = std::sqrt(rr);
+            break;
+        }
+        TRY(apply(p.p, q.p));
+        TRY(v.dot(nd, q.p, q.p, &qq));
+        if (qq <= 0) {
+            if (resid) for (int j = k; j <= niter; j++) resid[j] = std::sqrt(rr);
+            break;
+        }
+        const double alpha = gamma / qq;
+        TRY(v.axpy(nm, alpha, p.p, x.p));
+        TRY(v.axpy(nd, -alpha, q.p, r.p));
+        TRY(v.dot(nd, r.p, r.p, &rr));
+        if (resid) resid[k] = std::sqrt(rr);
+        TRY(apply_t(r.p, sv.p));
+        double gnew = 0;
+        TRY(v.dot(nm, sv.p, sv.p, &gnew));
+        const double beta = gnew / gamma;
+        gamma = gnew;
+        TRY(v.xpby(nm, sv.p, beta, p.p));
+    }
+    RTM_CUDA(cudaMemcpyAsync(dm, x.p, nm * sizeof(T), cudaMemcpyDeviceToHost, st));
+    RTM_CUDA(cudaStreamSynchronize(st));
     return RTM_OK;
 }
 
@@ -637,6 +851,23 @@ extern "C" int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, in
     float *D[5] = {Vx, Vz, sigmaxx, sigmazz, sigmaxz};
     return rtm_op_impl<float>(adj, nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, rho, lambda, mu, drho,
                               dlambda, dmu, D, linear, exact_adjoint, g_exact != 0);
+}
+
+extern "C" int rtm_lsrtm_c_(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc, int nshots,
+                            const int *xsrc, const int *zsrc, int zrec, const float *rho, const float *lambda,
+                            const float *mu, const float *data, int niter, float *dm, double *resid)
+{
+    return lsrtm_impl<float>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, rho, lambda, mu, data,
+                             niter, dm, resid, g_exact != 0);
+}
+
+extern "C" int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int nsource, int abc,
+                            int nshots, const int *xsrc, const int *zsrc, int zrec, const double *rho,
+                            const double *lambda, const double *mu, const double *data, int niter, double *dm,
+                            double *resid)
+{
+    return lsrtm_impl<double>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, rho, lambda, mu, data,
+                              niter, dm, resid, true);
 }
 
 extern "C" int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, int zsrc, int zrec,

@@ -165,3 +165,32 @@ class RtmOperator:
                  self.zrec, self.fp, self.nsource, self.abc, ptr(self.rho), ptr(self.lam), ptr(self.mu),
                  *[ptr(a) for a in arrs], 1 if self.linear else 0, 1 if self.exact_adjoint else 0))
         return 0
+
+
+def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, nsource=250, dtype=F32):
+    """Least-squares RTM by CGLS on the linear Born operator of ``rtm_op``
+    (linear=True) with its exact adjoint, over all shots stacked.
+
+    rho, lam, mu: (nx, nz) models.  data: (nshots, 5, nx, nt) gathers in the
+    order Vx, Vz, sigmaxx, sigmazz, sigmaxz.  xsrc, zsrc: 1-based source
+    positions per shot.  Returns (dm, resid): dm (3, nx, nz) = (drho,
+    dlambda, dmu) after niter iterations from zero, resid (niter+1,) the
+    data residual norms ||d - L m_k||.
+    """
+    dtype = np.dtype(dtype)
+    rho, lam, mu = (np.ascontiguousarray(a, dtype) for a in (rho, lam, mu))
+    nx, nz = rho.shape
+    data = np.ascontiguousarray(data, dtype)
+    nshots = data.shape[0]
+    if data.shape != (nshots, 5, nx, nt):
+        raise ValueError(f"data must be (nshots, 5, {nx}, {nt}), got {data.shape}")
+    xs = np.ascontiguousarray(xsrc, np.int32)
+    zs = np.ascontiguousarray(zsrc, np.int32)
+    if xs.shape != (nshots,) or zs.shape != (nshots,):
+        raise ValueError("one source position per shot")
+    dm = np.zeros((3, nx, nz), dtype)
+    resid = np.zeros(niter + 1, np.float64)
+    fn = load().rtm_lsrtm_d_ if dtype == np.float64 else load().rtm_lsrtm_c_
+    check(fn(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, ptr(xs), ptr(zs), zrec, ptr(rho), ptr(lam), ptr(mu),
+             ptr(data), niter, ptr(dm), ptr(resid)))
+    return dm, resid

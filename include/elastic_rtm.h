@@ -156,6 +156,23 @@ int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, int xsrc, int
               int nsource, int abc, const float *rho, const float *lambda, const float *mu, float *drho,
               float *dlambda, float *dmu, float *Vx, float *Vz, float *sigmaxx, float *sigmazz, float *sigmaxz,
               int linear, int exact_adjoint);
+/* Least-squares RTM (no counterpart in the reference, which only intends an
+ * iterative solver, W/rtm-mod-adj.f90:5-7): niter iterations of conjugate
+ * gradients on the normal equations (CGLS) for the linear Born operator of
+ * rtm_op_c_ (linear=1) over nshots shots on the full grid, with its exact
+ * adjoint (exact_adjoint=1) as transpose, starting from a zero model.
+ * xsrc/zsrc: 1-based source positions per shot; data: per shot the five
+ * gathers of rtm_op_c_ (Vx, Vz, sigmaxx, sigmazz, sigmaxz, each (nt,nx)
+ * Fortran order), shots consecutive.  dm: three (nz,nx) planes (drho,
+ * dlambda, dmu) out.  resid (optional, niter+1 doubles): ||d - L m_k||.
+ * Each shot's source history (5 nz*nx*nt volumes) stays on the device. */
+int rtm_lsrtm_c_(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc, int nshots,
+                 const int *xsrc, const int *zsrc, int zrec, const float *rho, const float *lambda, const float *mu,
+                 const float *data, int niter, float *dm, double *resid);
+int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int nsource, int abc, int nshots,
+                 const int *xsrc, const int *zsrc, int zrec, const double *rho, const double *lambda,
+                 const double *mu, const double *data, int niter, double *dm, double *resid);
+
 /* Double-precision twin of rtm_op_c_ (used for the FP64 oracle comparison
  * and the adjoint dot-product test). */
 int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, int zsrc, int zrec, double fp,
