@@ -45,6 +45,15 @@ SIGNATURES = {
                      + [_c_int, _P, _P]),
     "rtm_lsrtm_d_": (_c_int, [_c_int] * 3 + [_c_double] * 3 + [_c_int] * 3 + [_P, _P, _c_int] + [_P] * 4
                      + [_c_int, _P, _P]),
+    "unet_create": (ctypes.c_void_p, [_c_int, _c_int, _c_int, ctypes.c_uint]),
+    "unet_destroy": (None, [_P]),
+    "unet_num_params": (ctypes.c_longlong, [_P]),
+    "unet_layer_info": (_c_int, [_P, _c_int, _P]),
+    "unet_get_params": (_c_int, [_P, _P]),
+    "unet_set_params": (_c_int, [_P, _P]),
+    "unet_forward": (_c_int, [_P, _P, _c_int, _P, _c_int]),
+    "unet_loss_grad": (_c_int, [_P, _P, _P, _c_int, _c_int, _P, _P]),
+    "unet_train_step": (_c_int, [_P, _P, _P, _c_int, _c_int, _c_float, _c_float, _c_float, _c_float, _P]),
     "rtm_batch_create": (ctypes.c_void_p, [_c_int, _c_int, _c_int, _c_float, _c_float, _c_float, _c_int, _c_int]
                          + [_P] * 3 + [_c_int] + [_P] * 5 + [_c_int, _c_int, _c_int]),
     "rtm_batch_migrate": (_c_int, [_P, _c_int, _c_int, _P, _c_int, _P, _c_int]),

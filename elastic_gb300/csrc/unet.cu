@@ -1,0 +1,1008 @@
+// Learned image-domain preconditioner: a 4-level 3->3 channel convolutional
+// U-Net (about 0.9M parameters) with BF16 weights and activations and FP32
+// accumulation, trained with Adam.  Every convolution pass -- forward,
+// backward-data and backward-weights -- is one tensor-core GEMM of this file
+// (mma.sync m16n8k16 BF16, FP32 accumulators, cp.async 3-stage pipeline)
+// on im2col operands in NHWC layout.
+//
+// Network (channels c = 32, 64, 96, 128; 3x3 convolutions with ReLU):
+//   e1: 3->32->32    (H)      skip s1
+//   e2: 32->64->64   (H/2)    skip s2    (2x2 average pool between levels)
+//   e3: 64->96->96   (H/4)    skip s3
+//   b : 96->128->128 (H/8)
+//   d3: [up(b) 128 | s3 96] -> 96 -> 96    (nearest 2x upsampling)
+//   d2: [up(d3) 96 | s2 64] -> 64 -> 64
+//   d1: [up(d2) 64 | s1 32] -> 32 -> 32
+//   out: 1x1 convolution 32->3, no activation; loss = mean squared error.
+//
+// There is no counterpart in the reference (lgan/elastic only intends an
+// iterative solver, 2d_rtm_restart/Src_working/rtm-mod-adj.f90:5-7).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "../../include/elastic_rtm.h"
+#include "common.cuh"
+#include "engine.h"
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+using eg::DevBuf;
+
+// ----------------------------------------------------------------- GEMM
+// C[M,N] = A[M,K] * B[N,K]^T with BF16 operands and FP32 accumulation.
+// A_T=false: A[m*lda + k] (K contiguous); A_T=true: A[k*lda + m].
+// B_T=false: B[n*ldb + k];                 B_T=true: B[k*ldb + n].
+// K is a multiple of 32; split-K over blockIdx.z in chunks of kchunk.
+enum Epi { EPI_BF16 = 0, EPI_F32 = 1, EPI_F32_ATOMIC_T = 2 };
+
+struct GemmArgs {
+    const bf16 *A;
+    long long lda;
+    const bf16 *B;
+    long long ldb;
+    int M, N, K, kchunk;
+    const float *bias;  // EPI_BF16 / EPI_F32: per-n bias (or null)
+    int relu;           // EPI_BF16: ReLU after the bias
+    bf16 *Cb;           // EPI_BF16: Cb[m*ldc + coff + n]
+    float *Cf;          // EPI_F32: Cf[m*ldc + n]; EPI_F32_ATOMIC_T: Cf[n*ldc + m] += acc
+    long long ldc;
+    int coff;
+};
+
+constexpr int GBM = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
+
+template <bool A_T, bool B_T, int BN>
+struct GemmSmem {
+    static constexpr int A_ELEMS = A_T ? GBK * (GBM + 8) : GBM * (GBK + 8);
+    static constexpr int B_ELEMS = B_T ? GBK * (BN + 8) : BN * (GBK + 8);
+    static constexpr int STAGE = A_ELEMS + B_ELEMS;
+    static constexpr size_t BYTES = (size_t)GSTAGES * STAGE * sizeof(bf16);
+};
+
+__device__ __forceinline__ void cpa16(void *smem, const void *gmem, bool ok)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(ok ? 16 : 0));
+}
+__device__ __forceinline__ void ldsm_x4(unsigned r[4], const void *p)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(s));
+}
+__device__ __forceinline__ void ldsm_x4_t(unsigned r[4], const void *p)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(s));
+}
+__device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], unsigned b0, unsigned b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <bool A_T, bool B_T, int BN, int EPI>
+__global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
+{
+    using S = GemmSmem<A_T, B_T, BN>;
+    extern __shared__ __align__(16) unsigned char gsm_raw[];
+    bf16 *sm = reinterpret_cast<bf16 *>(gsm_raw);
+    constexpr int NT = BN / 16;  // n8 tiles per warp (warp tile 32 x BN/2)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp & 3, wn = warp >> 2;
+    const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * BN;
+    const int kbeg = blockIdx.z * g.kchunk;
+    const int kend = min(g.K, kbeg + g.kchunk);
+    const int ktiles = kend > kbeg ? (kend - kbeg) / GBK : 0;
+
+    auto load = [&](int kt, int stage) {
+        bf16 *sa = sm + stage * S::STAGE, *sb = sa + S::A_ELEMS;
+        const int k0 = kbeg + kt * GBK;
+        if (!A_T) {
+            for (int c = tid; c < GBM * 4; c += GTHREADS) {
+                const int r = c >> 2, q = c & 3;
+                const bool ok = m0 + r < g.M;
+                const bf16 *src = g.A + (ok ? (long long)(m0 + r) * g.lda + k0 + q * 8 : 0);
+                cpa16(sa + r * (GBK + 8) + q * 8, src, ok);
+            }
+        } else {
+            for (int c = tid; c < GBK * (GBM / 8); c += GTHREADS) {
+                const int r = c / (GBM / 8), q = c % (GBM / 8);
+                const bool ok = m0 + q * 8 < g.M;
+                const bf16 *src = g.A + (ok ? (long long)(k0 + r) * g.lda + m0 + q * 8 : 0);
+                cpa16(sa + r * (GBM + 8) + q * 8, src, ok);
+            }
+        }
+        if (!B_T) {
+            for (int c = tid; c < BN * 4; c += GTHREADS) {
+                const int r = c >> 2, q = c & 3;
+                const bool ok = n0 + r < g.N;
+                const bf16 *src = g.B + (ok ? (long long)(n0 + r) * g.ldb + k0 + q * 8 : 0);
+                cpa16(sb + r * (GBK + 8) + q * 8, src, ok);
+            }
+        } else {
+            for (int c = tid; c < GBK * (BN / 8); c += GTHREADS) {
+                const int r = c / (BN / 8), q = c % (BN / 8);
+                const bool ok = n0 + q * 8 < g.N;
+                const bf16 *src = g.B + (ok ? (long long)(k0 + r) * g.ldb + n0 + q * 8 : 0);
+                cpa16(sb + r * (BN + 8) + q * 8, src, ok);
+            }
+        }
+    };
+
+    float acc[2][NT][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < NT; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.f;
+
+#pragma unroll
+    for (int s = 0; s < GSTAGES - 1; s++) {
+        if (s < ktiles) load(s, s);
+        asm volatile("cp.async.commit_group;\n" ::);
+    }
+    for (int kt = 0; kt < ktiles; kt++) {
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(GSTAGES - 2));
+        __syncthreads();
+        if (kt + GSTAGES - 1 < ktiles) load(kt + GSTAGES - 1, (kt + GSTAGES - 1) % GSTAGES);
+        asm volatile("cp.async.commit_group;\n" ::);
+        const bf16 *sa = sm + (kt % GSTAGES) * S::STAGE, *sb = sa + S::A_ELEMS;
+#pragma unroll
+        for (int ks = 0; ks < GBK; ks += 16) {
+            unsigned af[2][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const int mb = wm * 32 + mt * 16;
+                if (!A_T) {
+                    ldsm_x4(af[mt], sa + (mb + (lane & 15)) * (GBK + 8) + ks + (lane >> 4) * 8);
+                } else {
+                    const int k = ks + (lane & 7) + (lane >> 4) * 8, m = mb + ((lane >> 3) & 1) * 8;
+                    ldsm_x4_t(af[mt], sa + k * (GBM + 8) + m);
+                }
+            }
+#pragma unroll
+            for (int np = 0; np < NT / 2; np++) {
+                const int nb = wn * (BN / 2) + np * 16;
+                unsigned bfr[4];
+                if (!B_T) {
+                    const int n = nb + (lane & 7) + (lane >> 4) * 8, k = ks + ((lane >> 3) & 1) * 8;
+                    ldsm_x4(bfr, sb + n * (GBK + 8) + k);
+                } else {
+                    const int k = ks + (lane & 7) + ((lane >> 3) & 1) * 8, n = nb + (lane >> 4) * 8;
+                    ldsm_x4_t(bfr, sb + k * (BN + 8) + n);
+                }
+#pragma unroll
+                for (int mt = 0; mt < 2; mt++) {
+                    mma_bf16(acc[mt][2 * np], af[mt], bfr[0], bfr[1]);
+                    mma_bf16(acc[mt][2 * np + 1], af[mt], bfr[2], bfr[3]);
+                }
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+
+    // epilogue
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int m = m0 + wm * 32 + mt * 16 + (lane >> 2) + h * 8;
+                const int n = n0 + wn * (BN / 2) + nt * 8 + (lane & 3) * 2;
+                if (m >= g.M) continue;
+                float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
+                if (EPI == EPI_F32_ATOMIC_T) {
+                    if (n < g.N) atomicAdd(g.Cf + (long long)n * g.ldc + m, v0);
+                    if (n + 1 < g.N) atomicAdd(g.Cf + (long long)(n + 1) * g.ldc + m, v1);
+                    continue;
+                }
+                if (g.bias) {
+                    if (n < g.N) v0 += g.bias[n];
+                    if (n + 1 < g.N) v1 += g.bias[n + 1];
+                }
+                if (EPI == EPI_F32) {
+                    if (n < g.N) g.Cf[(long long)m * g.ldc + n] = v0;
+                    if (n + 1 < g.N) g.Cf[(long long)m * g.ldc + n + 1] = v1;
+                } else {
+                    if (g.relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    bf16 *dst = g.Cb + (long long)m * g.ldc + g.coff + n;
+                    if (n + 1 < g.N) {
+                        *reinterpret_cast<__nv_bfloat162 *>(dst) = __floats2bfloat162_rn(v0, v1);
+                    } else if (n < g.N) {
+                        *dst = __float2bfloat16_rn(v0);
+                    }
+                }
+            }
+}
+
+template <bool A_T, bool B_T, int BN, int EPI>
+int gemm_launch(const GemmArgs &g, int splits, cudaStream_t st)
+{
+    using S = GemmSmem<A_T, B_T, BN>;
+    auto kern = k_gemm<A_T, B_T, BN, EPI>;
+    static bool attr = false;
+    if (!attr) {
+        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES));
+        attr = true;
+    }
+    dim3 grid((g.M + GBM - 1) / GBM, (g.N + BN - 1) / BN, splits);
+    kern<<<grid, GTHREADS, S::BYTES, st>>>(g);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+// Dispatch on operand layouts, epilogue and the N tile (32, 64 or 128).
+template <bool A_T, bool B_T, int EPI>
+int gemm_bn(const GemmArgs &g, int splits, cudaStream_t st)
+{
+    if (g.N <= 32) return gemm_launch<A_T, B_T, 32, EPI>(g, splits, st);
+    if (g.N % 128 == 0) return gemm_launch<A_T, B_T, 128, EPI>(g, splits, st);
+    if (g.N % 64 == 0) return gemm_launch<A_T, B_T, 64, EPI>(g, splits, st);
+    return gemm_launch<A_T, B_T, 32, EPI>(g, splits, st);
+}
+
+int gemm(const GemmArgs &g, bool a_t, bool b_t, int epi, int splits, cudaStream_t st)
+{
+    RTM_CHECK_ARG(g.K % GBK == 0 && g.kchunk % GBK == 0 && g.kchunk > 0, "GEMM K=%d (chunk %d) not a multiple of 32",
+                  g.K, g.kchunk);
+    RTM_CHECK_ARG(!a_t || g.M % 8 == 0, "GEMM with M-major A needs M %% 8 == 0 (M=%d)", g.M);
+    RTM_CHECK_ARG(!b_t || g.N % 8 == 0, "GEMM with N-major B needs N %% 8 == 0 (N=%d)", g.N);
+    RTM_CHECK_ARG(epi != EPI_BF16 || ((g.ldc | g.coff) & 1) == 0, "BF16 GEMM output needs even ldc and offset");
+    if (epi == EPI_BF16 && !a_t && !b_t) return gemm_bn<false, false, EPI_BF16>(g, splits, st);
+    if (epi == EPI_F32 && !a_t && !b_t) return gemm_bn<false, false, EPI_F32>(g, splits, st);
+    if (epi == EPI_F32_ATOMIC_T && a_t && b_t) return gemm_bn<true, true, EPI_F32_ATOMIC_T>(g, splits, st);
+    rtm_set_error("GEMM variant not instantiated (a_t=%d b_t=%d epi=%d)", a_t, b_t, epi);
+    return RTM_ERR_ARG;
+}
+
+// ------------------------------------------------------- layout kernels
+// im2col of a 3x3, pad-1 convolution in NHWC: col[p][(ky*3+kx)*C + c],
+// columns [9C, Kp) zero.  x: channels [coff, coff+C) of pixels with stride ldx.
+__global__ void k_im2col3(int n, int H, int W, int C, const bf16 *x, int ldx, int coff, bf16 *col, int Kp)
+{
+    const long long P = (long long)n * H * W;
+    const long long total = P * Kp;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / Kp;
+        const int k = (int)(i - p * Kp);
+        bf16 v = __float2bfloat16_rn(0.f);
+        if (k < 9 * C) {
+            const int tap = k / C, c = k - tap * C, ky = tap / 3, kx = tap - ky * 3;
+            const int xw = (int)(p % W), yh = (int)((p / W) % H);
+            const long long b = p / ((long long)W * H);
+            const int yy = yh + ky - 1, xx = xw + kx - 1;
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+                v = x[((b * H + yy) * W + xx) * ldx + coff + c];
+        }
+        col[i] = v;
+    }
+}
+// Vector im2col for C % 8 == 0 (16-byte chunks of 8 channels).
+__global__ void k_im2col3_v8(int n, int H, int W, int C, const bf16 *x, int ldx, int coff, bf16 *col, int Kp)
+{
+    const long long P = (long long)n * H * W;
+    const int kc = Kp / 8;
+    const long long total = P * kc;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / kc;
+        const int k = (int)(i - p * kc) * 8;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (k < 9 * C) {
+            const int tap = k / C, c = k - tap * C, ky = tap / 3, kx = tap - ky * 3;
+            const int xw = (int)(p % W), yh = (int)((p / W) % H);
+            const long long b = p / ((long long)W * H);
+            const int yy = yh + ky - 1, xx = xw + kx - 1;
+            if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+                v = *reinterpret_cast<const uint4 *>(x + ((b * H + yy) * W + xx) * ldx + coff + c);
+        }
+        *reinterpret_cast<uint4 *>(col + p * Kp + k) = v;
+    }
+}
+
+// g *= (y > 0), elementwise over P pixels x C channels (stride ld).
+__global__ void k_relu_mask(long long P, int C, int ld, const bf16 *y, bf16 *g)
+{
+    const long long total = P * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / C;
+        const int c = (int)(i - p * C);
+        if (!(__bfloat162float(y[p * ld + c]) > 0.f)) g[p * ld + c] = __float2bfloat16_rn(0.f);
+    }
+}
+
+// db[c] += sum_p g[p][c] (channels on threads, pixels split over blocks)
+__global__ void k_bias_grad(long long P, int C, int ld, const bf16 *g, float *db)
+{
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    const long long per = (P + gridDim.x - 1) / gridDim.x;
+    const long long p0 = blockIdx.x * per, p1 = min(P, p0 + per);
+    float s = 0.f;
+    for (long long p = p0; p < p1; p++) s += __bfloat162float(g[p * ld + c]);
+    atomicAdd(db + c, s);
+}
+
+// 2x2 average pool, NHWC; out channels [0,C) stride ldo, in stride ldi.
+__global__ void k_pool_fwd(int n, int Ho, int Wo, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
+{
+    const long long total = (long long)n * Ho * Wo * C;
+    const int Wi = 2 * Wo, Hi = 2 * Ho;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
+        const float s = __bfloat162float(in[q * ldi + c]) + __bfloat162float(in[(q + 1) * ldi + c]) +
+                        __bfloat162float(in[(q + Wi) * ldi + c]) + __bfloat162float(in[(q + Wi + 1) * ldi + c]);
+        out[p * ldo + c] = __float2bfloat16_rn(0.25f * s);
+    }
+}
+// gin[2y+i][2x+j] += 0.25 * gout[y][x]
+__global__ void k_pool_bwd_add(int n, int Ho, int Wo, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
+{
+    const long long total = (long long)n * Ho * Wo * C;
+    const int Wi = 2 * Wo, Hi = 2 * Ho;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
+        const float g = 0.25f * __bfloat162float(gout[p * ldo + c]);
+        const long long qs[4] = {q, q + 1, q + Wi, q + Wi + 1};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            bf16 *d = gin + qs[k] * ldi + c;
+            *d = __float2bfloat16_rn(__bfloat162float(*d) + g);
+        }
+    }
+}
+// nearest 2x upsampling into channels [0,C) of out (stride ldo)
+__global__ void k_up_fwd(int n, int Hi, int Wi, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
+{
+    const int Ho = 2 * Hi, Wo = 2 * Wi;
+    const long long total = (long long)n * Ho * Wo * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        out[p * ldo + c] = in[((b * Hi + y / 2) * Wi + x / 2) * ldi + c];
+    }
+}
+// gin[y][x] = sum of the 4 gout pixels it was copied to (channels [0,C) of gout)
+__global__ void k_up_bwd(int n, int Hi, int Wi, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
+{
+    const int Wo = 2 * Wi, Ho = 2 * Hi;
+    const long long total = (long long)n * Hi * Wi * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        const long long p = i / C;
+        const int x = (int)(p % Wi), y = (int)((p / Wi) % Hi);
+        const long long b = p / ((long long)Wi * Hi);
+        const long long q = (b * Ho + 2 * y) * Wo + 2 * x;
+        const float s = __bfloat162float(gout[q * ldo + c]) + __bfloat162float(gout[(q + 1) * ldo + c]) +
+                        __bfloat162float(gout[(q + Wo) * ldo + c]) + __bfloat162float(gout[(q + Wo + 1) * ldo + c]);
+        gin[p * ldi + c] = __float2bfloat16_rn(s);
+    }
+}
+// dst[p][doff + c] = src[p][soff + c] (add: dst += src, in FP32)
+__global__ void k_copy_ch(long long P, int C, const bf16 *src, int lds, int soff, bf16 *dst, int ldd, int doff, int add)
+{
+    const long long total = P * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / C;
+        const int c = (int)(i - p * C);
+        const bf16 v = src[p * lds + soff + c];
+        bf16 *d = dst + p * ldd + doff + c;
+        *d = add ? __float2bfloat16_rn(__bfloat162float(*d) + __bfloat162float(v)) : v;
+    }
+}
+// FP32 NHWC (C channels) -> BF16
+__global__ void k_to_bf16(long long n, const float *x, bf16 *y)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16_rn(x[i]);
+}
+// loss partials and output gradient: out (P x ldo FP32, channels [0,C)),
+// target (P x C); g (P x ldg BF16, channels [0,C) = 2(out-t)/(P*C), rest 0)
+__global__ void k_mse(long long P, int C, const float *out, int ldo, const float *t, bf16 *g, int ldg, double *part)
+{
+    double acc = 0.0;
+    const double scale = 2.0 / ((double)P * C);
+    const long long total = P * ldg;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / ldg;
+        const int c = (int)(i - p * ldg);
+        float gv = 0.f;
+        if (c < C) {
+            const double d = (double)out[p * ldo + c] - (double)t[p * C + c];
+            acc += d * d;
+            gv = (float)(scale * d);
+        }
+        g[i] = __float2bfloat16_rn(gv);
+    }
+    __shared__ double red[32];
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+        part[blockIdx.x] = s;
+    }
+}
+// out (P x ldo FP32) channels [0,C) -> y (P x C)
+__global__ void k_take(long long P, int C, const float *out, int ldo, float *y)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P * C; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / C;
+        y[i] = out[p * ldo + (int)(i - p * C)];
+    }
+}
+// Adam on a flat FP32 parameter vector (bias-corrected step sizes given)
+__global__ void k_adam(long long n, float *w, const float *g, float *m, float *v, float lr_t, float b1, float b2,
+                       float eps_t)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        w[i] -= lr_t * mi / (sqrtf(vi) + eps_t);
+    }
+}
+// BF16 weights of a layer: W [coutp][kp] and the backward-data weights
+// Wt [cin][9*coutp'] (3x3: flipped taps, cout/cin swapped; 1x1: transpose
+// into [cin][32]).
+__global__ void k_weights(int ks, int cin, int cout, int coutp, int kp, int ktp, const float *w, bf16 *wb, bf16 *wt)
+{
+    const int nw = coutp * kp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x) wb[i] = __float2bfloat16_rn(w[i]);
+    if (!wt) return;
+    const int nt = cin * ktp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        const int ci = i / ktp, k = i - ci * ktp;
+        float v = 0.f;
+        if (ks == 3) {
+            const int tap = k / coutp, co = k - tap * coutp;  // tap = ky'*3+kx'
+            if (co < cout) v = w[co * kp + (8 - tap) * cin + ci];
+        } else {
+            if (k < cout) v = w[k * kp + ci];
+        }
+        wt[i] = __float2bfloat16_rn(v);
+    }
+}
+
+int grid_for(long long n, int per = 256)
+{
+    long long g = (n + per - 1) / per;
+    const long long cap = 16LL * eg::device_sm_count() * 8;
+    return (int)std::max(1LL, std::min(g, cap));
+}
+
+// ------------------------------------------------------------- network
+struct Layer {
+    int ks, cin, cout, coutp, kp, ktp;  // ktp: K of the backward-data GEMM
+    long long woff, boff;              // offsets in the flat parameter vector
+    int H, W;                          // spatial size of this layer's output
+    DevBuf<bf16> wb, wt;
+    bool relu;
+};
+
+constexpr int NCONV = 15;
+
+}  // namespace
+
+struct unet {
+    int H = 0, W = 0, nmax = 0, cin = 3, cout = 3;
+    int ch[4] = {32, 64, 96, 128};
+    Layer L[NCONV];
+    long long nparam = 0;
+    DevBuf<float> w, gw, m, v;       // FP32 master weights, gradients, Adam moments
+    long long step = 0;
+    // activations (BF16 NHWC)
+    DevBuf<bf16> xin, a[NCONV], pool[3], cat[3];
+    DevBuf<bf16> ga[NCONV], gpool[3], gcat[3];
+    DevBuf<bf16> col, gout;
+    DevBuf<float> out, tgt;
+    DevBuf<double> part;
+    cudaStream_t st = nullptr;
+    int n_last = 0;
+
+    ~unet()
+    {
+        if (st) cudaStreamDestroy(st);
+    }
+};
+
+namespace {
+
+// layer order: e1a e1b e2a e2b e3a e3b ba bb d3a d3b d2a d2b d1a d1b out
+int setup(unet *u)
+{
+    const int *c = u->ch;
+    struct Spec { int ks, cin, cout, lvl; } spec[NCONV] = {
+        {3, u->cin, c[0], 0}, {3, c[0], c[0], 0}, {3, c[0], c[1], 1}, {3, c[1], c[1], 1},
+        {3, c[1], c[2], 2},   {3, c[2], c[2], 2}, {3, c[2], c[3], 3}, {3, c[3], c[3], 3},
+        {3, c[3] + c[2], c[2], 2}, {3, c[2], c[2], 2}, {3, c[2] + c[1], c[1], 1}, {3, c[1], c[1], 1},
+        {3, c[1] + c[0], c[0], 0}, {3, c[0], c[0], 0}, {1, c[0], u->cout, 0}};
+    long long off = 0;
+    for (int i = 0; i < NCONV; i++) {
+        Layer &l = u->L[i];
+        l.ks = spec[i].ks;
+        l.cin = spec[i].cin;
+        l.cout = spec[i].cout;
+        l.coutp = l.ks == 1 ? 8 : l.cout;
+        l.kp = l.ks == 3 ? (9 * l.cin + 31) / 32 * 32 : (l.cin + 31) / 32 * 32;
+        l.ktp = l.ks == 3 ? 9 * l.coutp : 32;
+        l.H = u->H >> spec[i].lvl;
+        l.W = u->W >> spec[i].lvl;
+        l.relu = i != NCONV - 1;
+        l.woff = off;
+        off += (long long)l.coutp * l.kp;
+        l.boff = off;
+        off += l.coutp;
+        TRY(l.wb.alloc((size_t)l.coutp * l.kp));
+        TRY(l.wt.alloc((size_t)l.cin * l.ktp));
+    }
+    u->nparam = off;
+    TRY(u->w.alloc(off));
+    TRY(u->gw.alloc(off));
+    TRY(u->m.alloc(off));
+    TRY(u->v.alloc(off));
+    RTM_CUDA(cudaMemset(u->w.p, 0, off * sizeof(float)));
+    RTM_CUDA(cudaMemset(u->m.p, 0, off * sizeof(float)));
+    RTM_CUDA(cudaMemset(u->v.p, 0, off * sizeof(float)));
+    // activations for nmax images
+    const long long P0 = (long long)u->nmax * u->H * u->W;
+    long long maxcol = 0;
+    for (int i = 0; i < NCONV; i++) {
+        const Layer &l = u->L[i];
+        const long long P = (long long)u->nmax * l.H * l.W;
+        TRY(u->a[i].alloc((size_t)P * l.coutp));
+        TRY(u->ga[i].alloc((size_t)P * std::max(l.coutp, 32)));
+        maxcol = std::max(maxcol, P * (long long)std::max(l.kp, l.ktp));
+    }
+    for (int k = 0; k < 3; k++) {
+        const long long Pp = (long long)u->nmax * (u->H >> (k + 1)) * (u->W >> (k + 1));
+        TRY(u->pool[k].alloc((size_t)Pp * c[k]));
+        TRY(u->gpool[k].alloc((size_t)Pp * c[k]));
+        const long long Pc = (long long)u->nmax * (u->H >> k) * (u->W >> k);
+        const int cc = c[k + 1] + c[k];
+        TRY(u->cat[k].alloc((size_t)Pc * cc));
+        TRY(u->gcat[k].alloc((size_t)Pc * cc));
+    }
+    TRY(u->col.alloc((size_t)maxcol));
+    TRY(u->xin.alloc((size_t)P0 * u->cin));
+    TRY(u->gout.alloc((size_t)P0 * 32));
+    TRY(u->out.alloc((size_t)P0 * 8));
+    TRY(u->tgt.alloc((size_t)P0 * u->cout));
+    TRY(u->part.alloc(4096));
+    return RTM_OK;
+}
+
+int refresh_weights(unet *u)
+{
+    for (int i = 0; i < NCONV; i++) {
+        Layer &l = u->L[i];
+        k_weights<<<64, 256, 0, u->st>>>(l.ks, l.cin, l.cout, l.coutp, l.kp, l.ktp, u->w.p + l.woff, l.wb.p, l.wt.p);
+        RTM_CUDA(cudaGetLastError());
+    }
+    return RTM_OK;
+}
+
+int im2col(unet *u, int n, int H, int W, int C, const bf16 *x, int ldx, int coff, int Kp)
+{
+    const long long P = (long long)n * H * W;
+    if (C % 8 == 0 && ldx % 8 == 0 && coff % 8 == 0)
+        k_im2col3_v8<<<grid_for(P * (Kp / 8)), 256, 0, u->st>>>(n, H, W, C, x, ldx, coff, u->col.p, Kp);
+    else
+        k_im2col3<<<grid_for(P * Kp), 256, 0, u->st>>>(n, H, W, C, x, ldx, coff, u->col.p, Kp);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+// input of conv i: (buffer, channel stride, channel offset, channels)
+struct In {
+    const bf16 *p;
+    int ld, off, c;
+};
+
+In layer_input(unet *u, int i)
+{
+    const int *c = u->ch;
+    switch (i) {
+    case 0: return {u->xin.p, u->cin, 0, u->cin};
+    case 2: return {u->pool[0].p, c[0], 0, c[0]};
+    case 4: return {u->pool[1].p, c[1], 0, c[1]};
+    case 6: return {u->pool[2].p, c[2], 0, c[2]};
+    case 8: return {u->cat[2].p, c[3] + c[2], 0, c[3] + c[2]};
+    case 10: return {u->cat[1].p, c[2] + c[1], 0, c[2] + c[1]};
+    case 12: return {u->cat[0].p, c[1] + c[0], 0, c[1] + c[0]};
+    default: return {u->a[i - 1].p, u->L[i - 1].coutp, 0, u->L[i].cin};
+    }
+}
+
+int conv_fwd(unet *u, int i, int n)
+{
+    Layer &l = u->L[i];
+    const In in = layer_input(u, i);
+    const long long P = (long long)n * l.H * l.W;
+    GemmArgs g;
+    memset(&g, 0, sizeof g);
+    if (l.ks == 3) {
+        TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
+        g.A = u->col.p;
+        g.lda = l.kp;
+    } else {
+        g.A = in.p;  // 1x1: the activation is the operand (cin = 32 = kp)
+        g.lda = in.ld;
+    }
+    g.B = l.wb.p;
+    g.ldb = l.kp;
+    g.M = (int)P;
+    g.N = l.coutp;
+    g.K = l.kp;
+    g.kchunk = l.kp;
+    g.bias = u->w.p + l.boff;
+    if (i == NCONV - 1) {
+        g.Cf = u->out.p;
+        g.ldc = 8;
+        return gemm(g, false, false, EPI_F32, 1, u->st);
+    }
+    g.relu = 1;
+    g.Cb = u->a[i].p;
+    g.ldc = l.coutp;
+    return gemm(g, false, false, EPI_BF16, 1, u->st);
+}
+
+int forward(unet *u, int n)
+{
+    const int *c = u->ch;
+    auto pool = [&](int k, const bf16 *src, int ld) {
+        const int Ho = u->H >> (k + 1), Wo = u->W >> (k + 1);
+        k_pool_fwd<<<grid_for((long long)n * Ho * Wo * c[k]), 256, 0, u->st>>>(n, Ho, Wo, c[k], src, ld, u->pool[k].p, c[k]);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    };
+    auto concat = [&](int k, const bf16 *low, int clow, const bf16 *skip) {
+        // cat[k] = [up(low) (clow ch) | skip (c[k] ch)] at level k
+        const int Hl = u->H >> (k + 1), Wl = u->W >> (k + 1), cc = clow + c[k];
+        const long long P = (long long)n * (u->H >> k) * (u->W >> k);
+        k_up_fwd<<<grid_for(P * clow), 256, 0, u->st>>>(n, Hl, Wl, clow, low, clow, u->cat[k].p, cc);
+        RTM_CUDA(cudaGetLastError());
+        k_copy_ch<<<grid_for(P * c[k]), 256, 0, u->st>>>(P, c[k], skip, c[k], 0, u->cat[k].p, cc, clow, 0);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    };
+    TRY(conv_fwd(u, 0, n));
+    TRY(conv_fwd(u, 1, n));
+    TRY(pool(0, u->a[1].p, c[0]));
+    TRY(conv_fwd(u, 2, n));
+    TRY(conv_fwd(u, 3, n));
+    TRY(pool(1, u->a[3].p, c[1]));
+    TRY(conv_fwd(u, 4, n));
+    TRY(conv_fwd(u, 5, n));
+    TRY(pool(2, u->a[5].p, c[2]));
+    TRY(conv_fwd(u, 6, n));
+    TRY(conv_fwd(u, 7, n));
+    TRY(concat(2, u->a[7].p, c[3], u->a[5].p));
+    TRY(conv_fwd(u, 8, n));
+    TRY(conv_fwd(u, 9, n));
+    TRY(concat(1, u->a[9].p, c[2], u->a[3].p));
+    TRY(conv_fwd(u, 10, n));
+    TRY(conv_fwd(u, 11, n));
+    TRY(concat(0, u->a[11].p, c[1], u->a[1].p));
+    TRY(conv_fwd(u, 12, n));
+    TRY(conv_fwd(u, 13, n));
+    TRY(conv_fwd(u, 14, n));
+    return RTM_OK;
+}
+
+// gradient buffer of the input of conv i (where dX goes), channel stride
+struct GIn {
+    bf16 *p;
+    int ld;
+};
+GIn layer_ginput(unet *u, int i)
+{
+    const int *c = u->ch;
+    switch (i) {
+    case 2: return {u->gpool[0].p, c[0]};
+    case 4: return {u->gpool[1].p, c[1]};
+    case 6: return {u->gpool[2].p, c[2]};
+    case 8: return {u->gcat[2].p, c[3] + c[2]};
+    case 10: return {u->gcat[1].p, c[2] + c[1]};
+    case 12: return {u->gcat[0].p, c[1] + c[0]};
+    default: return {u->ga[i - 1].p, u->L[i - 1].coutp};
+    }
+}
+
+// backward of conv i given the gradient of its output in ga[i] (or gout for
+// the last layer): relu mask, bias and weight gradients, input gradient
+int conv_bwd(unet *u, int i, int n, bool need_dx)
+{
+    Layer &l = u->L[i];
+    const long long P = (long long)n * l.H * l.W;
+    const bool last = i == NCONV - 1;
+    bf16 *gy = last ? u->gout.p : u->ga[i].p;
+    const int ldg = last ? 32 : l.coutp;
+    if (l.relu) {
+        k_relu_mask<<<grid_for(P * l.coutp), 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy);
+        RTM_CUDA(cudaGetLastError());
+    }
+    k_bias_grad<<<std::min<long long>(1024, std::max<long long>(1, P / 64)), 128, 0, u->st>>>(P, l.coutp, ldg, gy,
+                                                                                        u->gw.p + l.boff);
+    RTM_CUDA(cudaGetLastError());
+    // weight gradient: dW^T[kp][coutp] = col^T[kp][P] * gy[P][coutp]
+    const In in = layer_input(u, i);
+    GemmArgs g;
+    memset(&g, 0, sizeof g);
+    if (l.ks == 3) {
+        TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
+        g.A = u->col.p;
+        g.lda = l.kp;
+    } else {
+        g.A = in.p;
+        g.lda = in.ld;
+    }
+    g.B = gy;
+    g.ldb = ldg;
+    g.M = l.kp;
+    g.N = l.coutp;
+    const long long Kfull = (P + 31) / 32 * 32;
+    RTM_CHECK_ARG(P % 32 == 0, "pixel count %lld of a U-Net layer is not a multiple of 32", P);
+    g.K = (int)Kfull;
+    // split the pixel reduction so that the grid covers the SMs
+    const int tiles = ((g.M + GBM - 1) / GBM) * ((g.N + 31) / 32);
+    int splits = (int)std::max(1LL, std::min<long long>(Kfull / 256, (4LL * eg::device_sm_count() + tiles - 1) / tiles));
+    long long kc = (Kfull + splits - 1) / splits;
+    kc = (kc + 31) / 32 * 32;
+    splits = (int)((Kfull + kc - 1) / kc);
+    g.kchunk = (int)kc;
+    g.Cf = u->gw.p + l.woff;
+    g.ldc = l.kp;
+    TRY(gemm(g, true, true, EPI_F32_ATOMIC_T, splits, u->st));
+    if (!need_dx) return RTM_OK;
+    // input gradient: dX[P][cin] = im2col(gy)[P][ktp] * Wt[cin][ktp]^T
+    const GIn gin = layer_ginput(u, i);
+    memset(&g, 0, sizeof g);
+    if (l.ks == 3) {
+        TRY(im2col(u, n, l.H, l.W, l.coutp, gy, ldg, 0, l.ktp));
+        g.A = u->col.p;
+        g.lda = l.ktp;
+    } else {
+        g.A = gy;
+        g.lda = ldg;
+    }
+    g.B = l.wt.p;
+    g.ldb = l.ktp;
+    g.M = (int)P;
+    g.N = l.cin;
+    g.K = l.ktp;
+    g.kchunk = l.ktp;
+    g.Cb = gin.p;
+    g.ldc = gin.ld;
+    return gemm(g, false, false, EPI_BF16, 1, u->st);
+}
+
+int backward(unet *u, int n)
+{
+    const int *c = u->ch;
+    RTM_CUDA(cudaMemsetAsync(u->gw.p, 0, u->nparam * sizeof(float), u->st));
+    auto split = [&](int k, int clow, bf16 *glow, bf16 *gskip) {
+        // gcat[k] -> grad of the upsampled low level (into glow) and of the skip
+        const int Hl = u->H >> (k + 1), Wl = u->W >> (k + 1), cc = clow + c[k];
+        const long long P = (long long)n * (u->H >> k) * (u->W >> k);
+        k_up_bwd<<<grid_for((long long)n * Hl * Wl * clow), 256, 0, u->st>>>(n, Hl, Wl, clow, u->gcat[k].p, cc, glow,
+                                                                           clow);
+        RTM_CUDA(cudaGetLastError());
+        k_copy_ch<<<grid_for(P * c[k]), 256, 0, u->st>>>(P, c[k], u->gcat[k].p, cc, clow, gskip, c[k], 0, 0);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    };
+    auto pool_bwd = [&](int k, bf16 *gdst) {
+        const int Ho = u->H >> (k + 1), Wo = u->W >> (k + 1);
+        k_pool_bwd_add<<<grid_for((long long)n * Ho * Wo * c[k]), 256, 0, u->st>>>(n, Ho, Wo, c[k], u->gpool[k].p,
+                                                                                  c[k], gdst, c[k]);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    };
+    TRY(conv_bwd(u, 14, n, true));
+    TRY(conv_bwd(u, 13, n, true));
+    TRY(conv_bwd(u, 12, n, true));
+    TRY(split(0, c[1], u->ga[11].p, u->ga[1].p));
+    TRY(conv_bwd(u, 11, n, true));
+    TRY(conv_bwd(u, 10, n, true));
+    TRY(split(1, c[2], u->ga[9].p, u->ga[3].p));
+    TRY(conv_bwd(u, 9, n, true));
+    TRY(conv_bwd(u, 8, n, true));
+    TRY(split(2, c[3], u->ga[7].p, u->ga[5].p));
+    TRY(conv_bwd(u, 7, n, true));
+    TRY(conv_bwd(u, 6, n, true));
+    TRY(pool_bwd(2, u->ga[5].p));
+    TRY(conv_bwd(u, 5, n, true));
+    TRY(conv_bwd(u, 4, n, true));
+    TRY(pool_bwd(1, u->ga[3].p));
+    TRY(conv_bwd(u, 3, n, true));
+    TRY(conv_bwd(u, 2, n, true));
+    TRY(pool_bwd(0, u->ga[1].p));
+    TRY(conv_bwd(u, 1, n, true));
+    TRY(conv_bwd(u, 0, n, false));
+    return RTM_OK;
+}
+
+int load_input(unet *u, const float *x, int n, int on_device)
+{
+    RTM_CHECK_ARG(n >= 1 && n <= u->nmax, "batch %d outside 1..%d", n, u->nmax);
+    const long long cnt = (long long)n * u->H * u->W * u->cin;
+    const float *src = x;
+    if (!on_device) {
+        RTM_CUDA(cudaMemcpyAsync(u->tgt.p, x, cnt * sizeof(float), cudaMemcpyHostToDevice, u->st));
+        src = u->tgt.p;
+    }
+    k_to_bf16<<<grid_for(cnt), 256, 0, u->st>>>(cnt, src, u->xin.p);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+int loss_and_grad(unet *u, const float *t, int n, int on_device, double *loss)
+{
+    const long long P = (long long)n * u->H * u->W;
+    const float *tp = t;
+    if (!on_device) {
+        RTM_CUDA(cudaMemcpyAsync(u->tgt.p, t, P * u->cout * sizeof(float), cudaMemcpyHostToDevice, u->st));
+        tp = u->tgt.p;
+    }
+    const int blocks = std::min(grid_for(P * 32), 4096);
+    k_mse<<<blocks, 256, 0, u->st>>>(P, u->cout, u->out.p, 8, tp, u->gout.p, 32, u->part.p);
+    RTM_CUDA(cudaGetLastError());
+    std::vector<double> hp(blocks);
+    RTM_CUDA(cudaMemcpyAsync(hp.data(), u->part.p, blocks * sizeof(double), cudaMemcpyDeviceToHost, u->st));
+    RTM_CUDA(cudaStreamSynchronize(u->st));
+    double s = 0;
+    for (double x : hp) s += x;
+    *loss = s / ((double)P * u->cout);
+    return RTM_OK;
+}
+
+}  // namespace
+
+// ================================================================== C-ABI
+extern "C" unet *unet_create(int H, int W, int max_batch, unsigned seed)
+{
+    if (H < 8 || W < 8 || H % 8 || W % 8 || max_batch < 1) {
+        rtm_set_error("unet_create: H, W must be multiples of 8 (got %d x %d), batch >= 1", H, W);
+        return nullptr;
+    }
+    if (eg::ensure_device()) return nullptr;
+    unet *u = new unet();
+    u->H = H;
+    u->W = W;
+    u->nmax = max_batch;
+    if (setup(u) || cudaStreamCreateWithFlags(&u->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete u;
+        return nullptr;
+    }
+    // He-normal initial weights, zero biases (host RNG, then upload)
+    std::vector<float> w(u->nparam, 0.f);
+    std::mt19937 rng(seed);
+    for (int i = 0; i < NCONV; i++) {
+        const Layer &l = u->L[i];
+        const int fan_in = l.ks * l.ks * l.cin;
+        std::normal_distribution<float> nd(0.f, std::sqrt(2.f / fan_in));
+        for (int co = 0; co < l.cout; co++)
+            for (int k = 0; k < l.ks * l.ks * l.cin; k++) w[l.woff + (long long)co * l.kp + k] = nd(rng);
+    }
+    if (cudaMemcpy(u->w.p, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess ||
+        refresh_weights(u) || cudaStreamSynchronize(u->st) != cudaSuccess) {
+        rtm_set_error("unet_create: weight upload failed");
+        delete u;
+        return nullptr;
+    }
+    return u;
+}
+
+extern "C" void unet_destroy(unet *u) { delete u; }
+
+extern "C" long long unet_num_params(const unet *u) { return u ? u->nparam : -1; }
+
+// info[0..8]: ks, cin, cout, coutp, kp, woff, boff, H, W of conv layer i
+extern "C" int unet_layer_info(const unet *u, int i, long long *info)
+{
+    RTM_CHECK_ARG(u && info && i >= 0 && i < NCONV, "unet_layer_info: bad arguments");
+    const Layer &l = u->L[i];
+    const long long v[9] = {l.ks, l.cin, l.cout, l.coutp, l.kp, l.woff, l.boff, l.H, l.W};
+    for (int k = 0; k < 9; k++) info[k] = v[k];
+    return RTM_OK;
+}
+
+extern "C" int unet_get_params(const unet *u, float *w)
+{
+    RTM_CHECK_ARG(u && w, "null argument");
+    RTM_CUDA(cudaMemcpy(w, u->w.p, u->nparam * sizeof(float), cudaMemcpyDeviceToHost));
+    return RTM_OK;
+}
+
+extern "C" int unet_set_params(unet *u, const float *w)
+{
+    RTM_CHECK_ARG(u && w, "null argument");
+    RTM_CUDA(cudaMemcpy(u->w.p, w, u->nparam * sizeof(float), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemset(u->m.p, 0, u->nparam * sizeof(float)));
+    RTM_CUDA(cudaMemset(u->v.p, 0, u->nparam * sizeof(float)));
+    u->step = 0;
+    TRY(refresh_weights(u));
+    RTM_CUDA(cudaStreamSynchronize(u->st));
+    return RTM_OK;
+}
+
+extern "C" int unet_forward(unet *u, const float *x, int n, float *y, int on_device)
+{
+    RTM_CHECK_ARG(u && x && y, "null argument");
+    TRY(eg::ensure_device());
+    TRY(load_input(u, x, n, on_device));
+    TRY(forward(u, n));
+    const long long P = (long long)n * u->H * u->W;
+    float *dst = y;
+    if (!on_device) dst = u->tgt.p;
+    k_take<<<grid_for(P * u->cout), 256, 0, u->st>>>(P, u->cout, u->out.p, 8, dst);
+    RTM_CUDA(cudaGetLastError());
+    if (!on_device)
+        RTM_CUDA(cudaMemcpyAsync(y, u->tgt.p, P * u->cout * sizeof(float), cudaMemcpyDeviceToHost, u->st));
+    RTM_CUDA(cudaStreamSynchronize(u->st));
+    return RTM_OK;
+}
+
+extern "C" int unet_loss_grad(unet *u, const float *x, const float *t, int n, int on_device, double *loss, float *grad)
+{
+    RTM_CHECK_ARG(u && x && t && loss, "null argument");
+    TRY(eg::ensure_device());
+    TRY(load_input(u, x, n, on_device));
+    TRY(forward(u, n));
+    TRY(loss_and_grad(u, t, n, on_device, loss));
+    TRY(backward(u, n));
+    if (grad) RTM_CUDA(cudaMemcpyAsync(grad, u->gw.p, u->nparam * sizeof(float), cudaMemcpyDeviceToHost, u->st));
+    RTM_CUDA(cudaStreamSynchronize(u->st));
+    return RTM_OK;
+}
+
+extern "C" int unet_train_step(unet *u, const float *x, const float *t, int n, int on_device, float lr, float beta1,
+                               float beta2, float eps, double *loss)
+{
+    RTM_CHECK_ARG(u && x && t && loss, "null argument");
+    TRY(eg::ensure_device());
+    TRY(load_input(u, x, n, on_device));
+    TRY(forward(u, n));
+    TRY(loss_and_grad(u, t, n, on_device, loss));
+    TRY(backward(u, n));
+    u->step++;
+    const double bc1 = 1.0 - std::pow((double)beta1, (double)u->step);
+    const double bc2 = 1.0 - std::pow((double)beta2, (double)u->step);
+    // w -= lr * mhat / (sqrt(vhat) + eps)  ==  lr*sqrt(bc2)/bc1 * m / (sqrt(v) + eps*sqrt(bc2))
+    const float lr_t = (float)(lr * std::sqrt(bc2) / bc1), eps_t = (float)(eps * std::sqrt(bc2));
+    k_adam<<<grid_for(u->nparam), 256, 0, u->st>>>(u->nparam, u->w.p, u->gw.p, u->m.p, u->v.p, lr_t, beta1, beta2,
+                                                    eps_t);
+    RTM_CUDA(cudaGetLastError());
+    TRY(refresh_weights(u));
+    RTM_CUDA(cudaStreamSynchronize(u->st));
+    return RTM_OK;
+}

@@ -254,6 +254,34 @@ void rtm_batch_destroy(rtm_batch *b);
 void *rtm_host_alloc(size_t bytes);
 void rtm_host_free(void *p);
 
+/* ------------------------------------------ learned image preconditioner
+ * (no counterpart in the reference).  A 4-level 3->3 channel U-Net
+ * (channels 32/64/96/128, 3x3 convolutions with ReLU, 2x2 average pooling,
+ * nearest upsampling with skip concatenation, 1x1 output convolution;
+ * ~0.9M parameters) with BF16 weights and activations and FP32 accumulation
+ * on the tensor cores, trained with Adam on the mean squared error.  Images
+ * are FP32 NHWC (n, H, W, 3); H and W multiples of 8.  Parameters are one
+ * flat FP32 vector: per layer (15 convolutions in the order e1a e1b e2a e2b
+ * e3a e3b ba bb d3a d3b d2a d2b d1a d1b out) the weights [coutp][kp] with
+ * k = (ky*3+kx)*cin + ci (zero-padded to kp), then the bias [coutp]. */
+typedef struct unet unet;
+unet *unet_create(int H, int W, int max_batch, unsigned seed);
+void unet_destroy(unet *u);
+long long unet_num_params(const unet *u);
+/* info[0..8]: ks, cin, cout, coutp, kp, weight offset, bias offset, H, W */
+int unet_layer_info(const unet *u, int layer, long long *info);
+int unet_get_params(const unet *u, float *w);
+/* also resets the Adam moments and step count */
+int unet_set_params(unet *u, const float *w);
+/* y (n, H, W, 3) = net(x); *_on_device selects device or host pointers */
+int unet_forward(unet *u, const float *x, int n, float *y, int on_device);
+/* loss = mean((net(x) - t)^2) and its gradient (flat, like the parameters;
+ * grad may be null) without updating the weights */
+int unet_loss_grad(unet *u, const float *x, const float *t, int n, int on_device, double *loss, float *grad);
+/* one Adam step (bias-corrected) on the batch; loss before the update */
+int unet_train_step(unet *u, const float *x, const float *t, int n, int on_device, float lr, float beta1, float beta2,
+                    float eps, double *loss);
+
 #ifdef __cplusplus
 }
 #endif
