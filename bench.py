@@ -417,6 +417,116 @@ def run_acoustic3d(args):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- config 3
+CFG3 = dict(nx=256, nz=256, nz_model=200, dx=10.0, dt=1e-3, nt=2000, fp=15.0, abc=40, nsource=250, zsrc=5, zrec=5,
+            pairs=4096, ntest=4, batch=32, lr=1e-3, train_steps=1500, seed=3)
+
+
+def unet_train_flops(table, batch):
+    """Algorithmic FLOPs of one training step: forward, backward-data (all
+    layers but the first) and backward-weights GEMMs of every convolution,
+    2 * pixels * (ks^2 * cin) * cout each."""
+    f = 0.0
+    for i, (ks, ci, co, coutp, kp, woff, boff, H, W) in enumerate(table):
+        one = 2.0 * batch * H * W * ks * ks * ci * co
+        f += one * (3 if i else 2)
+    return f
+
+
+def run_precond(args):
+    """BASELINE configuration 3: the learned preconditioner.  (Reflectivity,
+    migrated image) pairs from the project's Born modelling and migration on
+    256 x 256 windows of the smoothed single-shot background, U-Net training
+    (Adam, batch 32) on the GPU; one step = one training step.  Then the
+    learned migration (migration + network + least-squares scale) is timed
+    against 10-iteration plain LSRTM at their Born data residuals."""
+    import torch
+    from elastic_gb300 import precond as PC
+    c = dict(CFG3)
+    if args.pairs:
+        c["pairs"] = args.pairs
+    if args.nt:
+        c["nt"] = args.nt
+    rho, lam, mu = PC.background_window(c["nx"], c["nz"], nz_model=c["nz_model"])
+    pb = PC.Problem(rho, lam, mu, c["dx"], c["dt"], c["nt"], c["nx"] // 2 + 1, c["zsrc"], c["zrec"], c["fp"], c["abc"],
+                    c["nsource"])
+    rng = np.random.default_rng(c["seed"])
+    ntr, nte = c["pairs"], c["ntest"]
+    t0 = time.perf_counter()
+    r = PC.random_reflectivity(rng, ntr + nte, c["nx"], c["nz"], c["abc"] + 2)
+    img = np.concatenate([pb.normal(r[i:min(ntr, i + 64)] * pb.bg[None]) for i in range(0, ntr, 64)])
+    d_test, _ = pb.born_migrate(r[ntr:] * pb.bg[None])
+    gen_s = time.perf_counter() - t0
+    pc = PC.Preconditioner(c["nx"], c["nz"], batch=c["batch"], seed=0)
+    pc.fit_scales(img)
+    x = torch.from_numpy(pc.inputs(img)).cuda()
+    y = torch.from_numpy(PC.to_nhwc(r[:ntr] * pc.out_scale)).cuda()
+    del img
+    g = torch.Generator().manual_seed(c["seed"])
+
+    def step():
+        idx = torch.randint(0, ntr, (c["batch"],), generator=g).cuda()
+        return pc.net.train_step(x.index_select(0, idx).contiguous(), y.index_select(0, idx).contiguous(), lr=c["lr"])
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        losses = [step() for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+    clocks = clk.summary()
+    # rest of the training budget (untimed)
+    for _ in range(max(0, c["train_steps"] - args.steps - args.warmup)):
+        losses.append(step())
+    # learned migration vs LSRTM-10 on held-out pairs
+    res_nn, res_ls, res_rtm, t_nn, t_ls = [], [], [], [], []
+    for k in range(nte):
+        t0 = time.perf_counter()
+        im = pb.migrate(d_test[k:k + 1])
+        m = pc.apply(im, pb.bg)
+        res_nn.append(float(PC.scaled_residual(pb, m, d_test[k:k + 1])[0]))
+        t_nn.append(time.perf_counter() - t0)
+        res_rtm.append(float(PC.scaled_residual(pb, im, d_test[k:k + 1])[0]))
+        _, resid, tl = pb.lsrtm(d_test[k], 10)
+        res_ls.append(float(resid[-1] / resid[0]))
+        t_ls.append(tl)
+    table = pc.net.layer_table()
+    flops = unet_train_flops(table, c["batch"])
+    tflops = flops * args.steps / train_s / 1e12
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, kind = (json.load(open(pk))["bf16_tflops"], "measured") if os.path.exists(pk) else (1900.0, "fallback")
+    rate = c["batch"] * args.steps / train_s
+    line = {"metric": "training images/s (learned preconditioner)", "value": round(rate, 2), "unit": "images/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * train_s / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"learned preconditioner (BASELINE config 3): 3->3 channel 4-level U-Net, "
+                                   f"{pc.net.nparam} parameters, {c['nx']}x{c['nz']} patches, batch {c['batch']}, "
+                                   f"Adam lr {c['lr']}; {ntr} training pairs (Born-modelled then migrated, one shot, "
+                                   f"Vx/Vz receivers, nt={c['nt']})",
+                       "pair_generation_s": round(gen_s, 1), "train_steps": len(losses) + args.warmup,
+                       "loss_first_last": [round(losses[0], 5), round(float(np.mean(losses[-50:])), 5)],
+                       "inputs_vs_l2": "training set (%.1f GB) larger than L2" % (x.numel() * 8 / 1e9)},
+            "time_to_residual": {"learned_residual": round(float(np.mean(res_nn)), 4),
+                                 "lsrtm10_residual": round(float(np.mean(res_ls)), 4),
+                                 "rtm_residual": round(float(np.mean(res_rtm)), 4),
+                                 "learned_s": round(float(np.mean(t_nn)), 4), "lsrtm10_s": round(float(np.mean(t_ls)), 4),
+                                 "lsrtm10_over_learned_time": round(float(np.mean(t_ls) / np.mean(t_nn)), 2),
+                                 "held_out_pairs": nte,
+                                 "note": "residual = ||L m - d|| / ||d|| on Vx/Vz; learned = migration + network + "
+                                         "least-squares scale (one Born); RTM with its best scale"},
+            "e2e": {"value": round(rate, 2), "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8,
+                    "note": "training batches are gathered on the device from the resident training set; the loss "
+                            "is read back every step"},
+            "gpu_launches": None,
+            "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
+                         "frac": round(tflops / peak, 4), "peak_kind": kind + " bf16 (cuBLAS burst)",
+                         "kernel": "k_gemm (mma.sync m16n8k16 BF16) over the whole training step", "traffic": None},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -426,7 +536,8 @@ def main():
     ap.add_argument("--group", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--tune-steps", type=int, default=20)
-    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "acoustic3d"])
+    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "acoustic3d", "precond"])
+    ap.add_argument("--pairs", type=int, default=None, help="training pairs of the precond workload")
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -441,6 +552,8 @@ def main():
         run_reference(args)
     elif args.workload == "acoustic3d":
         run_acoustic3d(args)
+    elif args.workload == "precond":
+        run_precond(args)
     else:
         run_gpu(args)
 

@@ -41,9 +41,11 @@ SIGNATURES = {
                   + [_P] * 11 + [_c_int, _c_int]),
     "rtm_op_d_": (_c_int, [_c_int] * 4 + [_c_double, _c_double] + [_c_int] * 3 + [_c_double, _c_int, _c_int]
                   + [_P] * 11 + [_c_int, _c_int]),
-    "rtm_lsrtm_c_": (_c_int, [_c_int] * 3 + [_c_float] * 3 + [_c_int] * 3 + [_P, _P, _c_int] + [_P] * 4
+    "rtm_born_migrate_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 3
+                            + [_P] * 3 + [_c_int] + [_P] * 4 + [_c_int]),
+    "rtm_lsrtm_c_": (_c_int, [_c_int] * 3 + [_c_float] * 3 + [_c_int] * 3 + [_P, _P, _c_int, _c_int] + [_P] * 4
                      + [_c_int, _P, _P]),
-    "rtm_lsrtm_d_": (_c_int, [_c_int] * 3 + [_c_double] * 3 + [_c_int] * 3 + [_P, _P, _c_int] + [_P] * 4
+    "rtm_lsrtm_d_": (_c_int, [_c_int] * 3 + [_c_double] * 3 + [_c_int] * 3 + [_P, _P, _c_int, _c_int] + [_P] * 4
                      + [_c_int, _P, _P]),
     "unet_create": (ctypes.c_void_p, [_c_int, _c_int, _c_int, ctypes.c_uint]),
     "unet_destroy": (None, [_P]),

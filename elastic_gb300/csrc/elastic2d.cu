@@ -537,6 +537,7 @@ struct BornShot {
     Hist<T> h;
     DevBuf<T> S;  // source wavefield, 5 histories of nt levels
     int nz = 0, nx = 0, nt = 0, zrec0 = 0;
+    int comp_mask = 31;  // recorded components (bit c: Vx, Vz, sxx, szz, sxz)
     size_t plane = 0, vol = 0;
     T inv_dt = 0, inv_dx = 0;
 
@@ -597,6 +598,15 @@ struct BornShot {
         k_gather_from_rec<T><<<gr, b, 0, h.st>>>(nt, nx, rec, data, data + gs, data + 2 * gs, data + 3 * gs,
                                                  data + 4 * gs);
         RTM_CUDA(cudaGetLastError());
+        // components that are not recorded are zero (L := mask * L)
+        return mask_data(data);
+    }
+    // zero the unrecorded components of device gathers in place
+    int mask_data(T *data)
+    {
+        const size_t gs = gather_size();
+        for (int c = 0; c < 5; c++)
+            if (!(comp_mask & (1 << c))) RTM_CUDA(cudaMemsetAsync(data + c * gs, 0, gs * sizeof(T), h.st));
         return RTM_OK;
     }
 
@@ -762,10 +772,11 @@ struct Vec {
 // L^T is the exact adjoint.  resid[k] = ||d - L m_k|| (k = 0..niter).
 template <typename T>
 int lsrtm_impl(int nz, int nx, int nt, T dx, T dt, T fp, int nsource, int abc, int nshots, const int *xsrc,
-               const int *zsrc, int zrec, const T *rho, const T *lam, const T *mu, const T *data, int niter, T *dm,
-               double *resid, bool exact)
+               const int *zsrc, int zrec, int comp_mask, const T *rho, const T *lam, const T *mu, const T *data,
+               int niter, T *dm, double *resid, bool exact)
 {
     RTM_CHECK_ARG(nshots >= 1 && niter >= 0 && xsrc && zsrc && data && dm, "bad LSRTM arguments");
+    RTM_CHECK_ARG(comp_mask >= 1 && comp_mask <= 31, "comp_mask must select 1 to 5 components");
     TRY(ensure_device());
     const size_t plane = (size_t)nz * nx, nm = 3 * plane, gs = (size_t)nt * nx, nd1 = 5 * gs,
                  nd = nd1 * (size_t)nshots;
@@ -778,6 +789,7 @@ int lsrtm_impl(int nz, int nx, int nt, T dx, T dt, T fp, int nsource, int abc, i
     for (int s = 0; s < nshots; s++) {
         shots.emplace_back(new BornShot<T>());
         TRY(shots.back()->init(nz, nx, nt, dx, dt, xsrc[s], zsrc[s], zrec, fp, nsource, abc, model.p, exact));
+        shots.back()->comp_mask = comp_mask;
     }
     cudaStream_t st = shots[0]->h.st;
     const size_t vol = shots[0]->vol;
@@ -790,6 +802,7 @@ int lsrtm_impl(int nz, int nx, int nt, T dx, T dt, T fp, int nsource, int abc, i
     TRY(r.alloc(nd)); TRY(q.alloc(nd));
     RTM_CUDA(cudaMemsetAsync(x.p, 0, nm * sizeof(T), st));
     RTM_CUDA(cudaMemcpyAsync(r.p, data, nd * sizeof(T), cudaMemcpyHostToDevice, st));
+    for (int s = 0; s < nshots; s++) TRY(shots[s]->mask_data(r.p + (size_t)s * nd1));
     Vec<T> v;
     TRY(v.init(st));
     // L m for all shots (data of shot s at offset s*nd1)
@@ -840,6 +853,60 @@ int lsrtm_impl(int nz, int nx, int nt, T dx, T dt, T fp, int nsource, int abc, i
     return RTM_OK;
 }
 
+// Born modelling and migration of a batch of model perturbations for one
+// shot with the source wavefield computed once: data_k = L dm_k and
+// img_k = L^T data_k (exact adjoint), or img_k = L^T data_in_k.  Every
+// array may be on the device (on_device=1) or the host.
+template <typename T>
+int born_migrate_impl(int nz, int nx, int nt, T dx, T dt, int xsrc, int zsrc, int zrec, T fp, int nsource, int abc,
+                      int comp_mask, const T *rho, const T *lam, const T *mu, int npairs, const T *dm, T *data,
+                      const T *data_in, T *img, int on_device, bool exact)
+{
+    RTM_CHECK_ARG(npairs >= 1, "npairs must be >= 1");
+    RTM_CHECK_ARG(comp_mask >= 1 && comp_mask <= 31, "comp_mask must select 1 to 5 components");
+    RTM_CHECK_ARG(dm || data_in, "need model perturbations or data");
+    RTM_CHECK_ARG(!dm || !data_in, "give model perturbations or data, not both");
+    RTM_CHECK_ARG(data || img, "nothing to compute");
+    TRY(ensure_device());
+    const size_t plane = (size_t)nz * nx;
+    const cudaMemcpyKind h2d = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind d2h = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    DevBuf<T> model;
+    TRY(model.alloc(3 * plane));
+    RTM_CUDA(cudaMemcpy(model.p, rho, plane * sizeof(T), h2d));
+    RTM_CUDA(cudaMemcpy(model.p + plane, lam, plane * sizeof(T), h2d));
+    RTM_CUDA(cudaMemcpy(model.p + 2 * plane, mu, plane * sizeof(T), h2d));
+    BornShot<T> sh;
+    TRY(sh.init(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, model.p, exact));
+    sh.comp_mask = comp_mask;
+    const size_t vol = sh.vol, nd = 5 * sh.gather_size();
+    cudaStream_t st = sh.h.st;
+    DevBuf<T> W, rec, m, d, im;
+    TRY(W.alloc(5 * vol));
+    T *A[5];
+    for (int f = 0; f < 5; f++) A[f] = W.p + f * vol;
+    TRY(rec.alloc((size_t)nt * 5 * nx));
+    TRY(m.alloc(3 * plane));
+    TRY(d.alloc(nd));
+    TRY(im.alloc(3 * plane));
+    for (int k = 0; k < npairs; k++) {
+        if (dm) {
+            RTM_CUDA(cudaMemcpyAsync(m.p, dm + k * 3 * plane, 3 * plane * sizeof(T), h2d, st));
+            TRY(sh.born(m.p, m.p + plane, m.p + 2 * plane, A, rec.p, d.p));
+            if (data) RTM_CUDA(cudaMemcpyAsync(data + k * nd, d.p, nd * sizeof(T), d2h, st));
+        } else {
+            RTM_CUDA(cudaMemcpyAsync(d.p, data_in + k * nd, nd * sizeof(T), h2d, st));
+            TRY(sh.mask_data(d.p));
+        }
+        if (img) {
+            TRY(sh.adjoint(d.p, A, im.p, true));
+            RTM_CUDA(cudaMemcpyAsync(img + k * 3 * plane, im.p, 3 * plane * sizeof(T), d2h, st));
+        }
+    }
+    RTM_CUDA(cudaStreamSynchronize(st));
+    return RTM_OK;
+}
+
 }  // namespace
 
 // ===================================================================== C-ABI
@@ -853,21 +920,31 @@ extern "C" int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, in
                               dlambda, dmu, D, linear, exact_adjoint, g_exact != 0);
 }
 
-extern "C" int rtm_lsrtm_c_(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc, int nshots,
-                            const int *xsrc, const int *zsrc, int zrec, const float *rho, const float *lambda,
-                            const float *mu, const float *data, int niter, float *dm, double *resid)
+extern "C" int rtm_born_migrate_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,
+                                   int nsource, int abc, int comp_mask, const float *rho, const float *lambda,
+                                   const float *mu, int npairs, const float *dm, float *data, const float *data_in,
+                                   float *img, int on_device)
 {
-    return lsrtm_impl<float>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, rho, lambda, mu, data,
-                             niter, dm, resid, g_exact != 0);
+    return born_migrate_impl<float>(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, comp_mask, rho, lambda, mu,
+                                    npairs, dm, data, data_in, img, on_device, g_exact != 0);
+}
+
+extern "C" int rtm_lsrtm_c_(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc, int nshots,
+                            const int *xsrc, const int *zsrc, int zrec, int comp_mask, const float *rho,
+                            const float *lambda, const float *mu, const float *data, int niter, float *dm,
+                            double *resid)
+{
+    return lsrtm_impl<float>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, comp_mask, rho, lambda,
+                             mu, data, niter, dm, resid, g_exact != 0);
 }
 
 extern "C" int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int nsource, int abc,
-                            int nshots, const int *xsrc, const int *zsrc, int zrec, const double *rho,
+                            int nshots, const int *xsrc, const int *zsrc, int zrec, int comp_mask, const double *rho,
                             const double *lambda, const double *mu, const double *data, int niter, double *dm,
                             double *resid)
 {
-    return lsrtm_impl<double>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, rho, lambda, mu, data,
-                              niter, dm, resid, true);
+    return lsrtm_impl<double>(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, xsrc, zsrc, zrec, comp_mask, rho, lambda,
+                              mu, data, niter, dm, resid, true);
 }
 
 extern "C" int rtm_op_d_(int adj, int nz, int nx, int nt, double dx, double dt, int xsrc, int zsrc, int zrec,

@@ -167,7 +167,7 @@ class RtmOperator:
         return 0
 
 
-def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, nsource=250, dtype=F32):
+def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, nsource=250, dtype=F32, comp_mask=31):
     """Least-squares RTM by CGLS on the linear Born operator of ``rtm_op``
     (linear=True) with its exact adjoint, over all shots stacked.
 
@@ -175,7 +175,9 @@ def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, n
     order Vx, Vz, sigmaxx, sigmazz, sigmaxz.  xsrc, zsrc: 1-based source
     positions per shot.  Returns (dm, resid): dm (3, nx, nz) = (drho,
     dlambda, dmu) after niter iterations from zero, resid (niter+1,) the
-    data residual norms ||d - L m_k||.
+    data residual norms ||d - L m_k||.  comp_mask selects the recorded
+    components (bit c: Vx, Vz, sigmaxx, sigmazz, sigmaxz); the others are
+    ignored.
     """
     dtype = np.dtype(dtype)
     rho, lam, mu = (np.ascontiguousarray(a, dtype) for a in (rho, lam, mu))
@@ -191,6 +193,6 @@ def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, n
     dm = np.zeros((3, nx, nz), dtype)
     resid = np.zeros(niter + 1, np.float64)
     fn = load().rtm_lsrtm_d_ if dtype == np.float64 else load().rtm_lsrtm_c_
-    check(fn(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, ptr(xs), ptr(zs), zrec, ptr(rho), ptr(lam), ptr(mu),
-             ptr(data), niter, ptr(dm), ptr(resid)))
+    check(fn(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, ptr(xs), ptr(zs), zrec, comp_mask, ptr(rho), ptr(lam),
+             ptr(mu), ptr(data), niter, ptr(dm), ptr(resid)))
     return dm, resid

@@ -165,13 +165,30 @@ int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, int xsrc, int
  * gathers of rtm_op_c_ (Vx, Vz, sigmaxx, sigmazz, sigmaxz, each (nt,nx)
  * Fortran order), shots consecutive.  dm: three (nz,nx) planes (drho,
  * dlambda, dmu) out.  resid (optional, niter+1 doubles): ||d - L m_k||.
- * Each shot's source history (5 nz*nx*nt volumes) stays on the device. */
+ * comp_mask selects the recorded components as in rtm_born_migrate_c_
+ * (the operator is mask * L).  Each shot's source history (5 nz*nx*nt
+ * volumes) stays on the device. */
 int rtm_lsrtm_c_(int nz, int nx, int nt, float dx, float dt, float fp, int nsource, int abc, int nshots,
-                 const int *xsrc, const int *zsrc, int zrec, const float *rho, const float *lambda, const float *mu,
-                 const float *data, int niter, float *dm, double *resid);
+                 const int *xsrc, const int *zsrc, int zrec, int comp_mask, const float *rho, const float *lambda,
+                 const float *mu, const float *data, int niter, float *dm, double *resid);
 int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int nsource, int abc, int nshots,
-                 const int *xsrc, const int *zsrc, int zrec, const double *rho, const double *lambda,
+                 const int *xsrc, const int *zsrc, int zrec, int comp_mask, const double *rho, const double *lambda,
                  const double *mu, const double *data, int niter, double *dm, double *resid);
+
+/* Born modelling and migration of a batch of npairs model perturbations
+ * for one shot on the full grid, the source wavefield computed once (no
+ * counterpart in the reference; builds the learned preconditioner's
+ * training pairs).  With dm (npairs x 3 planes drho, dlambda, dmu): data_k =
+ * L dm_k (linear Born, written to data when not null) and, when img is not
+ * null, img_k = L^T data_k with the exact adjoint.  With data_in instead of
+ * dm: img_k = L^T data_in_k.  Gathers as in rtm_op_c_ (5 x (nt,nx) per pair).
+ * comp_mask (bit c for Vx, Vz, sigmaxx, sigmazz, sigmaxz; 31 = all) selects
+ * the recorded components: the others are zero in data and ignored in
+ * data_in (the operator is mask * L).  on_device=1: all arrays are device
+ * pointers. */
+int rtm_born_migrate_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,
+                        int nsource, int abc, int comp_mask, const float *rho, const float *lambda, const float *mu,
+                        int npairs, const float *dm, float *data, const float *data_in, float *img, int on_device);
 
 /* Double-precision twin of rtm_op_c_ (used for the FP64 oracle comparison
  * and the adjoint dot-product test). */
