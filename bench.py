@@ -457,7 +457,7 @@ def run_precond(args):
     img = np.concatenate([pb.normal(r[i:min(ntr, i + 64)] * pb.bg[None]) for i in range(0, ntr, 64)])
     d_test, _ = pb.born_migrate(r[ntr:] * pb.bg[None])
     gen_s = time.perf_counter() - t0
-    pc = PC.Preconditioner(c["nx"], c["nz"], batch=c["batch"], seed=0)
+    pc = PC.Preconditioner(c["nx"], c["nz"], batch=c["batch"], seed=0, margin=c["abc"] + 2)
     pc.fit_scales(img)
     x = torch.from_numpy(pc.inputs(img)).cuda()
     y = torch.from_numpy(PC.to_nhwc(r[:ntr] * pc.out_scale)).cuda()
@@ -481,13 +481,15 @@ def run_precond(args):
     for _ in range(max(0, c["train_steps"] - args.steps - args.warmup)):
         losses.append(step())
     # learned migration vs LSRTM-10 on held-out pairs
-    res_nn, res_ls, res_rtm, t_nn, t_ls = [], [], [], [], []
+    res_nn, res_ls, res_rtm, t_nn, t_ls, refl_err = [], [], [], [], [], []
     for k in range(nte):
         t0 = time.perf_counter()
         im = pb.migrate(d_test[k:k + 1])
         m = pc.apply(im, pb.bg)
         res_nn.append(float(PC.scaled_residual(pb, m, d_test[k:k + 1])[0]))
         t_nn.append(time.perf_counter() - t0)
+        rt = r[ntr + k]
+        refl_err.append(float(np.linalg.norm(m[0] / pb.bg - rt) / np.linalg.norm(rt)))
         res_rtm.append(float(PC.scaled_residual(pb, im, d_test[k:k + 1])[0]))
         _, resid, tl = pb.lsrtm(d_test[k], 10)
         res_ls.append(float(resid[-1] / resid[0]))
@@ -514,6 +516,7 @@ def run_precond(args):
                                  "learned_s": round(float(np.mean(t_nn)), 4), "lsrtm10_s": round(float(np.mean(t_ls)), 4),
                                  "lsrtm10_over_learned_time": round(float(np.mean(t_ls) / np.mean(t_nn)), 2),
                                  "held_out_pairs": nte,
+                                 "learned_reflectivity_rel_err": round(float(np.mean(refl_err)), 4),
                                  "note": "residual = ||L m - d|| / ||d|| on Vx/Vz; learned = migration + network + "
                                          "least-squares scale (one Born); RTM with its best scale"},
             "e2e": {"value": round(rate, 2), "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8,

@@ -147,11 +147,15 @@ def from_nhwc(a):
 
 
 class Preconditioner:
-    """U-Net on normalised migrated images -> reflectivity."""
+    """U-Net on normalised migrated images -> reflectivity.  The estimate is
+    kept to the imaging region of the training targets: zero within
+    `margin` cells of the edges (the sponge, where the source sits and the
+    data are most sensitive to any model change)."""
 
-    def __init__(self, nx, nz, batch=32, seed=0):
+    def __init__(self, nx, nz, batch=32, seed=0, margin=0):
         self.net = UNet(nx, nz, batch, seed=seed)
         self.batch = batch
+        self.margin = margin
         self.in_scale = np.ones(3, np.float32)
         self.out_scale = np.float32(10.0)  # reflectivity is O(0.1)
 
@@ -186,6 +190,12 @@ class Preconditioner:
         for i in range(0, img.shape[0], self.batch):
             out.append(from_nhwc(self.net.forward(self.inputs(img[i:i + self.batch]))))
         r = np.concatenate(out) / self.out_scale
+        if self.margin:
+            m = self.margin
+            r[:, :, :m] = 0
+            r[:, :, r.shape[2] - m:] = 0
+            r[:, :, :, :m] = 0
+            r[:, :, :, r.shape[3] - m:] = 0
         return r * bg[None]
 
 

@@ -64,7 +64,7 @@ def test_learned_preconditioner_beats_rtm_and_lsrtm_on_held_out_pairs():
     r = PC.random_reflectivity(rng, ntrain + ntest, NX, NZ, ABC + 2)
     dm = r * pb.bg[None]
     data, img = pb.born_migrate(dm)
-    pc = PC.Preconditioner(NX, NZ, batch=32, seed=0)
+    pc = PC.Preconditioner(NX, NZ, batch=32, seed=0, margin=ABC + 2)
     pc.fit_scales(img[:ntrain])
     losses = pc.train(img[:ntrain], r[:ntrain], steps=1500, lr=1e-3)
     zero_loss = float(np.mean((pc.out_scale * r[:ntrain]) ** 2))
