@@ -418,8 +418,12 @@ def run_acoustic3d(args):
 
 
 # --------------------------------------------------------------- config 3
-CFG3 = dict(nx=256, nz=256, nz_model=200, dx=10.0, dt=1e-3, nt=2000, fp=15.0, abc=40, nsource=250, zsrc=5, zrec=5,
-            pairs=4096, ntest=4, batch=32, lr=1e-3, train_steps=1500, seed=3)
+# The single-shot configuration's 40-cell sponge with source and receivers at
+# 50 m puts the acquisition inside the sponge, where recorded reflections are
+# damped by about 1e-3; the preconditioner study uses a 20-cell sponge with
+# source and receivers just below it.
+CFG3 = dict(nx=256, nz=256, nz_model=200, dx=10.0, dt=1e-3, nt=2000, fp=15.0, abc=20, nsource=250, zsrc=26, zrec=26,
+            pairs=4096, ntest=4, batch=32, lr=1e-3, train_steps=3000, seed=3)
 
 
 def unet_train_flops(table, batch):
@@ -508,6 +512,7 @@ def run_precond(args):
                                    f"Adam lr {c['lr']}; {ntr} training pairs (Born-modelled then migrated, one shot, "
                                    f"Vx/Vz receivers, nt={c['nt']})",
                        "pair_generation_s": round(gen_s, 1), "train_steps": len(losses) + args.warmup,
+                       "input_normalisation": "per channel and depth row RMS over the imaging region, clipped to +-20",
                        "loss_first_last": [round(losses[0], 5), round(float(np.mean(losses[-50:])), 5)],
                        "inputs_vs_l2": "training set (%.1f GB) larger than L2" % (x.numel() * 8 / 1e9)},
             "time_to_residual": {"learned_residual": round(float(np.mean(res_nn)), 4),

@@ -5,7 +5,9 @@
 // (mma.sync m16n8k16 BF16, FP32 accumulators, cp.async 3-stage pipeline)
 // on im2col operands in NHWC layout.
 //
-// Network (channels c = 32, 64, 96, 128; 3x3 convolutions with ReLU):
+// Network (channels c = 32, 64, 96, 128; 3x3 convolutions with leaky ReLU,
+// slope LEAK for negative inputs, which keeps units from dying without any
+// normalisation layer):
 //   e1: 3->32->32    (H)      skip s1
 //   e2: 32->64->64   (H/2)    skip s2    (2x2 average pool between levels)
 //   e3: 64->96->96   (H/4)    skip s3
@@ -47,7 +49,7 @@ struct GemmArgs {
     long long ldb;
     int M, N, K, kchunk;
     const float *bias;  // EPI_BF16 / EPI_F32: per-n bias (or null)
-    int relu;           // EPI_BF16: ReLU after the bias
+    int relu;           // EPI_BF16: leaky ReLU after the bias
     bf16 *Cb;           // EPI_BF16: Cb[m*ldc + coff + n]
     float *Cf;          // EPI_F32: Cf[m*ldc + n]; EPI_F32_ATOMIC_T: Cf[n*ldc + m] += acc
     long long ldc;
@@ -55,6 +57,7 @@ struct GemmArgs {
 };
 
 constexpr int GBM = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
+constexpr float LEAK = 0.1f;  // negative-side slope of the activation
 
 template <bool A_T, bool B_T, int BN>
 struct GemmSmem {
@@ -218,8 +221,8 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
                     if (n + 1 < g.N) g.Cf[(long long)m * g.ldc + n + 1] = v1;
                 } else {
                     if (g.relu) {
-                        v0 = fmaxf(v0, 0.f);
-                        v1 = fmaxf(v1, 0.f);
+                        v0 = v0 > 0.f ? v0 : LEAK * v0;
+                        v1 = v1 > 0.f ? v1 : LEAK * v1;
                     }
                     bf16 *dst = g.Cb + (long long)m * g.ldc + g.coff + n;
                     if (n + 1 < g.N) {
@@ -315,14 +318,16 @@ __global__ void k_im2col3_v8(int n, int H, int W, int C, const bf16 *x, int ldx,
     }
 }
 
-// g *= (y > 0), elementwise over P pixels x C channels (stride ld).
+// g *= (y > 0 ? 1 : LEAK), elementwise over P pixels x C channels (stride
+// ld): the activation's derivative (y > 0 exactly where its input is > 0).
 __global__ void k_relu_mask(long long P, int C, int ld, const bf16 *y, bf16 *g)
 {
     const long long total = P * C;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
         const long long p = i / C;
         const int c = (int)(i - p * C);
-        if (!(__bfloat162float(y[p * ld + c]) > 0.f)) g[p * ld + c] = __float2bfloat16_rn(0.f);
+        if (!(__bfloat162float(y[p * ld + c]) > 0.f))
+            g[p * ld + c] = __float2bfloat16_rn(LEAK * __bfloat162float(g[p * ld + c]));
     }
 }
 

@@ -152,20 +152,54 @@ class Preconditioner:
     `margin` cells of the edges (the sponge, where the source sits and the
     data are most sensitive to any model change)."""
 
-    def __init__(self, nx, nz, batch=32, seed=0, margin=0):
+    def __init__(self, nx, nz, batch=32, seed=0, margin=0, mask_input=True):
         self.net = UNet(nx, nz, batch, seed=seed)
         self.batch = batch
         self.margin = margin
-        self.in_scale = np.ones(3, np.float32)
+        self.mask_input = mask_input
+        self.in_scale = np.ones((3, 1), np.float32)
+        self.clip = 0.0
         self.out_scale = np.float32(10.0)  # reflectivity is O(0.1)
 
-    def fit_scales(self, img):
-        """Per-channel RMS of the training images (n, 3, nx, nz)."""
-        rms = np.sqrt(np.mean(np.asarray(img, np.float64) ** 2, axis=(0, 2, 3)))
+    def fit_scales(self, img, mode="depth", clip=20.0):
+        """Input normalisation from the training images (n, 3, nx, nz).
+        mode "channel": one RMS per channel; "interior": one RMS per channel
+        over the imaging region (outside `margin`); "depth": one RMS per
+        channel and depth row over the imaging region's columns (a gain that
+        compensates the decay of illumination with depth).  clip > 0 clips
+        the normalised image to [-clip, clip] (the strong image next to the
+        source)."""
+        a = np.asarray(img, np.float64)
+        m = self.margin
+        inner = a[:, :, m:a.shape[2] - m, :] if m else a
+        if mode == "channel":
+            rms = np.sqrt(np.mean(a ** 2, axis=(0, 2, 3)))[:, None]
+        elif mode == "interior":
+            rms = np.sqrt(np.mean(inner[:, :, :, m:a.shape[3] - m] ** 2, axis=(0, 2, 3)))[:, None]
+        elif mode == "depth":
+            rms = np.sqrt(np.mean(inner ** 2, axis=(0, 2)))  # (3, nz)
+            rms = np.maximum(rms, 1e-3 * rms.max(axis=1, keepdims=True))
+        else:
+            raise ValueError(mode)
         self.in_scale = (1.0 / np.maximum(rms, 1e-30)).astype(np.float32)
+        self.clip = clip
 
     def inputs(self, img):
-        return to_nhwc(img * self.in_scale[None, :, None, None])
+        """Normalised network input; with mask_input, zero outside the
+        imaging region (the image next to the source and in the sponge
+        carries no information on the targets, which are zero there)."""
+        s = self.in_scale
+        x = img * s[None, :, None, :]
+        if self.clip:
+            x = np.clip(x, -self.clip, self.clip)
+        if self.mask_input and self.margin:
+            m = self.margin
+            x = x.copy()
+            x[:, :, :m] = 0
+            x[:, :, x.shape[2] - m:] = 0
+            x[:, :, :, :m] = 0
+            x[:, :, :, x.shape[3] - m:] = 0
+        return to_nhwc(x)
 
     def train(self, img, refl, steps, lr=1e-3, seed=0, log_every=0):
         """Adam on random batches of (image, reflectivity) pairs held on the

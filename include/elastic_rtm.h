@@ -273,7 +273,7 @@ void rtm_host_free(void *p);
 
 /* ------------------------------------------ learned image preconditioner
  * (no counterpart in the reference).  A 4-level 3->3 channel U-Net
- * (channels 32/64/96/128, 3x3 convolutions with ReLU, 2x2 average pooling,
+ * (channels 32/64/96/128, 3x3 convolutions with leaky ReLU (slope 0.1), 2x2 average pooling,
  * nearest upsampling with skip concatenation, 1x1 output convolution;
  * ~0.9M parameters) with BF16 weights and activations and FP32 accumulation
  * on the tensor cores, trained with Adam on the mean squared error.  Images

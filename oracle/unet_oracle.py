@@ -15,6 +15,7 @@ tests.  Layout conventions (shared with the CUDA code):
 import numpy as np
 
 CH = (32, 64, 96, 128)
+LEAK = 0.1  # negative-side slope of the leaky ReLU
 
 
 def layer_table(H, W, cin=3, cout=3, ch=CH):
@@ -100,7 +101,7 @@ def forward(params, x, table):
         cols = im2col3(inp) if ks == 3 else inp.reshape(-1, C)
         z = cols @ Wk.T + b
         cache[i] = (inp, cols)
-        y = np.maximum(z, 0.0) if i != 14 else z
+        y = np.where(z > 0, z, LEAK * z) if i != 14 else z
         return y.reshape(n, H, W, -1)
 
     a[0] = conv(0, np.asarray(x, np.float64))
@@ -138,7 +139,7 @@ def loss_grad(params, x, t, table):
         ks, ci, co, coutp, kp, woff, boff, H, W = table[i]
         g = gy.reshape(-1, co)
         if i != 14:
-            g = g * (y.reshape(-1, co) > 0)
+            g = g * np.where(y.reshape(-1, co) > 0, 1.0, LEAK)
         inp, cols = cache[i]
         dW = g.T @ cols
         full = np.zeros((coutp, kp))

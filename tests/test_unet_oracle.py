@@ -20,7 +20,7 @@ def torch_net(params, x, t, table):
         ks, ci, co = table[i][0], table[i][1], table[i][2]
         k = W.reshape(co, ks, ks, ci).permute(0, 3, 1, 2)  # (co, ci, ky, kx)
         y = F.conv2d(inp, k, b, padding=ks // 2)
-        return F.relu(y) if i != 14 else y
+        return F.leaky_relu(y, U.LEAK) if i != 14 else y
 
     up = lambda z: F.interpolate(z, scale_factor=2, mode="nearest")
     pool = lambda z: F.avg_pool2d(z, 2)
