@@ -320,18 +320,22 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
         }
         __syncthreads();
         if (ADJ && !EXACT) {
-            // products coef*field in place (slots 0..6 of the 10 raw arrays)
-            for (int e = threadIdx.x; e < SZ; e += blockDim.x) {
-                float fv[5], cv[5];
+            // products coef*field in place (slots 0..6 of the 10 raw arrays),
+            // four elements per 128-bit shared access
+            float4 *s4 = reinterpret_cast<float4 *>(sm);
+            constexpr int SZ4 = SZ / 4;
+            auto mul4 = [](float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); };
+            for (int e = threadIdx.x; e < SZ4; e += blockDim.x) {
+                float4 fv[5], cv[5];
 #pragma unroll
-                for (int f = 0; f < 5; f++) { fv[f] = sm[f * SZ + e]; cv[f] = sm[(5 + f) * SZ + e]; }
-                sm[P_A23XX * SZ + e] = cv[A23] * fv[SXX];
-                sm[P_A2ZZ * SZ + e] = cv[A2] * fv[SZZ];
-                sm[P_A3XZ * SZ + e] = cv[A3] * fv[SXZ];
-                sm[P_A2XX * SZ + e] = cv[A2] * fv[SXX];
-                sm[P_A23ZZ * SZ + e] = cv[A23] * fv[SZZ];
-                sm[P_M1XVX * SZ + e] = cv[M1X] * fv[VX];
-                sm[P_M1ZVZ * SZ + e] = cv[M1Z] * fv[VZ];
+                for (int f = 0; f < 5; f++) { fv[f] = s4[f * SZ4 + e]; cv[f] = s4[(5 + f) * SZ4 + e]; }
+                s4[P_A23XX * SZ4 + e] = mul4(cv[A23], fv[SXX]);
+                s4[P_A2ZZ * SZ4 + e] = mul4(cv[A2], fv[SZZ]);
+                s4[P_A3XZ * SZ4 + e] = mul4(cv[A3], fv[SXZ]);
+                s4[P_A2XX * SZ4 + e] = mul4(cv[A2], fv[SXX]);
+                s4[P_A23ZZ * SZ4 + e] = mul4(cv[A23], fv[SZZ]);
+                s4[P_M1XVX * SZ4 + e] = mul4(cv[M1X], fv[VX]);
+                s4[P_M1ZVZ * SZ4 + e] = mul4(cv[M1Z], fv[VZ]);
             }
             __syncthreads();
         }
