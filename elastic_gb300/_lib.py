@@ -41,6 +41,7 @@ SIGNATURES = {
                   + [_P] * 11 + [_c_int, _c_int]),
     "rtm_op_d_": (_c_int, [_c_int] * 4 + [_c_double, _c_double] + [_c_int] * 3 + [_c_double, _c_int, _c_int]
                   + [_P] * 11 + [_c_int, _c_int]),
+    "rtm_model_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 2 + [_P] * 8),
     "rtm_born_migrate_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 3
                             + [_P] * 3 + [_c_int] + [_P] * 4 + [_c_int]),
     "rtm_lsrtm_c_": (_c_int, [_c_int] * 3 + [_c_float] * 3 + [_c_int] * 3 + [_P, _P, _c_int, _c_int] + [_P] * 4

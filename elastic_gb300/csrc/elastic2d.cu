@@ -434,6 +434,40 @@ struct Hist {
         return tb.build(tb.tx, tb.tz);
     }
 
+    // Nonlinear forward modelling (W/elastic-mod.f90:95-240, the same time
+    // loop as the source wavefield): two rolling levels per field in B[f]
+    // (2 planes each; level L in plane L & 1, written over level L-2 in
+    // place) and the five components of row zrec0 of every level recorded
+    // into rec ([it][5][nx], level 1 zero).
+    int model(T *const B[5], const std::vector<T> &dtsrc, int zsrc0, int xsrc0, int zrec0, T *rec)
+    {
+        for (int f = 0; f < 5; f++) RTM_CUDA(cudaMemsetAsync(B[f], 0, 2 * plane * sizeof(T), st));
+        RTM_CUDA(cudaMemsetAsync(rec, 0, (size_t)nt * 5 * nx * sizeof(T), st));
+        tab.shots[0].src_iz = zsrc0;
+        tab.shots[0].src_ix = xsrc0;
+        tab.shots[0].rec_iz = zrec0;
+        tab.shots[0].doff = 0;
+        TRY(tab.build(tab.tx, tab.tz));
+        for (int L = 2; L <= nt; L++) {
+            Step2DArgs<T> a = args();
+            for (int f = 0; f < 5; f++) {
+                a.out[f] = B[f] + (L & 1) * plane;
+                a.own2[f] = L >= 3 ? a.out[f] : zero.p;
+                a.nb[f] = B[f] + ((L - 1) & 1) * plane;
+            }
+            a.sponge = L >= 3;
+            a.has_src = 1;
+            a.srcval = dtsrc[L - 2];
+            a.rec = rec;
+            a.comp_mask = 31;
+            a.ncomp = 5;
+            a.it = L - 1;
+            TRY(step(a, false));
+        }
+        tab.shots[0].src_iz = tab.shots[0].src_ix = tab.shots[0].rec_iz = -1;
+        return tab.build(tab.tx, tab.tz);
+    }
+
     // Born scattered loop (W/rtm-mod-adj.f90:291-357) on histories already
     // holding the secondary sources; records five gathers at zrec0 into
     // rec ([it][5][nx] device) when rec != null.
@@ -907,6 +941,49 @@ int born_migrate_impl(int nz, int nx, int nt, T dx, T dt, int xsrc, int zsrc, in
     return RTM_OK;
 }
 
+// Nonlinear elastic modelling of one shot (W/elastic-mod.f90:95-240):
+// gathers of the five components at row zrec (Fortran (nt,nx) each).
+template <typename T>
+int model_impl(int nz, int nx, int nt, T dx, T dt, int xsrc, int zsrc, int zrec, T fp, int nsource, int abc,
+               const T *rho, const T *lam, const T *mu, T *const D[5], bool exact)
+{
+    RTM_CHECK_ARG(nz >= 11 && nx >= 11 && nt >= 3, "grid too small (nz=%d nx=%d nt=%d)", nz, nx, nt);
+    RTM_CHECK_ARG(zsrc >= 1 && zsrc <= nz && xsrc >= 1 && xsrc <= nx && zrec >= 1 && zrec <= nz,
+                  "source/receiver position outside the grid");
+    for (int c = 0; c < 5; c++) RTM_CHECK_ARG(D[c], "null gather pointer");
+    TRY(ensure_device());
+    Hist<T> h;
+    TRY(h.init(nz, nx, nt, exact));
+    TRY(h.set_abc(abc));
+    const size_t plane = h.plane, gs = (size_t)nt * nx;
+    DevBuf<T> model, raw, B, rec, g;
+    TRY(model.alloc(3 * plane));
+    RTM_CUDA(cudaMemcpy(model.p, rho, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + plane, lam, plane * sizeof(T), cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(model.p + 2 * plane, mu, plane * sizeof(T), cudaMemcpyHostToDevice));
+    TRY(raw.alloc(5 * plane));
+    T *r[5];
+    for (int i = 0; i < 5; i++) r[i] = raw.p + i * plane;
+    TRY(model_coefs<T>(nz, nx, dx, dt, model.p, model.p + plane, model.p + 2 * plane, nz, r[M1X], r[M1Z], nullptr,
+                       nullptr, r[A2], r[A3], r[A23], nz, h.st));
+    TRY(h.set_coefs_dev(r));
+    std::vector<T> src(nt), dtsrc(nt);
+    host_ricker<T>(nt, dt, fp, nsource, src.data());
+    for (int i = 0; i < nt; i++) dtsrc[i] = dt * src[i];
+    TRY(B.alloc(10 * plane));
+    T *Bp[5];
+    for (int f = 0; f < 5; f++) Bp[f] = B.p + 2 * f * plane;
+    TRY(rec.alloc((size_t)nt * 5 * nx));
+    TRY(h.model(Bp, dtsrc, zsrc - 1, xsrc - 1, zrec - 1, rec.p));
+    TRY(g.alloc(5 * gs));
+    dim3 b(128), gr(ceil_div(nt, 128), nx);
+    k_gather_from_rec<T><<<gr, b, 0, h.st>>>(nt, nx, rec.p, g.p, g.p + gs, g.p + 2 * gs, g.p + 3 * gs, g.p + 4 * gs);
+    RTM_CUDA(cudaGetLastError());
+    for (int c = 0; c < 5; c++) RTM_CUDA(cudaMemcpyAsync(D[c], g.p + c * gs, gs * sizeof(T), cudaMemcpyDeviceToHost, h.st));
+    RTM_CUDA(cudaStreamSynchronize(h.st));
+    return RTM_OK;
+}
+
 }  // namespace
 
 // ===================================================================== C-ABI
@@ -918,6 +995,14 @@ extern "C" int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, in
     float *D[5] = {Vx, Vz, sigmaxx, sigmazz, sigmaxz};
     return rtm_op_impl<float>(adj, nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, rho, lambda, mu, drho,
                               dlambda, dmu, D, linear, exact_adjoint, g_exact != 0);
+}
+
+extern "C" int rtm_model_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,
+                            int nsource, int abc, const float *rho, const float *lambda, const float *mu, float *Vx_rec,
+                            float *Vz_rec, float *sigmaxx_rec, float *sigmazz_rec, float *sigmaxz_rec)
+{
+    float *D[5] = {Vx_rec, Vz_rec, sigmaxx_rec, sigmazz_rec, sigmaxz_rec};
+    return model_impl<float>(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, rho, lambda, mu, D, g_exact != 0);
 }
 
 extern "C" int rtm_born_migrate_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,

@@ -196,3 +196,16 @@ def lsrtm(rho, lam, mu, data, xsrc, zsrc, zrec, dx, dt, nt, fp, abc, niter=10, n
     check(fn(nz, nx, nt, dx, dt, fp, nsource, abc, nshots, ptr(xs), ptr(zs), zrec, comp_mask, ptr(rho), ptr(lam),
              ptr(mu), ptr(data), niter, ptr(dm), ptr(resid)))
     return dm, resid
+
+
+def model(rho, lam, mu, dx, dt, nt, xsrc, zsrc, zrec, fp, abc, nsource=250):
+    """Nonlinear elastic modelling of one shot (elastic.x of the reference):
+    returns the five receiver gathers (Vx, Vz, sigmaxx, sigmazz, sigmaxz),
+    each (nx, nt) -- the C view of Fortran (nt, nx).  1-based positions;
+    rho, lam, mu are (nx, nz) float32."""
+    rho, lam, mu = (np.ascontiguousarray(a, F32) for a in (rho, lam, mu))
+    nx, nz = rho.shape
+    D = [np.zeros((nx, nt), F32) for _ in range(5)]
+    check(load().rtm_model_c_(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, ptr(rho), ptr(lam), ptr(mu),
+                              *[ptr(d) for d in D]))
+    return D

@@ -175,6 +175,16 @@ int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int ns
                  const int *xsrc, const int *zsrc, int zrec, int comp_mask, const double *rho, const double *lambda,
                  const double *mu, const double *data, int niter, double *dm, double *resid);
 
+/* Nonlinear elastic forward modelling of one shot (W/elastic-mod.f90:95-240,
+ * the driver of elastic.x): the forward time loop of rtm_op on the raw
+ * model (rho, lambda, mu), keeping two levels per field instead of the
+ * reference's full histories, with the five receiver gathers at row zrec
+ * (each (nt,nx) Fortran order, as W/elastic-mod.f90:226-234 samples them).
+ * 1-based positions. */
+int rtm_model_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp, int nsource,
+                 int abc, const float *rho, const float *lambda, const float *mu, float *Vx_rec, float *Vz_rec,
+                 float *sigmaxx_rec, float *sigmazz_rec, float *sigmaxz_rec);
+
 /* Born modelling and migration of a batch of npairs model perturbations
  * for one shot on the full grid, the source wavefield computed once (no
  * counterpart in the reference; builds the learned preconditioner's
