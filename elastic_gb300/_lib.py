@@ -41,6 +41,10 @@ SIGNATURES = {
                   + [_P] * 11 + [_c_int, _c_int]),
     "rtm_op_d_": (_c_int, [_c_int] * 4 + [_c_double, _c_double] + [_c_int] * 3 + [_c_double, _c_int, _c_int]
                   + [_P] * 11 + [_c_int, _c_int]),
+    "rtm_velocity_jacobian_c_": (_c_int, [_c_int] * 3 + [_P] * 9),
+    "rtm_velocity_jacobian_d_": (_c_int, [_c_int] * 3 + [_P] * 9),
+    "rtm_velocity_model_c_": (_c_int, [_c_int] * 2 + [_P] * 5),
+    "rtm_velocity_model_d_": (_c_int, [_c_int] * 2 + [_P] * 5),
     "rtm_model_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 2 + [_P] * 8),
     "rtm_born_migrate_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 3
                             + [_P] * 3 + [_c_int] + [_P] * 4 + [_c_int]),

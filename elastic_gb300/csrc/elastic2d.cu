@@ -984,6 +984,74 @@ int model_impl(int nz, int nx, int nt, T dx, T dt, int xsrc, int zsrc, int zrec,
     return RTM_OK;
 }
 
+// Velocity parameterisation (lame=.false., W/image-mod-rtm.f90:182-225).
+// With lambda = rho (vp^2 - 2 vs^2) and mu = rho vs^2, the reference's
+// velocity imaging condition is, cell by cell, the transpose J^T of the
+// Jacobian d(rho, lambda, mu)/d(rho, vp, vs) applied to the Lame images, and
+// its Born sources are those of the Lame perturbation J (drho, dvp, dvs).
+// adj=1: (drho, dlambda, dmu) images -> (drho, dvp, dvs) images;
+// adj=0: (drho, dvp, dvs) -> (drho, dlambda, dmu) perturbations.
+template <typename T>
+__global__ void k_vel_jacobian(long long n, int adj, const T *rho, const T *vp, const T *vs, const T *a, const T *b,
+                               const T *c, T *o1, T *o2, T *o3)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const T r = rho[i], p = vp[i], q = vs[i];
+        const T p2 = p * p, q2 = q * q, l2 = p2 - T(2) * q2;
+        const T x = a[i], y = b[i], z = c[i];
+        if (adj) {
+            o1[i] = x + l2 * y + q2 * z;
+            o2[i] = T(2) * r * p * y;
+            o3[i] = T(2) * r * q * z - T(4) * r * q * y;
+        } else {
+            o1[i] = x;
+            o2[i] = l2 * x + T(2) * r * p * y - T(4) * r * q * z;
+            o3[i] = q2 * x + T(2) * r * q * z;
+        }
+    }
+}
+// lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2
+template <typename T>
+__global__ void k_vel_model(long long n, const T *rho, const T *vp, const T *vs, T *lam, T *mu)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const T r = rho[i], p = vp[i], q = vs[i];
+        lam[i] = r * (p * p - T(2) * q * q);
+        mu[i] = r * q * q;
+    }
+}
+
+template <typename T>
+int velocity_impl(int mode, int nz, int nx, const T *rho, const T *vp, const T *vs, const T *i1, const T *i2,
+                  const T *i3, T *o1, T *o2, T *o3)
+{
+    RTM_CHECK_ARG(nz >= 1 && nx >= 1 && rho && vp && vs && o1 && o2, "bad velocity-parameterisation arguments");
+    TRY(ensure_device());
+    const long long n = (long long)nz * nx;
+    DevBuf<T> buf;
+    TRY(buf.alloc(9 * (size_t)n));
+    T *d[9];
+    for (int k = 0; k < 9; k++) d[k] = buf.p + k * n;
+    const T *src[6] = {rho, vp, vs, i1, i2, i3};
+    const int nin = mode == 2 ? 3 : 6;
+    for (int k = 0; k < nin; k++) {
+        RTM_CHECK_ARG(src[k], "null input");
+        RTM_CUDA(cudaMemcpy(d[k], src[k], n * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    const int grid = (int)std::min<long long>((n + 255) / 256, 4096);
+    if (mode == 2) {
+        k_vel_model<T><<<grid, 256>>>(n, d[0], d[1], d[2], d[6], d[7]);
+    } else {
+        RTM_CHECK_ARG(o3, "null output");
+        k_vel_jacobian<T><<<grid, 256>>>(n, mode, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]);
+    }
+    RTM_CUDA(cudaGetLastError());
+    T *outs[3] = {o1, o2, o3};
+    for (int k = 0; k < (mode == 2 ? 2 : 3); k++)
+        RTM_CUDA(cudaMemcpy(outs[k], d[6 + k], n * sizeof(T), cudaMemcpyDeviceToHost));
+    return RTM_OK;
+}
+
 }  // namespace
 
 // ===================================================================== C-ABI
@@ -995,6 +1063,34 @@ extern "C" int rtm_op_c_(int adj, int nz, int nx, int nt, float dx, float dt, in
     float *D[5] = {Vx, Vz, sigmaxx, sigmazz, sigmaxz};
     return rtm_op_impl<float>(adj, nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, rho, lambda, mu, drho,
                               dlambda, dmu, D, linear, exact_adjoint, g_exact != 0);
+}
+
+extern "C" int rtm_velocity_jacobian_c_(int adj, int nz, int nx, const float *rho, const float *vp, const float *vs,
+                                        const float *in1, const float *in2, const float *in3, float *out1, float *out2,
+                                        float *out3)
+{
+    RTM_CHECK_ARG(adj == 0 || adj == 1, "adj must be 0 or 1");
+    return velocity_impl<float>(adj, nz, nx, rho, vp, vs, in1, in2, in3, out1, out2, out3);
+}
+
+extern "C" int rtm_velocity_jacobian_d_(int adj, int nz, int nx, const double *rho, const double *vp,
+                                        const double *vs, const double *in1, const double *in2, const double *in3,
+                                        double *out1, double *out2, double *out3)
+{
+    RTM_CHECK_ARG(adj == 0 || adj == 1, "adj must be 0 or 1");
+    return velocity_impl<double>(adj, nz, nx, rho, vp, vs, in1, in2, in3, out1, out2, out3);
+}
+
+extern "C" int rtm_velocity_model_c_(int nz, int nx, const float *rho, const float *vp, const float *vs,
+                                     float *lambda, float *mu)
+{
+    return velocity_impl<float>(2, nz, nx, rho, vp, vs, nullptr, nullptr, nullptr, lambda, mu, nullptr);
+}
+
+extern "C" int rtm_velocity_model_d_(int nz, int nx, const double *rho, const double *vp, const double *vs,
+                                     double *lambda, double *mu)
+{
+    return velocity_impl<double>(2, nz, nx, rho, vp, vs, nullptr, nullptr, nullptr, lambda, mu, nullptr);
 }
 
 extern "C" int rtm_model_c_(int nz, int nx, int nt, float dx, float dt, int xsrc, int zsrc, int zrec, float fp,

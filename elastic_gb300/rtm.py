@@ -144,18 +144,46 @@ class RtmOperator:
     """
 
     def __init__(self, nz, dz, nx, dx, dt, xsource, zsource, zrec, fp, nt, abc, rho, lam, mu, nsource=250,
-                 dtype=F32, linear=False, exact_adjoint=False):
+                 dtype=F32, linear=False, exact_adjoint=False, lame=True):
+        """With lame=False the model is (rho, vp, vs) in place of (rho,
+        lambda, mu) and the images / perturbations are (drho, dvp, dvs)
+        (W/image-mod-rtm.f90:182-225); lambda and mu are derived from the
+        velocities."""
         self.nz, self.nx, self.nt = nz, nx, nt
         self.dz, self.dx, self.dt = dz, dx, dt
         self.xsource, self.zsource, self.zrec = xsource, zsource, zrec
         self.fp, self.abc, self.nsource = fp, abc, nsource
         self.dtype = np.dtype(dtype)
+        self.lame = lame
         self.rho = np.ascontiguousarray(rho, self.dtype)
-        self.lam = np.ascontiguousarray(lam, self.dtype)
-        self.mu = np.ascontiguousarray(mu, self.dtype)
+        if lame:
+            self.lam = np.ascontiguousarray(lam, self.dtype)
+            self.mu = np.ascontiguousarray(mu, self.dtype)
+        else:
+            self.vp = np.ascontiguousarray(lam, self.dtype)
+            self.vs = np.ascontiguousarray(mu, self.dtype)
+            self.lam, self.mu = velocity_model(self.rho, self.vp, self.vs)
         self.linear, self.exact_adjoint = linear, exact_adjoint
 
     def rtm_op(self, adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz):
+        if not self.lame:
+            return self._rtm_op_velocity(adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz)
+        return self._rtm_op_lame(adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz)
+
+    def _rtm_op_velocity(self, adj, drho, dvp, dvs, *gathers):
+        if adj:
+            im = [np.zeros_like(drho) for _ in range(3)]
+            self._rtm_op_lame(True, *im, *gathers)
+            out = velocity_jacobian(True, self.rho, self.vp, self.vs, *im)
+        else:
+            dl = velocity_jacobian(False, self.rho, self.vp, self.vs, drho, dvp, dvs)
+            self._rtm_op_lame(False, *dl, *gathers)
+            return 0
+        for dst, src in zip((drho, dvp, dvs), out):
+            dst[...] = src
+        return 0
+
+    def _rtm_op_lame(self, adj, drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz):
         arrs = [drho, dlambda, dmu, Vx, Vz, sigmaxx, sigmazz, sigmaxz]
         for a in arrs:
             if a.dtype != self.dtype or not a.flags["C_CONTIGUOUS"]:
@@ -209,3 +237,27 @@ def model(rho, lam, mu, dx, dt, nt, xsrc, zsrc, zrec, fp, abc, nsource=250):
     check(load().rtm_model_c_(nz, nx, nt, dx, dt, xsrc, zsrc, zrec, fp, nsource, abc, ptr(rho), ptr(lam), ptr(mu),
                               *[ptr(d) for d in D]))
     return D
+
+
+def velocity_model(rho, vp, vs):
+    """lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2 on the GPU; (nx, nz)
+    planes, float32 or float64."""
+    d = np.asarray(rho).dtype if np.asarray(rho).dtype == np.float64 else F32
+    rho, vp, vs = (np.ascontiguousarray(a, d) for a in (rho, vp, vs))
+    nx, nz = rho.shape
+    lam, mu = np.zeros_like(rho), np.zeros_like(rho)
+    fn = load().rtm_velocity_model_d_ if d == np.float64 else load().rtm_velocity_model_c_
+    check(fn(nz, nx, ptr(rho), ptr(vp), ptr(vs), ptr(lam), ptr(mu)))
+    return lam, mu
+
+
+def velocity_jacobian(adj, rho, vp, vs, a, b, c):
+    """adj=True: Lame images (drho, dlambda, dmu) -> velocity images (drho,
+    dvp, dvs); adj=False: velocity perturbations -> Lame perturbations."""
+    d = np.asarray(rho).dtype if np.asarray(rho).dtype == np.float64 else F32
+    ins = [np.ascontiguousarray(x, d) for x in (rho, vp, vs, a, b, c)]
+    nx, nz = ins[0].shape
+    out = [np.zeros_like(ins[0]) for _ in range(3)]
+    fn = load().rtm_velocity_jacobian_d_ if d == np.float64 else load().rtm_velocity_jacobian_c_
+    check(fn(1 if adj else 0, nz, nx, *[ptr(x) for x in ins], *[ptr(o) for o in out]))
+    return out

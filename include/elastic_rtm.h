@@ -175,6 +175,26 @@ int rtm_lsrtm_d_(int nz, int nx, int nt, double dx, double dt, double fp, int ns
                  const int *xsrc, const int *zsrc, int zrec, int comp_mask, const double *rho, const double *lambda,
                  const double *mu, const double *data, int niter, double *dm, double *resid);
 
+/* Velocity parameterisation (lame=.false., W/image-mod-rtm.f90:182-225; its
+ * initialisation is commented out in W/rtmlib-mod.f90:59-63, so the
+ * background Lame parameters are computed from the velocities here).
+ * rtm_velocity_model_*: lambda = rho (vp^2 - 2 vs^2), mu = rho vs^2.
+ * rtm_velocity_jacobian_*: adj=1 maps the Lame images (drho, dlambda, dmu)
+ * of rtm_op_c_ to the velocity images (drho, dvp, dvs) -- the reference's
+ * velocity imaging condition, cell by cell the transpose of the Jacobian of
+ * (rho, lambda, mu) with respect to (rho, vp, vs); adj=0 maps velocity
+ * perturbations to the Lame perturbations whose Born sources the reference's
+ * velocity branch injects.  All planes (nz,nx), host arrays. */
+int rtm_velocity_model_c_(int nz, int nx, const float *rho, const float *vp, const float *vs, float *lambda, float *mu);
+int rtm_velocity_model_d_(int nz, int nx, const double *rho, const double *vp, const double *vs, double *lambda,
+                          double *mu);
+int rtm_velocity_jacobian_c_(int adj, int nz, int nx, const float *rho, const float *vp, const float *vs,
+                             const float *in1, const float *in2, const float *in3, float *out1, float *out2,
+                             float *out3);
+int rtm_velocity_jacobian_d_(int adj, int nz, int nx, const double *rho, const double *vp, const double *vs,
+                             const double *in1, const double *in2, const double *in3, double *out1, double *out2,
+                             double *out3);
+
 /* Nonlinear elastic forward modelling of one shot (W/elastic-mod.f90:95-240,
  * the driver of elastic.x): the forward time loop of rtm_op on the raw
  * model (rho, lambda, mu), keeping two levels per field instead of the
