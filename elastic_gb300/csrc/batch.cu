@@ -20,6 +20,7 @@
 // same image as the single-shot pipeline on its subgrid (up to the FP16
 // snapshot rounding and the summation order of the imaging condition).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -109,6 +110,13 @@ struct rtm_batch {
     long long cap_cols = 0, gplane = 0;
     DevBuf<float> model, coefraw, coef, F, A, zero, img, filt, maxes, traces, tstage, full;
     DevBuf<__half> snaps;
+    // Checkpoint-restart: ckpt = 0 keeps the FP16 snapshots of every level;
+    // ckpt = k keeps the full forward state (two levels of the five fields)
+    // at the start of every k-level segment in `ck`, and a ring of k + 1
+    // snapshot levels that the adjoint pass refills by recomputing each
+    // segment from its checkpoint before migrating through it.
+    int ckpt = 0;
+    DevBuf<float> ck;
     DevBuf<int> dx0;
     ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
     ShotTable tab_a;  // adjoint pass work items
@@ -242,7 +250,11 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         RTM_CUDA(cudaGetLastError());
         return RTM_OK;
     };
-    auto snap = [&](int L, int f) { return b->snaps.p + ((size_t)(L - 1) * 2 + f) * gp; };  // level L (1-based)
+    // snapshot slot of level L (1-based): its own level, or a ring slot
+    auto snap = [&](int L, int f) {
+        const size_t slot = b->ckpt ? (size_t)(L % (b->ckpt + 1)) : (size_t)(L - 1);
+        return b->snaps.p + (slot * 2 + f) * gp;
+    };
     auto mx = [&](int L) { return b->maxes.p + (size_t)L * b->group_max * 2; };
     const float inv_dt = 1.0f / b->dt, inv_dx = 1.0f / b->dx;
 
@@ -335,8 +347,47 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     RTM_CUDA(cudaEventCreate(&e2));
     int nkern = 0;
     // ---- forward pass: levels 2..nt (level 1 is zero), then the snapshot
-    // of the last level
+    // of the last level.  One step of the forward recursion:
+    auto fwd_step = [&](int L) -> int {
+        Step2DArgs<float> a = base_args(false);
+        for (int f = 0; f < 5; f++) {
+            a.out[f] = fb(L & 1, f);
+            a.own2[f] = fb(L & 1, f);
+            a.nb[f] = fb((L - 1) & 1, f);
+        }
+        a.sponge = L >= 3;
+        a.has_src = 1;
+        a.srcval = b->dtsrc[L - 2];
+        a.snap_out[0] = snap(L - 1, 0);
+        a.snap_out[1] = snap(L - 1, 1);
+        a.snap_max_in = mx(L - 1);
+        a.snap_max_out = mx(L);
+        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
+        nkern++;
+        return RTM_OK;
+    };
+    auto snap_last = [&]() -> int {
+        dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
+        k_snap_plane<<<grd, blk, 0, st>>>(b->tab.d_geom, ld, fb(nt & 1, VX), fb(nt & 1, VZ), mx(nt), snap(nt, 0), snap(nt, 1));
+        RTM_CUDA(cudaGetLastError());
+        nkern++;
+        return RTM_OK;
+    };
+    const int ck = b->ckpt;
+    const int nseg = ck ? (nt + ck - 1) / ck : 1;
+    // checkpoint of segment s >= 1: levels a-1, a (a = s*ck + 1) of F
+    auto ck_state = [&](int sgm) { return b->ck.p + (size_t)(sgm - 1) * 10 * gp; };
+    auto record_fwd_ckpt = [&]() -> int {
+        for (int L = 2; L <= nt; L++) {
+            TRY(fwd_step(L));
+            if ((L - 1) % ck == 0)
+                RTM_CUDA(cudaMemcpyAsync(ck_state((L - 1) / ck), b->F.p, 10 * gp * sizeof(float),
+                                         cudaMemcpyDeviceToDevice, st));
+        }
+        return RTM_OK;
+    };
     auto record_fwd = [&]() -> int {
+        if (ck) return record_fwd_ckpt();
         for (int L = 2; L <= nt; L++) {
             Step2DArgs<float> a = base_args(false);
             for (int f = 0; f < 5; f++) {
@@ -361,7 +412,53 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         return RTM_OK;
     };
     // ---- adjoint pass with the imaging condition: levels nt..1
+    auto adj_level = [&](int L) -> int {
+        Step2DArgs<float> a = base_args(true);
+        for (int f = 0; f < 5; f++) {
+            a.out[f] = ab(L & 1, f);
+            a.own2[f] = L + 2 <= nt ? ab(L & 1, f) : b->zero.p;
+            a.nb[f] = L + 1 <= nt ? ab((L + 1) & 1, f) : b->zero.p;
+        }
+        a.sponge = b->exact_adj;
+        a.rec = b->traces.p;
+        a.comp_mask = b->comp_mask;
+        a.ncomp = b->ncomp;
+        a.it = L - 1;
+        a.isnap0[0] = snap(L, 0);
+        a.isnap0[1] = snap(L, 1);
+        a.imax0 = mx(L);
+        a.ilast = L == nt;
+        a.isnap1[0] = L < nt ? snap(L + 1, 0) : snap(L, 0);
+        a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
+        a.imax1 = L < nt ? mx(L + 1) : mx(L);
+        set_img(a);
+        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
+        nkern++;
+        if (blocked && ((nt - L + 1) % IMG_FOLD == 0 || L == 1)) {
+            TRY(fold());
+            nkern++;
+        }
+        return RTM_OK;
+    };
+    // checkpoint-restart: per segment (last first) restore its forward state,
+    // recompute its snapshots (and the next segment's first), migrate through it
+    auto record_adj_ckpt = [&]() -> int {
+        for (int sgm = nseg - 1; sgm >= 0; sgm--) {
+            const int a0 = sgm * ck + 1, b0 = std::min((sgm + 1) * ck, nt);
+            if (sgm == 0) {
+                RTM_CUDA(cudaMemsetAsync(b->F.p, 0, 10 * gp * sizeof(float), st));
+            } else {
+                RTM_CUDA(cudaMemcpyAsync(b->F.p, ck_state(sgm), 10 * gp * sizeof(float), cudaMemcpyDeviceToDevice, st));
+            }
+            const int last = std::min(b0 + 2, nt);
+            for (int L = a0 + 1; L <= last; L++) TRY(fwd_step(L));
+            if (b0 + 2 > nt) TRY(snap_last());
+            for (int L = b0; L >= a0; L--) TRY(adj_level(L));
+        }
+        return RTM_OK;
+    };
     auto record_adj = [&]() -> int {
+        if (ck) return record_adj_ckpt();
         for (int L = nt; L >= 1; L--) {
             Step2DArgs<float> a = base_args(true);
             for (int f = 0; f < 5; f++) {
@@ -525,7 +622,24 @@ extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float d
     if (!s) s = b->traces.alloc((size_t)tcap);
     if (!s) s = b->tstage.alloc((size_t)tcap);
     if (!s) s = b->full.alloc(3 * pf);
-    if (!s) s = b->snaps.alloc((size_t)nt * 2 * gp);
+    if (!s) {
+        // keep every level's snapshots when they fit in 80 % of the free
+        // device memory, otherwise checkpoint every ck levels (ck ~ sqrt(10 nt)
+        // minimises ring + checkpoint storage)
+        size_t free_b = 0, total_b = 0;
+        cudaMemGetInfo(&free_b, &total_b);
+        const double full = (double)nt * 2 * gp * sizeof(__half);
+        if (full > 0.8 * (double)free_b) {
+            int k = (int)std::ceil(std::sqrt(10.0 * nt));
+            b->ckpt = std::max(1, std::min(k, nt));
+        }
+        const int nlev = b->ckpt ? b->ckpt + 1 : nt;
+        s = b->snaps.alloc((size_t)nlev * 2 * gp);
+        if (!s && b->ckpt) {
+            const int nseg = (nt + b->ckpt - 1) / b->ckpt;
+            if (nseg > 1) s = b->ck.alloc((size_t)(nseg - 1) * 10 * gp);
+        }
+    }
     if (!s) s = b->dx0.alloc(b->group_max);
     note_pending("after allocations");
     if (s) { delete b; return nullptr; }
@@ -614,6 +728,7 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[15] = b->st_a;
     out[40] = b->th_f;
     out[41] = b->th_a;
+    out[42] = b->ckpt;
     return RTM_OK;
 }
 
@@ -623,6 +738,24 @@ extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
     RTM_CHECK_ARG(tile_x == 0 || tile_x == 8 || tile_x == 16 || tile_x == 32, "tile_x must be 0, 8, 16 or 32");
     b->use_graph = use_graph != 0;
     b->tile_x = tile_x;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_set_checkpoint(rtm_batch *b, int interval)
+{
+    RTM_CHECK_ARG(b && interval >= 0, "bad arguments");
+    TRY(ensure_device());
+    const int k = std::min(interval, b->nt);
+    const size_t gp = (size_t)b->gplane;
+    b->snaps.release();
+    b->ck.release();
+    b->ckpt = k;
+    const int nlev = k ? k + 1 : b->nt;
+    TRY(b->snaps.alloc((size_t)nlev * 2 * gp));
+    if (k) {
+        const int nseg = (b->nt + k - 1) / k;
+        if (nseg > 1) TRY(b->ck.alloc((size_t)(nseg - 1) * 10 * gp));
+    }
     return RTM_OK;
 }
 

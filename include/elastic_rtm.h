@@ -273,7 +273,7 @@ rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp
  * host pointers. */
 int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device, float *image,
                       int image_on_device);
-/* out[0..41] (pass an array of at least 42 doubles): forward ms, adjoint
+/* out[0..42] (pass an array of at least 43 doubles): forward ms, adjoint
  * ms, cells of the last group, kernels launched, total ms of the last call,
  * forward tile width, forward work items, adjoint tile width; [8..13] the
  * autotuner's best ms per step for tile widths 8, 16, 32 (forward, then
@@ -281,7 +281,8 @@ int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, i
  * adjoint pass; [16..39] the autotuner's ms per step for every tile width
  * (8, 16, 32) and launch shape (1 stage, 2 stages, each with 256 then 512
  * threads), forward then adjoint, -1 where a shape does not fit in a block;
- * [40..41] threads per CTA of the forward and adjoint pass. */
+ * [40..41] threads per CTA of the forward and adjoint pass; [42] checkpoint
+ * interval (0 = every level's snapshots kept). */
 int rtm_batch_stats(const rtm_batch *b, double *out);
 /* Autotuner: times `steps` launches of each pass for every tile width and
  * staging depth on the geometry of shots [shot0, shot0+nshot) and keeps the
@@ -296,6 +297,15 @@ int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x);
  * fit in a block with the tile width in use falls back to 1 stage and 256
  * threads. */
 int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj, int threads_fwd, int threads_adj);
+/* Checkpoint-restart of the source wavefield.  interval = 0 keeps the FP16
+ * snapshots of every level (4 bytes per cell and level); interval = k keeps
+ * the full forward state every k levels (40 bytes per cell each) and a ring
+ * of k + 1 snapshot levels, and the adjoint pass recomputes each k-level
+ * segment from its checkpoint before migrating through it (one more forward
+ * propagation; images bit-identical to interval 0).  rtm_batch_create picks
+ * k ~ sqrt(10 nt) by itself when every level's snapshots would not fit in 80 %
+ * of the free device memory.  out[42] of rtm_batch_stats reports k. */
+int rtm_batch_set_checkpoint(rtm_batch *b, int interval);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */
 void *rtm_host_alloc(size_t bytes);
