@@ -54,6 +54,12 @@ struct GemmArgs {
     float *Cf;          // EPI_F32: Cf[m*ldc + n]; EPI_F32_ATOMIC_T: Cf[n*ldc + m] += acc
     long long ldc;
     int coff;
+    // implicit 3x3 (pad 1) im2col operand: with conv set, A is not read; the
+    // A element of (pixel p, k) is X[p's neighbour at tap k / C][xoff + k % C]
+    // of an NHWC tensor (channel stride ldx, H x W images); C % 8 == 0
+    int conv;
+    const bf16 *X;
+    int ldx, xoff, C, H, W;
 };
 
 constexpr int GBM = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
@@ -108,21 +114,41 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
     const int kend = min(g.K, kbeg + g.kchunk);
     const int ktiles = kend > kbeg ? (kend - kbeg) / GBK : 0;
 
+    // implicit im2col: address of the 8 channels at (pixel p, column kk)
+    auto conv_src = [&](long long p, int kk, bool &ok) -> const bf16 * {
+        const int tap = kk / g.C, c = kk - tap * g.C;
+        const int ky = tap / 3, kx = tap - 3 * ky;
+        const int x = (int)(p % g.W);
+        const long long t = p / g.W;
+        const int y = (int)(t % g.H);
+        const long long b = t / g.H;
+        const int yy = y + ky - 1, xx = x + kx - 1;
+        ok = ok && tap < 9 && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+        return ok ? g.X + ((b * g.H + yy) * g.W + xx) * g.ldx + g.xoff + c : g.X;
+    };
     auto load = [&](int kt, int stage) {
         bf16 *sa = sm + stage * S::STAGE, *sb = sa + S::A_ELEMS;
         const int k0 = kbeg + kt * GBK;
         if (!A_T) {
             for (int c = tid; c < GBM * 4; c += GTHREADS) {
                 const int r = c >> 2, q = c & 3;
-                const bool ok = m0 + r < g.M;
-                const bf16 *src = g.A + (ok ? (long long)(m0 + r) * g.lda + k0 + q * 8 : 0);
+                bool ok = m0 + r < g.M;
+                const bf16 *src;
+                if (g.conv)
+                    src = conv_src(m0 + r, k0 + q * 8, ok);
+                else
+                    src = g.A + (ok ? (long long)(m0 + r) * g.lda + k0 + q * 8 : 0);
                 cpa16(sa + r * (GBK + 8) + q * 8, src, ok);
             }
         } else {
             for (int c = tid; c < GBK * (GBM / 8); c += GTHREADS) {
                 const int r = c / (GBM / 8), q = c % (GBM / 8);
-                const bool ok = m0 + q * 8 < g.M;
-                const bf16 *src = g.A + (ok ? (long long)(k0 + r) * g.lda + m0 + q * 8 : 0);
+                bool ok = m0 + q * 8 < g.M;
+                const bf16 *src;
+                if (g.conv)
+                    src = conv_src(k0 + r, m0 + q * 8, ok);
+                else
+                    src = g.A + (ok ? (long long)(k0 + r) * g.lda + m0 + q * 8 : 0);
                 cpa16(sa + r * (GBM + 8) + q * 8, src, ok);
             }
         }
@@ -267,6 +293,8 @@ int gemm(const GemmArgs &g, bool a_t, bool b_t, int epi, int splits, cudaStream_
     RTM_CHECK_ARG(!a_t || g.M % 8 == 0, "GEMM with M-major A needs M %% 8 == 0 (M=%d)", g.M);
     RTM_CHECK_ARG(!b_t || g.N % 8 == 0, "GEMM with N-major B needs N %% 8 == 0 (N=%d)", g.N);
     RTM_CHECK_ARG(epi != EPI_BF16 || ((g.ldc | g.coff) & 1) == 0, "BF16 GEMM output needs even ldc and offset");
+    RTM_CHECK_ARG(!g.conv || (g.C % 32 == 0 && (g.ldx | g.xoff) % 8 == 0 && g.X && g.H > 0 && g.W > 0),
+                  "implicit im2col needs C %% 32 == 0 and 16-byte aligned channel runs");
     if (epi == EPI_BF16 && !a_t && !b_t) return gemm_bn<false, false, EPI_BF16>(g, splits, st);
     if (epi == EPI_F32 && !a_t && !b_t) return gemm_bn<false, false, EPI_F32>(g, splits, st);
     if (epi == EPI_F32_ATOMIC_T && a_t && b_t) return gemm_bn<true, true, EPI_F32_ATOMIC_T>(g, splits, st);
@@ -626,6 +654,21 @@ int im2col(unet *u, int n, int H, int W, int C, const bf16 *x, int ldx, int coff
     return RTM_OK;
 }
 
+// GEMM A operand as the implicit im2col of an NHWC tensor (C % 32 == 0, so
+// K = 9*C needs no padding and a 32-column chunk stays within one tap)
+void set_implicit(GemmArgs &g, const bf16 *x, int ldx, int xoff, int C, int H, int W)
+{
+    g.conv = 1;
+    g.X = x;
+    g.ldx = ldx;
+    g.xoff = xoff;
+    g.C = C;
+    g.H = H;
+    g.W = W;
+    g.A = x;
+    g.lda = 0;
+}
+
 // input of conv i: (buffer, channel stride, channel offset, channels)
 struct In {
     const bf16 *p;
@@ -654,7 +697,9 @@ int conv_fwd(unet *u, int i, int n)
     const long long P = (long long)n * l.H * l.W;
     GemmArgs g;
     memset(&g, 0, sizeof g);
-    if (l.ks == 3) {
+    if (l.ks == 3 && in.c % 32 == 0) {
+        set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
+    } else if (l.ks == 3) {
         TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
         g.A = u->col.p;
         g.lda = l.kp;
@@ -762,7 +807,9 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     const In in = layer_input(u, i);
     GemmArgs g;
     memset(&g, 0, sizeof g);
-    if (l.ks == 3) {
+    if (l.ks == 3 && in.c % 32 == 0) {
+        set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
+    } else if (l.ks == 3) {
         TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
         g.A = u->col.p;
         g.lda = l.kp;
@@ -792,9 +839,7 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     const GIn gin = layer_ginput(u, i);
     memset(&g, 0, sizeof g);
     if (l.ks == 3) {
-        TRY(im2col(u, n, l.H, l.W, l.coutp, gy, ldg, 0, l.ktp));
-        g.A = u->col.p;
-        g.lda = l.ktp;
+        set_implicit(g, gy, ldg, 0, l.coutp, l.H, l.W);
     } else {
         g.A = gy;
         g.lda = ldg;
