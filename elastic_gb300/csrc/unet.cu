@@ -65,9 +65,9 @@ struct GemmArgs {
 constexpr int GBM = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
 constexpr float LEAK = 0.1f;  // negative-side slope of the activation
 
-template <bool A_T, bool B_T, int BN>
+template <bool A_T, bool B_T, int BM, int BN>
 struct GemmSmem {
-    static constexpr int A_ELEMS = A_T ? GBK * (GBM + 8) : GBM * (GBK + 8);
+    static constexpr int A_ELEMS = A_T ? GBK * (BM + 8) : BM * (GBK + 8);
     static constexpr int B_ELEMS = B_T ? GBK * (BN + 8) : BN * (GBK + 8);
     static constexpr int STAGE = A_ELEMS + B_ELEMS;
     static constexpr size_t BYTES = (size_t)GSTAGES * STAGE * sizeof(bf16);
@@ -100,16 +100,20 @@ __device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], unsign
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-template <bool A_T, bool B_T, int BN, int EPI>
+// Block tile (32*WM) x BN, 8 warps as WM (along M) x 8/WM (along N), warp
+// tile 32 x BN*WM/8.
+template <bool A_T, bool B_T, int BN, int WM, int EPI>
 __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
 {
-    using S = GemmSmem<A_T, B_T, BN>;
+    constexpr int BM = 32 * WM, WN = 8 / WM, WNT = BN / WN;
+    using S = GemmSmem<A_T, B_T, BM, BN>;
     extern __shared__ __align__(16) unsigned char gsm_raw[];
     bf16 *sm = reinterpret_cast<bf16 *>(gsm_raw);
-    constexpr int NT = BN / 16;  // n8 tiles per warp (warp tile 32 x BN/2)
+    constexpr int NT = WNT / 8;  // n8 tiles per warp
+    static_assert(NT % 2 == 0 && WM * WN == 8, "warp layout");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp & 3, wn = warp >> 2;
-    const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * BN;
+    const int wm = warp % WM, wn = warp / WM;
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
     const int kbeg = blockIdx.z * g.kchunk;
     const int kend = min(g.K, kbeg + g.kchunk);
     const int ktiles = kend > kbeg ? (kend - kbeg) / GBK : 0;
@@ -130,7 +134,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
         bf16 *sa = sm + stage * S::STAGE, *sb = sa + S::A_ELEMS;
         const int k0 = kbeg + kt * GBK;
         if (!A_T) {
-            for (int c = tid; c < GBM * 4; c += GTHREADS) {
+            for (int c = tid; c < BM * 4; c += GTHREADS) {
                 const int r = c >> 2, q = c & 3;
                 bool ok = m0 + r < g.M;
                 const bf16 *src;
@@ -141,15 +145,15 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
                 cpa16(sa + r * (GBK + 8) + q * 8, src, ok);
             }
         } else {
-            for (int c = tid; c < GBK * (GBM / 8); c += GTHREADS) {
-                const int r = c / (GBM / 8), q = c % (GBM / 8);
+            for (int c = tid; c < GBK * (BM / 8); c += GTHREADS) {
+                const int r = c / (BM / 8), q = c % (BM / 8);
                 bool ok = m0 + q * 8 < g.M;
                 const bf16 *src;
                 if (g.conv)
                     src = conv_src(k0 + r, m0 + q * 8, ok);
                 else
                     src = g.A + (ok ? (long long)(k0 + r) * g.lda + m0 + q * 8 : 0);
-                cpa16(sa + r * (GBM + 8) + q * 8, src, ok);
+                cpa16(sa + r * (BM + 8) + q * 8, src, ok);
             }
         }
         if (!B_T) {
@@ -198,12 +202,12 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
                     ldsm_x4(af[mt], sa + (mb + (lane & 15)) * (GBK + 8) + ks + (lane >> 4) * 8);
                 } else {
                     const int k = ks + (lane & 7) + (lane >> 4) * 8, m = mb + ((lane >> 3) & 1) * 8;
-                    ldsm_x4_t(af[mt], sa + k * (GBM + 8) + m);
+                    ldsm_x4_t(af[mt], sa + k * (BM + 8) + m);
                 }
             }
 #pragma unroll
             for (int np = 0; np < NT / 2; np++) {
-                const int nb = wn * (BN / 2) + np * 16;
+                const int nb = wn * WNT + np * 16;
                 unsigned bfr[4];
                 if (!B_T) {
                     const int n = nb + (lane & 7) + (lane >> 4) * 8, k = ks + ((lane >> 3) & 1) * 8;
@@ -230,7 +234,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int m = m0 + wm * 32 + mt * 16 + (lane >> 2) + h * 8;
-                const int n = n0 + wn * (BN / 2) + nt * 8 + (lane & 3) * 2;
+                const int n = n0 + wn * WNT + nt * 8 + (lane & 3) * 2;
                 if (m >= g.M) continue;
                 float v0 = acc[mt][nt][2 * h], v1 = acc[mt][nt][2 * h + 1];
                 if (EPI == EPI_F32_ATOMIC_T) {
@@ -260,30 +264,33 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
             }
 }
 
-template <bool A_T, bool B_T, int BN, int EPI>
+template <bool A_T, bool B_T, int BN, int WM, int EPI>
 int gemm_launch(const GemmArgs &g, int splits, cudaStream_t st)
 {
-    using S = GemmSmem<A_T, B_T, BN>;
-    auto kern = k_gemm<A_T, B_T, BN, EPI>;
+    constexpr int BM = 32 * WM;
+    using S = GemmSmem<A_T, B_T, BM, BN>;
+    auto kern = k_gemm<A_T, B_T, BN, WM, EPI>;
     static bool attr = false;
     if (!attr) {
         RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES));
         attr = true;
     }
-    dim3 grid((g.M + GBM - 1) / GBM, (g.N + BN - 1) / BN, splits);
+    dim3 grid((g.M + BM - 1) / BM, (g.N + BN - 1) / BN, splits);
     kern<<<grid, GTHREADS, S::BYTES, st>>>(g);
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }
 
-// Dispatch on operand layouts, epilogue and the N tile (32, 64 or 128).
+// Dispatch on operand layouts, epilogue and the tile shape: 128 x N for
+// N = 64, 96 and multiples of 128 (warp tile 32 x N/2); otherwise 256 x 32
+// tiles with all eight warps along M (warp tile 32 x 32).
 template <bool A_T, bool B_T, int EPI>
 int gemm_bn(const GemmArgs &g, int splits, cudaStream_t st)
 {
-    if (g.N <= 32) return gemm_launch<A_T, B_T, 32, EPI>(g, splits, st);
-    if (g.N % 128 == 0) return gemm_launch<A_T, B_T, 128, EPI>(g, splits, st);
-    if (g.N % 64 == 0) return gemm_launch<A_T, B_T, 64, EPI>(g, splits, st);
-    return gemm_launch<A_T, B_T, 32, EPI>(g, splits, st);
+    if (g.N == 64) return gemm_launch<A_T, B_T, 64, 4, EPI>(g, splits, st);
+    if (g.N == 96) return gemm_launch<A_T, B_T, 96, 4, EPI>(g, splits, st);
+    if (g.N % 128 == 0) return gemm_launch<A_T, B_T, 128, 4, EPI>(g, splits, st);
+    return gemm_launch<A_T, B_T, 32, 8, EPI>(g, splits, st);
 }
 
 int gemm(const GemmArgs &g, bool a_t, bool b_t, int epi, int splits, cudaStream_t st)
@@ -346,18 +353,133 @@ __global__ void k_im2col3_v8(int n, int H, int W, int C, const bf16 *x, int ldx,
     }
 }
 
-// g *= (y > 0 ? 1 : LEAK), elementwise over P pixels x C channels (stride
-// ld): the activation's derivative (y > 0 exactly where its input is > 0).
-__global__ void k_relu_mask(long long P, int C, int ld, const bf16 *y, bf16 *g)
+// 8 BF16 values <-> floats
+__device__ __forceinline__ void unpack8(const uint4 &u, float f[8])
 {
-    const long long total = P * C;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / C;
-        const int c = (int)(i - p * C);
-        if (!(__bfloat162float(y[p * ld + c]) > 0.f))
-            g[p * ld + c] = __float2bfloat16_rn(LEAK * __bfloat162float(g[p * ld + c]));
+    const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f[2 * i] = t.x;
+        f[2 * i + 1] = t.y;
     }
 }
+__device__ __forceinline__ uint4 pack8(const float f[8])
+{
+    uint4 u;
+    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    return u;
+}
+
+// Vector forms of the layout kernels below, 8 channels per thread (C, the
+// strides and offsets multiples of 8).
+__global__ void k_relu_mask8(long long P, int C, int ld, const bf16 *y, bf16 *g)
+{
+    const int c8 = C / 8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P * c8; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / c8;
+        const long long o = p * ld + (i - p * c8) * 8;
+        float yv[8], gv[8];
+        unpack8(*reinterpret_cast<const uint4 *>(y + o), yv);
+        unpack8(*reinterpret_cast<const uint4 *>(g + o), gv);
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (!(yv[k] > 0.f)) gv[k] *= LEAK;
+        *reinterpret_cast<uint4 *>(g + o) = pack8(gv);
+    }
+}
+__global__ void k_up_fwd8(int n, int Hi, int Wi, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
+{
+    const int Ho = 2 * Hi, Wo = 2 * Wi, c8 = C / 8;
+    const long long total = (long long)n * Ho * Wo * c8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % c8) * 8;
+        const long long p = i / c8;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        *reinterpret_cast<uint4 *>(out + p * ldo + c) =
+            *reinterpret_cast<const uint4 *>(in + ((b * Hi + y / 2) * Wi + x / 2) * ldi + c);
+    }
+}
+__global__ void k_up_bwd8(int n, int Hi, int Wi, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
+{
+    const int Wo = 2 * Wi, Ho = 2 * Hi, c8 = C / 8;
+    const long long total = (long long)n * Hi * Wi * c8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % c8) * 8;
+        const long long p = i / c8;
+        const int x = (int)(p % Wi), y = (int)((p / Wi) % Hi);
+        const long long b = p / ((long long)Wi * Hi);
+        const long long q = (b * Ho + 2 * y) * Wo + 2 * x;
+        const long long qs[4] = {q, q + 1, q + Wo, q + Wo + 1};
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, v[8];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            unpack8(*reinterpret_cast<const uint4 *>(gout + qs[k] * ldo + c), v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) s[j] += v[j];
+        }
+        *reinterpret_cast<uint4 *>(gin + p * ldi + c) = pack8(s);
+    }
+}
+__global__ void k_pool_fwd8(int n, int Ho, int Wo, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
+{
+    const int Wi = 2 * Wo, Hi = 2 * Ho, c8 = C / 8;
+    const long long total = (long long)n * Ho * Wo * c8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % c8) * 8;
+        const long long p = i / c8;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
+        const long long qs[4] = {q, q + 1, q + Wi, q + Wi + 1};
+        float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, v[8];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            unpack8(*reinterpret_cast<const uint4 *>(in + qs[k] * ldi + c), v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) s[j] += v[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) s[j] *= 0.25f;
+        *reinterpret_cast<uint4 *>(out + p * ldo + c) = pack8(s);
+    }
+}
+__global__ void k_pool_bwd_add8(int n, int Ho, int Wo, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
+{
+    const int Wi = 2 * Wo, Hi = 2 * Ho, c8 = C / 8;
+    const long long total = (long long)n * Ho * Wo * c8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % c8) * 8;
+        const long long p = i / c8;
+        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
+        const long long b = p / ((long long)Wo * Ho);
+        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
+        float g[8], v[8];
+        unpack8(*reinterpret_cast<const uint4 *>(gout + p * ldo + c), g);
+        const long long qs[4] = {q, q + 1, q + Wi, q + Wi + 1};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint4 *d = reinterpret_cast<uint4 *>(gin + qs[k] * ldi + c);
+            unpack8(*d, v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] += 0.25f * g[j];
+            *d = pack8(v);
+        }
+    }
+}
+__global__ void k_copy_ch8(long long P, int C, const bf16 *src, int lds, int soff, bf16 *dst, int ldd, int doff)
+{
+    const int c8 = C / 8;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P * c8; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / c8;
+        const int c = (int)(i - p * c8) * 8;
+        *reinterpret_cast<uint4 *>(dst + p * ldd + doff + c) = *reinterpret_cast<const uint4 *>(src + p * lds + soff + c);
+    }
+}
+
 
 // db[c] += sum_p g[p][c] (channels on threads, pixels split over blocks)
 __global__ void k_bias_grad(long long P, int C, int ld, const bf16 *g, float *db)
@@ -371,83 +493,6 @@ __global__ void k_bias_grad(long long P, int C, int ld, const bf16 *g, float *db
     atomicAdd(db + c, s);
 }
 
-// 2x2 average pool, NHWC; out channels [0,C) stride ldo, in stride ldi.
-__global__ void k_pool_fwd(int n, int Ho, int Wo, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
-{
-    const long long total = (long long)n * Ho * Wo * C;
-    const int Wi = 2 * Wo, Hi = 2 * Ho;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
-        const long long b = p / ((long long)Wo * Ho);
-        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
-        const float s = __bfloat162float(in[q * ldi + c]) + __bfloat162float(in[(q + 1) * ldi + c]) +
-                        __bfloat162float(in[(q + Wi) * ldi + c]) + __bfloat162float(in[(q + Wi + 1) * ldi + c]);
-        out[p * ldo + c] = __float2bfloat16_rn(0.25f * s);
-    }
-}
-// gin[2y+i][2x+j] += 0.25 * gout[y][x]
-__global__ void k_pool_bwd_add(int n, int Ho, int Wo, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
-{
-    const long long total = (long long)n * Ho * Wo * C;
-    const int Wi = 2 * Wo, Hi = 2 * Ho;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
-        const long long b = p / ((long long)Wo * Ho);
-        const long long q = (b * Hi + 2 * y) * Wi + 2 * x;
-        const float g = 0.25f * __bfloat162float(gout[p * ldo + c]);
-        const long long qs[4] = {q, q + 1, q + Wi, q + Wi + 1};
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            bf16 *d = gin + qs[k] * ldi + c;
-            *d = __float2bfloat16_rn(__bfloat162float(*d) + g);
-        }
-    }
-}
-// nearest 2x upsampling into channels [0,C) of out (stride ldo)
-__global__ void k_up_fwd(int n, int Hi, int Wi, int C, const bf16 *in, int ldi, bf16 *out, int ldo)
-{
-    const int Ho = 2 * Hi, Wo = 2 * Wi;
-    const long long total = (long long)n * Ho * Wo * C;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wo), y = (int)((p / Wo) % Ho);
-        const long long b = p / ((long long)Wo * Ho);
-        out[p * ldo + c] = in[((b * Hi + y / 2) * Wi + x / 2) * ldi + c];
-    }
-}
-// gin[y][x] = sum of the 4 gout pixels it was copied to (channels [0,C) of gout)
-__global__ void k_up_bwd(int n, int Hi, int Wi, int C, const bf16 *gout, int ldo, bf16 *gin, int ldi)
-{
-    const int Wo = 2 * Wi, Ho = 2 * Hi;
-    const long long total = (long long)n * Hi * Wi * C;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const long long p = i / C;
-        const int x = (int)(p % Wi), y = (int)((p / Wi) % Hi);
-        const long long b = p / ((long long)Wi * Hi);
-        const long long q = (b * Ho + 2 * y) * Wo + 2 * x;
-        const float s = __bfloat162float(gout[q * ldo + c]) + __bfloat162float(gout[(q + 1) * ldo + c]) +
-                        __bfloat162float(gout[(q + Wo) * ldo + c]) + __bfloat162float(gout[(q + Wo + 1) * ldo + c]);
-        gin[p * ldi + c] = __float2bfloat16_rn(s);
-    }
-}
-// dst[p][doff + c] = src[p][soff + c] (add: dst += src, in FP32)
-__global__ void k_copy_ch(long long P, int C, const bf16 *src, int lds, int soff, bf16 *dst, int ldd, int doff, int add)
-{
-    const long long total = P * C;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / C;
-        const int c = (int)(i - p * C);
-        const bf16 v = src[p * lds + soff + c];
-        bf16 *d = dst + p * ldd + doff + c;
-        *d = add ? __float2bfloat16_rn(__bfloat162float(*d) + __bfloat162float(v)) : v;
-    }
-}
 // FP32 NHWC (C channels) -> BF16
 __global__ void k_to_bf16(long long n, const float *x, bf16 *y)
 {
@@ -459,18 +504,14 @@ __global__ void k_to_bf16(long long n, const float *x, bf16 *y)
 __global__ void k_mse(long long P, int C, const float *out, int ldo, const float *t, bf16 *g, int ldg, double *part)
 {
     double acc = 0.0;
-    const double scale = 2.0 / ((double)P * C);
-    const long long total = P * ldg;
+    const float scale = (float)(2.0 / ((double)P * C));
+    const long long total = P * C;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-        const long long p = i / ldg;
-        const int c = (int)(i - p * ldg);
-        float gv = 0.f;
-        if (c < C) {
-            const double d = (double)out[p * ldo + c] - (double)t[p * C + c];
-            acc += d * d;
-            gv = (float)(scale * d);
-        }
-        g[i] = __float2bfloat16_rn(gv);
+        const long long p = i / C;
+        const int c = (int)(i - p * C);
+        const float d = out[p * ldo + c] - t[i];
+        acc += (double)d * (double)d;
+        g[p * ldg + c] = __float2bfloat16_rn(scale * d);
     }
     __shared__ double red[32];
     for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
@@ -627,6 +668,8 @@ int setup(unet *u)
     TRY(u->col.alloc((size_t)maxcol));
     TRY(u->xin.alloc((size_t)P0 * u->cin));
     TRY(u->gout.alloc((size_t)P0 * 32));
+    // channels >= cout of the output gradient are never written: zero once
+    RTM_CUDA(cudaMemset(u->gout.p, 0, (size_t)P0 * 32 * sizeof(bf16)));
     TRY(u->out.alloc((size_t)P0 * 8));
     TRY(u->tgt.alloc((size_t)P0 * u->cout));
     TRY(u->part.alloc(4096));
@@ -730,7 +773,8 @@ int forward(unet *u, int n)
     const int *c = u->ch;
     auto pool = [&](int k, const bf16 *src, int ld) {
         const int Ho = u->H >> (k + 1), Wo = u->W >> (k + 1);
-        k_pool_fwd<<<grid_for((long long)n * Ho * Wo * c[k]), 256, 0, u->st>>>(n, Ho, Wo, c[k], src, ld, u->pool[k].p, c[k]);
+        k_pool_fwd8<<<grid_for((long long)n * Ho * Wo * c[k] / 8), 256, 0, u->st>>>(n, Ho, Wo, c[k], src, ld, u->pool[k].p,
+                                                                                   c[k]);
         RTM_CUDA(cudaGetLastError());
         return RTM_OK;
     };
@@ -738,9 +782,9 @@ int forward(unet *u, int n)
         // cat[k] = [up(low) (clow ch) | skip (c[k] ch)] at level k
         const int Hl = u->H >> (k + 1), Wl = u->W >> (k + 1), cc = clow + c[k];
         const long long P = (long long)n * (u->H >> k) * (u->W >> k);
-        k_up_fwd<<<grid_for(P * clow), 256, 0, u->st>>>(n, Hl, Wl, clow, low, clow, u->cat[k].p, cc);
+        k_up_fwd8<<<grid_for(P * clow / 8), 256, 0, u->st>>>(n, Hl, Wl, clow, low, clow, u->cat[k].p, cc);
         RTM_CUDA(cudaGetLastError());
-        k_copy_ch<<<grid_for(P * c[k]), 256, 0, u->st>>>(P, c[k], skip, c[k], 0, u->cat[k].p, cc, clow, 0);
+        k_copy_ch8<<<grid_for(P * c[k] / 8), 256, 0, u->st>>>(P, c[k], skip, c[k], 0, u->cat[k].p, cc, clow);
         RTM_CUDA(cudaGetLastError());
         return RTM_OK;
     };
@@ -797,7 +841,7 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     bf16 *gy = last ? u->gout.p : u->ga[i].p;
     const int ldg = last ? 32 : l.coutp;
     if (l.relu) {
-        k_relu_mask<<<grid_for(P * l.coutp), 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy);
+        k_relu_mask8<<<grid_for(P * l.coutp / 8), 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy);
         RTM_CUDA(cudaGetLastError());
     }
     k_bias_grad<<<std::min<long long>(1024, std::max<long long>(1, P / 64)), 128, 0, u->st>>>(P, l.coutp, ldg, gy,
@@ -825,7 +869,7 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     RTM_CHECK_ARG(P % 32 == 0, "pixel count %lld of a U-Net layer is not a multiple of 32", P);
     g.K = (int)Kfull;
     // split the pixel reduction so that the grid covers the SMs
-    const int tiles = ((g.M + GBM - 1) / GBM) * ((g.N + 31) / 32);
+    const int tiles = ((g.M + 255) / 256) * ((g.N + 31) / 32);
     int splits = (int)std::max(1LL, std::min<long long>(Kfull / 256, (4LL * eg::device_sm_count() + tiles - 1) / tiles));
     long long kc = (Kfull + splits - 1) / splits;
     kc = (kc + 31) / 32 * 32;
@@ -863,16 +907,16 @@ int backward(unet *u, int n)
         // gcat[k] -> grad of the upsampled low level (into glow) and of the skip
         const int Hl = u->H >> (k + 1), Wl = u->W >> (k + 1), cc = clow + c[k];
         const long long P = (long long)n * (u->H >> k) * (u->W >> k);
-        k_up_bwd<<<grid_for((long long)n * Hl * Wl * clow), 256, 0, u->st>>>(n, Hl, Wl, clow, u->gcat[k].p, cc, glow,
+        k_up_bwd8<<<grid_for((long long)n * Hl * Wl * clow / 8), 256, 0, u->st>>>(n, Hl, Wl, clow, u->gcat[k].p, cc, glow,
                                                                            clow);
         RTM_CUDA(cudaGetLastError());
-        k_copy_ch<<<grid_for(P * c[k]), 256, 0, u->st>>>(P, c[k], u->gcat[k].p, cc, clow, gskip, c[k], 0, 0);
+        k_copy_ch8<<<grid_for(P * c[k] / 8), 256, 0, u->st>>>(P, c[k], u->gcat[k].p, cc, clow, gskip, c[k], 0);
         RTM_CUDA(cudaGetLastError());
         return RTM_OK;
     };
     auto pool_bwd = [&](int k, bf16 *gdst) {
         const int Ho = u->H >> (k + 1), Wo = u->W >> (k + 1);
-        k_pool_bwd_add<<<grid_for((long long)n * Ho * Wo * c[k]), 256, 0, u->st>>>(n, Ho, Wo, c[k], u->gpool[k].p,
+        k_pool_bwd_add8<<<grid_for((long long)n * Ho * Wo * c[k] / 8), 256, 0, u->st>>>(n, Ho, Wo, c[k], u->gpool[k].p,
                                                                                   c[k], gdst, c[k]);
         RTM_CUDA(cudaGetLastError());
         return RTM_OK;
