@@ -153,6 +153,7 @@ def run_gpu(args):
     eng = BatchRTM(c["nz"], c["nx"], c["nt"], c["dx"], c["dt"], c["fp"], c["abc"], rho, lam, mu, x0, nxs, xsrc, zs,
                    zr, comp_mask=c["comp_mask"], group_max=args.group, nsource=c["nsource"])
     groups = eng.groups()
+    eng.set_tma(args.staging == "tma")
     # autotuner: tile width per pass, timed on the widest group (untimed)
     widest = max(groups, key=lambda g: int(eng.nxs[g[0]:g[0] + g[1]].sum()))
     tune = eng.autotune(widest[0], widest[1], steps=args.tune_steps)
@@ -258,6 +259,7 @@ def run_gpu(args):
         "config": {"workload": c["desc"] + f"; one step = one group of {args.group} shots (forward + adjoint with "
                                "imaging); FP16 source snapshots",
                    "group_shots": args.group, "checkpoint_interval": st["checkpoint"],
+                   "tile_staging": "tensor-memory-access bulk loads" if st["tma"] else "per-thread cp.async",
                    "inputs_vs_l2": "inputs larger than L2 (snapshots or checkpoints ~100+ GB)",
                    "tile": {"forward_tx": tune["tile_x"], "adjoint_tx": tune["tile_x_adj"], "tz": 128,
                             "forward_stages": tune["stages"], "adjoint_stages": tune["stages_adj"],
@@ -560,6 +562,7 @@ def main():
     ap.add_argument("--tune-steps", type=int, default=20)
     ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond"])
     ap.add_argument("--pairs", type=int, default=None, help="training pairs of the precond workload")
+    ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")

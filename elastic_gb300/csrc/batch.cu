@@ -19,6 +19,8 @@
 // sponge are those of the subgrid), so a shot migrated in a batch gives the
 // same image as the single-shot pipeline on its subgrid (up to the FP16
 // snapshot rounding and the summation order of the imaging condition).
+#include <cuda.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -27,6 +29,7 @@
 #include "../../include/elastic_rtm.h"
 #include "elastic2d.cuh"
 #include "elastic2d_aux.cuh"
+#include "elastic2d_v2.cuh"
 #include "engine.h"
 
 using namespace eg;
@@ -96,8 +99,55 @@ __global__ void k_fold(long long n4, float4 *sum, float4 *cmp, float4 *part)
     }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// 3D tensor map (ldz rows x cols columns x planes, plane stride plane_elems)
+// with the v2 step's tile box (V2_LZ rows x tx + 2*HALO columns x 1 plane)
+int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
+             long long plane_elems, int tx)
+{
+    EncodeTiledFn fn = encode_fn();
+    RTM_CHECK_ARG(fn, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t es = half ? 2 : 4;
+    const cuuint64_t dims[3] = {(cuuint64_t)ldz, (cuuint64_t)cols, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldz * es, (cuuint64_t)plane_elems * es};
+    const cuuint32_t box[3] = {(cuuint32_t)V2_LZ, (cuuint32_t)(tx + 2 * HALO), 1};
+    const cuuint32_t el[3] = {1, 1, 1};
+    const CUresult r = fn(m, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                          const_cast<void *>(base), dims, strides, box, el, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        rtm_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return RTM_ERR_CUDA;
+    }
+    return RTM_OK;
+}
+
 // levels accumulated in FP32 partial planes between two folds
 constexpr int IMG_FOLD = 32;
+// zero guard columns after every shot of a group: a halo read across a shot's
+// edge (5 columns) lands on zeros, so tile staging needs no per-shot masking
+constexpr int GUARD = 5;
 
 }  // namespace
 
@@ -117,6 +167,8 @@ struct rtm_batch {
     // segment from its checkpoint before migrating through it.
     int ckpt = 0;
     DevBuf<float> ck;
+    bool use_tma = true;   // stage step tiles with tensor-memory-access loads
+    DevBuf<int> err;       // set by a step kernel whose tile load never completed
     DevBuf<int> dx0;
     ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
     ShotTable tab_a;  // adjoint pass work items
@@ -140,6 +192,19 @@ struct rtm_batch {
 };
 
 namespace {
+
+// A step kernel that gave up waiting for its staged tile sets b->err.
+int check_tile_loads(rtm_batch *b)
+{
+    int e = 0;
+    RTM_CUDA(cudaMemcpy(&e, b->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        RTM_CUDA(cudaMemset(b->err.p, 0, sizeof(int)));
+        rtm_set_error("a step kernel's tile load did not complete within its time limit");
+        return RTM_ERR_TIMEOUT;
+    }
+    return RTM_OK;
+}
 
 int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_dev, float *image, int image_dev,
                 int tune_steps = 0)
@@ -173,7 +238,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         b->tab.shots.push_back(h);
         x0g[i] = b->x0[s];
         tin_off[i] = tin;
-        col += b->nxs[s];
+        col += b->nxs[s] + GUARD;
         doff += (long long)nt * b->ncomp * b->nxs[s];
         tin += (long long)b->ncomp * b->nxs[s] * nt;
     }
@@ -198,7 +263,24 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     }
     RTM_CUDA(cudaMemcpyAsync(b->dx0.p, x0g.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
     const long long gp = b->gplane;
-    // ---- coefficients of every shot's subgrid
+    // tensor maps of the staged planes (tile box of the pass's width)
+    const bool tma_on = b->use_tma && tz == TZ_TILE2;
+    CUtensorMap mF, mA, mC, mS;
+    memset(&mF, 0, sizeof mF); memset(&mA, 0, sizeof mA); memset(&mC, 0, sizeof mC); memset(&mS, 0, sizeof mS);
+    auto build_maps = [&](int txf, int txa) -> int {
+        if (!tma_on) return RTM_OK;
+        const long long cols = b->cap_cols;
+        const long long nlev = b->ckpt ? b->ckpt + 1 : nt;
+        TRY(make_map(&mF, b->F.p, false, ld, cols, 10, gp, txf));
+        TRY(make_map(&mA, b->A.p, false, ld, cols, 10, gp, txa));
+        TRY(make_map(&mC, b->coef.p, false, ld, cols, 5, gp, txa));
+        TRY(make_map(&mS, b->snaps.p, true, ld, cols, 2 * nlev, gp, txa));
+        return RTM_OK;
+    };
+    TRY(build_maps(b->tab.tx, b->tab_a.tx));
+    // ---- coefficients of every shot's subgrid (guard columns and columns of
+    // the previous group's shots are zero)
+    RTM_CUDA(cudaMemsetAsync(b->coef.p, 0, 5 * gp * sizeof(float), st));
     for (int i = 0; i < ns; i++) {
         const HostShot &h = b->tab.shots[i];
         const long long mo = (long long)x0g[i] * nz;
@@ -271,8 +353,16 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         a.abc2 = b->abc + 5;
         a.inv_dt = inv_dt;
         a.inv_dx = inv_dx;
+        if (tma_on) {
+            a.tma = 1;
+            a.err = b->err.p;
+            a.tm[0] = adj ? mA : mF;
+            a.tm[1] = mC;
+            a.tm[2] = mS;
+        }
         return a;
     };
+    auto slot = [&](int L) { return b->ckpt ? L % (b->ckpt + 1) : L - 1; };
     // initialise launch configuration outside any capture
     {
         Step2DArgs<float> a = base_args(false);
@@ -301,6 +391,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                     }
                     ShotTable &tb = pass ? b->tab_a : b->tab;
                     TRY(tb.build(cand[ci], tz));
+                    TRY(build_maps(b->tab.tx, b->tab_a.tx));
                     for (int rep = 0; rep < 2; rep++) {  // first round warms up
                         RTM_CUDA(cudaEventRecord(t0, st));
                         for (int k = 0; k < tune_steps; k++) {
@@ -310,7 +401,10 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                                 a.out[f] = pass ? ab(L & 1, f) : fb(L & 1, f);
                                 a.own2[f] = a.out[f];
                                 a.nb[f] = pass ? ab((L + 1) & 1, f) : fb((L + 1) & 1, f);
+                                a.nb_plane[f] = ((L + 1) & 1) * 5 + f;
                             }
+                            a.snap_plane[0] = 2 * slot(1);
+                            a.snap_plane[1] = 2 * slot(1) + 1;
                             if (!pass) {
                                 a.sponge = 1;
                                 a.snap_out[0] = snap(1, 0);
@@ -338,7 +432,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         }
         cudaEventDestroy(t0);
         cudaEventDestroy(t1);
-        return RTM_OK;
+        return check_tile_loads(b);
     }
 
     cudaEvent_t e0, e1, e2;
@@ -354,6 +448,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.out[f] = fb(L & 1, f);
             a.own2[f] = fb(L & 1, f);
             a.nb[f] = fb((L - 1) & 1, f);
+            a.nb_plane[f] = ((L - 1) & 1) * 5 + f;
         }
         a.sponge = L >= 3;
         a.has_src = 1;
@@ -388,28 +483,8 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     };
     auto record_fwd = [&]() -> int {
         if (ck) return record_fwd_ckpt();
-        for (int L = 2; L <= nt; L++) {
-            Step2DArgs<float> a = base_args(false);
-            for (int f = 0; f < 5; f++) {
-                a.out[f] = fb(L & 1, f);
-                a.own2[f] = fb(L & 1, f);
-                a.nb[f] = fb((L - 1) & 1, f);
-            }
-            a.sponge = L >= 3;
-            a.has_src = 1;
-            a.srcval = b->dtsrc[L - 2];
-            a.snap_out[0] = snap(L - 1, 0);
-            a.snap_out[1] = snap(L - 1, 1);
-            a.snap_max_in = mx(L - 1);
-            a.snap_max_out = mx(L);
-            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
-            nkern++;
-        }
-        dim3 blk(128), grd(ceil_div(nz, 128), (unsigned)*std::max_element(b->nxs.begin() + s0, b->nxs.begin() + s0 + ns), ns);
-        k_snap_plane<<<grd, blk, 0, st>>>(b->tab.d_geom, ld, fb(nt & 1, VX), fb(nt & 1, VZ), mx(nt), snap(nt, 0), snap(nt, 1));
-        RTM_CUDA(cudaGetLastError());
-        nkern++;
-        return RTM_OK;
+        for (int L = 2; L <= nt; L++) TRY(fwd_step(L));
+        return snap_last();
     };
     // ---- adjoint pass with the imaging condition: levels nt..1
     auto adj_level = [&](int L) -> int {
@@ -418,7 +493,10 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
             a.out[f] = ab(L & 1, f);
             a.own2[f] = L + 2 <= nt ? ab(L & 1, f) : b->zero.p;
             a.nb[f] = L + 1 <= nt ? ab((L + 1) & 1, f) : b->zero.p;
+            a.nb_plane[f] = L + 1 <= nt ? ((L + 1) & 1) * 5 + f : 10;  // past the last plane: zeros
         }
+        a.snap_plane[0] = 2 * slot(L);
+        a.snap_plane[1] = 2 * slot(L) + 1;
         a.sponge = b->exact_adj;
         a.rec = b->traces.p;
         a.comp_mask = b->comp_mask;
@@ -459,33 +537,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
     };
     auto record_adj = [&]() -> int {
         if (ck) return record_adj_ckpt();
-        for (int L = nt; L >= 1; L--) {
-            Step2DArgs<float> a = base_args(true);
-            for (int f = 0; f < 5; f++) {
-                a.out[f] = ab(L & 1, f);
-                a.own2[f] = L + 2 <= nt ? ab(L & 1, f) : b->zero.p;
-                a.nb[f] = L + 1 <= nt ? ab((L + 1) & 1, f) : b->zero.p;
-            }
-            a.sponge = b->exact_adj;
-            a.rec = b->traces.p;
-            a.comp_mask = b->comp_mask;
-            a.ncomp = b->ncomp;
-            a.it = L - 1;
-            a.isnap0[0] = snap(L, 0);
-            a.isnap0[1] = snap(L, 1);
-            a.imax0 = mx(L);
-            a.ilast = L == nt;
-            a.isnap1[0] = L < nt ? snap(L + 1, 0) : snap(L, 0);
-            a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
-            a.imax1 = L < nt ? mx(L + 1) : mx(L);
-            set_img(a);
-            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
-            nkern++;
-            if (blocked && ((nt - L + 1) % IMG_FOLD == 0 || L == 1)) {
-                TRY(fold());
-                nkern++;
-            }
-        }
+        for (int L = nt; L >= 1; L--) TRY(adj_level(L));
         return RTM_OK;
     };
     // capture one graph per pass; timing events stay outside the graphs
@@ -550,6 +602,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         RTM_CUDA(cudaMemcpyAsync(image, b->full.p, 3 * pf * sizeof(float), cudaMemcpyDeviceToHost, st));
     }
     RTM_CUDA(cudaStreamSynchronize(st));
+    TRY(check_tile_loads(b));
     float f_ms = 0, a_ms = 0;
     RTM_CUDA(cudaEventElapsedTime(&f_ms, e0, e1));
     RTM_CUDA(cudaEventElapsedTime(&a_ms, e1, e2));
@@ -603,7 +656,7 @@ extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float d
     std::vector<int> w(b->nxs);
     std::sort(w.begin(), w.end(), std::greater<int>());
     long long cap = 0;
-    for (int i = 0; i < b->group_max; i++) cap += w[i];
+    for (int i = 0; i < b->group_max; i++) cap += w[i] + GUARD;
     b->cap_cols = cap;
     b->gplane = cap * b->ldz;
     long long tcap = 0;
@@ -641,6 +694,7 @@ extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float d
         }
     }
     if (!s) s = b->dx0.alloc(b->group_max);
+    if (!s) s = b->err.alloc(1);
     note_pending("after allocations");
     if (s) { delete b; return nullptr; }
     if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) {
@@ -659,6 +713,8 @@ extern "C" rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float d
         {cudaMemcpy(b->model.p + pf, lambda, pf * sizeof(float), cudaMemcpyHostToDevice), "lambda upload"},
         {cudaMemcpy(b->model.p + 2 * pf, mu, pf * sizeof(float), cudaMemcpyHostToDevice), "mu upload"},
         {cudaMemset(b->zero.p, 0, gp * sizeof(float)), "zero plane"},
+        {cudaMemset(b->err.p, 0, sizeof(int)), "error flag"},
+        {cudaMemset(b->snaps.p, 0, b->snaps.n * sizeof(__half)), "snapshot store"},
         {cudaMemset(b->coefraw.p, 0, 5 * gp * sizeof(float)), "coefficient planes"},
         {cudaMemset(b->coef.p, 0, 5 * gp * sizeof(float)), "masked coefficient planes"},
         {cudaMemcpy(b->filt.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice), "filter upload"},
@@ -729,6 +785,7 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[40] = b->th_f;
     out[41] = b->th_a;
     out[42] = b->ckpt;
+    out[43] = b->use_tma ? 1 : 0;
     return RTM_OK;
 }
 
@@ -738,6 +795,14 @@ extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
     RTM_CHECK_ARG(tile_x == 0 || tile_x == 8 || tile_x == 16 || tile_x == 32, "tile_x must be 0, 8, 16 or 32");
     b->use_graph = use_graph != 0;
     b->tile_x = tile_x;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_set_tma(rtm_batch *b, int on)
+{
+    RTM_CHECK_ARG(b, "null argument");
+    if (on) RTM_CHECK_ARG(encode_fn() != nullptr, "tensor maps are not available from the driver");
+    b->use_tma = on != 0;
     return RTM_OK;
 }
 
@@ -752,6 +817,7 @@ extern "C" int rtm_batch_set_checkpoint(rtm_batch *b, int interval)
     b->ckpt = k;
     const int nlev = k ? k + 1 : b->nt;
     TRY(b->snaps.alloc((size_t)nlev * 2 * gp));
+    RTM_CUDA(cudaMemset(b->snaps.p, 0, b->snaps.n * sizeof(__half)));
     if (k) {
         const int nseg = (b->nt + k - 1) / k;
         if (nseg > 1) TRY(b->ck.alloc((size_t)(nseg - 1) * 10 * gp));

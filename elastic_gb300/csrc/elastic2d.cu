@@ -136,7 +136,7 @@ bool v2_fits(bool adj, bool exact, int tx, int stages, int threads)
 {
     if (stages < 1 || stages > 2 || !v2_threads_ok(exact, tx, threads)) return false;
     const size_t b = v2_stage_bytes(adj, exact, tx);
-    return b > 0 && (size_t)stages * b <= (size_t)max_smem_optin();
+    return b > 0 && (size_t)stages * b + V2_SMEM_EXTRA <= (size_t)max_smem_optin();
 }
 
 template <bool EXACT, bool ADJ, int TX>
@@ -146,7 +146,7 @@ static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t s
     const bool img = ADJ && a.img[0] != nullptr;
     RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX, stages, threads),
                   "tile width %d with %d stages and %d threads does not fit in a block", TX, stages, threads);
-    const size_t smem = (size_t)stages * v2_smem<ADJ, EXACT, TX>(img);
+    const size_t smem = (size_t)stages * v2_smem<ADJ, EXACT, TX>(img) + V2_SMEM_EXTRA;
     static bool attr_set = false;
     static int grid_max[2][2][2] = {};
     if (!attr_set) {

@@ -21,6 +21,7 @@
 // compiler may fuse multiply-adds and the adjoint uses pre-multiplied
 // coefficient*field products.
 #pragma once
+#include <cuda.h>
 #include "common.cuh"
 
 namespace eg {
@@ -87,6 +88,20 @@ struct Step2DArgs {
     T *img[3];
     T *imgc[3];
     T inv_dt, inv_dx;
+
+    // ---- TMA tile staging (v2 float kernel, batch engine) ------------------
+    // With tma set, the halo tiles of the neighbour level, the coefficients
+    // (adjoint) and the level's FP16 snapshots (imaging) are loaded by
+    // cp.async.bulk.tensor from 3D tensors (ldz rows x columns x planes):
+    // tm[0] the neighbour-level planes (nb_plane[f] selects field f's plane;
+    // a plane index past the last reads zeros), tm[1] the five coefficient
+    // planes, tm[2] the snapshot planes (snap_plane[f]).  The shot's first
+    // column is off / ldz.  err receives 1 if a tile load never completed.
+    int tma;
+    int nb_plane[5];
+    int snap_plane[2];
+    int *err;
+    CUtensorMap tm[3];  // 128-byte aligned by its type
 };
 
 constexpr float SNAP_Q = 16384.0f;  // FP16 snapshot full scale (2^14, headroom to 65504)

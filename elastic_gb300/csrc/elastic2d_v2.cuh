@@ -32,8 +32,51 @@ template <int TX>
 struct V2 {
     static constexpr int LX = TX + 2 * HALO;        // staged columns
     static constexpr int SIZE = V2_LZ * LX;         // floats per staged array
+    static constexpr int SIZEH = (SIZE + 63) / 64 * 64;  // halves per FP16 array (128-byte multiple)
     static constexpr int CHUNKS = (V2_LZ / 4) * LX; // 16-byte chunks per array
 };
+
+// Dynamic shared memory beyond the stages: 128 bytes of alignment slack (TMA
+// destinations are 128-byte aligned) and two mbarriers.
+constexpr int V2_SMEM_EXTRA = 128 + 16;
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"((unsigned)__cvta_generic_to_shared(bar)));
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Wait for phase `parity` of the barrier, giving up after about a second.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    const long long t0 = clock64();
+    while (true) {
+        unsigned done;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (clock64() - t0 > 2000000000LL) return false;
+    }
+}
+// One 3D tile load (coordinates c0 innermost) completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int c0, int c1, int c2,
+                                            unsigned long long *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+            "r"((unsigned)__cvta_generic_to_shared(dst)),
+        "l"(tm), "r"(c0), "r"(c1), "r"(c2), "r"((unsigned)__cvta_generic_to_shared(bar))
+        : "memory");
+}
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid)
 {
@@ -54,12 +97,6 @@ __device__ __forceinline__ unsigned long long l2_evict_last()
     unsigned long long p;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
     return p;
-}
-__device__ __forceinline__ void cp_async16_pol(void *smem, const void *gmem, bool valid, unsigned long long pol)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int n = valid ? 16 : 0;
-    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2, %3;\n" ::"r"(s), "l"(gmem), "r"(n), "l"(pol));
 }
 __device__ __forceinline__ float4 ldg4_pol(const float *p, unsigned long long pol)
 {
@@ -199,12 +236,13 @@ struct V2Arr {
 };
 
 // Shared memory of one stage of a v2 launch: NRAW float arrays (+ 2 FP16
-// snapshot arrays for fused imaging, stored as halves).
+// snapshot arrays for fused imaging, stored as halves); a multiple of 128
+// bytes.
 template <bool ADJ, bool EXACT, int TX>
 __host__ __device__ constexpr size_t v2_smem(bool img)
 {
     return (size_t)V2Arr<ADJ, EXACT>::NRAW * V2<TX>::SIZE * sizeof(float) +
-           (ADJ && img ? (size_t)2 * V2<TX>::SIZE * sizeof(__half) : 0);
+           (ADJ && img ? (size_t)2 * V2<TX>::SIZEH * sizeof(__half) : 0);
 }
 
 template <typename V>
@@ -214,7 +252,7 @@ __device__ __forceinline__ float4 ld_f4(const V *p) { return *reinterpret_cast<c
 template <int TX>
 __device__ __forceinline__ float4 ldh4(const __half *smh, int arr, int x, int z)
 {
-    const uint2 u = *reinterpret_cast<const uint2 *>(smh + arr * V2<TX>::SIZE + (x + HALO) * V2_LZ + (z + V2_ZH));
+    const uint2 u = *reinterpret_cast<const uint2 *>(smh + arr * V2<TX>::SIZEH + (x + HALO) * V2_LZ + (z + V2_ZH));
     const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
     const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
     return make_float4(a.x, a.y, b.x, b.y);
@@ -222,7 +260,8 @@ __device__ __forceinline__ float4 ldh4(const __half *smh, int arr, int x, int z)
 
 // Issue the cp.async staging of work item t into the stage at `sm`.
 template <bool ADJ, int TX>
-__device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, float *sm, bool img, unsigned long long keep)
+__device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, float *sm, bool img, unsigned long long keep,
+                                         unsigned long long *bar)
 {
     constexpr int NRAW = V2Arr<ADJ, false>::NRAW;
     constexpr int SZ = V2<TX>::SIZE;
@@ -232,6 +271,27 @@ __device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, floa
     const int lt = t - g.tile0;
     const int tz0 = (lt % g.ntz) * V2_TZ, tx0 = (lt / g.ntz) * TX;
     const int nz = g.nz, nx = g.nx, ldz = a.ldz;
+    if (a.tma) {
+        // one thread stages the whole tile: zeros outside the tensors come
+        // from the hardware fill, zeros across shot edges from the engine's
+        // guard columns
+        if (threadIdx.x == 0) {
+            const int c0 = tz0 - V2_ZH, c1 = (int)(g.off / ldz) + tx0 - HALO;
+            constexpr unsigned FB = V2_LZ * V2<TX>::LX * 4, HB = V2_LZ * V2<TX>::LX * 2;
+            mbar_expect_tx(bar, 5 * FB + (ADJ ? 5 * FB + (img ? 2 * HB : 0) : 0));
+#pragma unroll
+            for (int f = 0; f < 5; f++) tma_load_3d(sm + f * SZ, &a.tm[0], c0, c1, a.nb_plane[f], bar);
+            if (ADJ) {
+#pragma unroll
+                for (int f = 0; f < 5; f++) tma_load_3d(sm + (5 + f) * SZ, &a.tm[1], c0, c1, f, bar);
+                if (img) {
+                    tma_load_3d(smh, &a.tm[2], c0, c1, a.snap_plane[0], bar);
+                    tma_load_3d(smh + V2<TX>::SIZEH, &a.tm[2], c0, c1, a.snap_plane[1], bar);
+                }
+            }
+        }
+        return;
+    }
     for (int c = threadIdx.x; c < V2<TX>::CHUNKS; c += blockDim.x) {
         const int col = c / (V2_LZ / 4), zc = c - col * (V2_LZ / 4);
         const int gx = tx0 - HALO + col, gz = tz0 - V2_ZH + 4 * zc;
@@ -242,11 +302,11 @@ __device__ __forceinline__ void v2_stage(const Step2DArgs<float> &a, int t, floa
         for (int f = 0; f < 5; f++) cp_async16(sm + f * SZ + so, a.nb[f] + o, ok);
         if (ADJ) {
 #pragma unroll
-            for (int f = 0; f < 5; f++) cp_async16_pol(sm + (5 + f) * SZ + so, a.coef[f] + o, ok, keep);
+            for (int f = 0; f < 5; f++) cp_async16(sm + (5 + f) * SZ + so, a.coef[f] + o, ok);
             if (img) {
                 const bool oks = ok & (gz < nz);
                 cp_async8(smh + so, a.isnap0[0] + o, oks);
-                cp_async8(smh + SZ + so, a.isnap0[1] + o, oks);
+                cp_async8(smh + V2<TX>::SIZEH + so, a.isnap0[1] + o, oks);
             }
         }
     }
@@ -262,21 +322,34 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
     const int cw = TX * 32 / (int)blockDim.x;  // columns per warp (blockDim.x = 32 * TX / cw)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool img = ADJ && a.img[0] != nullptr;
-    // one or two stages, depending on the shared memory this launch received
+    // one or two stages, depending on the shared memory this launch received;
+    // stages start on a 128-byte boundary, the two mbarriers follow them
     unsigned dyn;
     asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
     const size_t stage_bytes = v2_smem<ADJ, EXACT, TX>(img);
     const unsigned long long keep = l2_evict_last();
-    const bool dbuf = dyn >= 2 * stage_bytes;
-    auto stage = [&](int k) { return reinterpret_cast<float *>(smem_raw + (k ? stage_bytes : 0)); };
+    const bool dbuf = dyn >= 2 * stage_bytes + V2_SMEM_EXTRA;
+    unsigned char *base = smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u);
+    auto stage = [&](int k) { return reinterpret_cast<float *>(base + (k ? stage_bytes : 0)); };
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(base + (dbuf ? 2 : 1) * stage_bytes);
+    const bool tma = a.tma != 0;
+    unsigned phase = 0;  // bit k: parity of the next completion of bars[k]
+    if (tma) {
+        if (threadIdx.x == 0) {
+            mbar_init(&bars[0]);
+            mbar_init(&bars[1]);
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
+        __syncthreads();
+    }
 
     int cur = 0;
-    if (blockIdx.x < a.ntiles) v2_stage<ADJ, TX>(a, blockIdx.x, stage(0), img, keep);
+    if (blockIdx.x < a.ntiles) v2_stage<ADJ, TX>(a, blockIdx.x, stage(0), img, keep, &bars[0]);
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
         float *sm = stage(cur);
         __half *smh = reinterpret_cast<__half *>(sm + NRAW * SZ);
-        if (dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(cur ^ 1), img, keep);
+        if (dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(cur ^ 1), img, keep, &bars[cur ^ 1]);
         const int s = find_shot<float>(a.shots, a.nshots, t);
         const ShotGeom g = a.shots[s];
         const int lt = t - g.tile0;
@@ -313,12 +386,21 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
             return true;
         };
         bool have = fetch(0);
-        if (dbuf && tn < a.ntiles) {
-            asm volatile("cp.async.wait_group 1;\n" ::);
+        if (tma) {
+            const bool ok = mbar_wait(&bars[cur], (phase >> cur) & 1u);
+            phase ^= 1u << cur;
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+                return;
+            }
         } else {
-            asm volatile("cp.async.wait_group 0;\n" ::);
+            if (dbuf && tn < a.ntiles) {
+                asm volatile("cp.async.wait_group 1;\n" ::);
+            } else {
+                asm volatile("cp.async.wait_group 0;\n" ::);
+            }
+            __syncthreads();
         }
-        __syncthreads();
         if (ADJ && !EXACT) {
             // products coef*field in place (slots 0..6 of the 10 raw arrays),
             // four elements per 128-bit shared access
@@ -623,9 +705,12 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
                 atomic_max_abs(a.snap_max_out + 2 * s + 1, wmax1);
             }
         }
-        __syncthreads();  // the stage is free for the prefetch of the next iteration
+        // the stage is free for the next tile's loads (generic-proxy writes
+        // to it, the adjoint's products, are ordered before async-proxy ones)
+        if (tma) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
         cur ^= dbuf ? 1 : 0;
-        if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img, keep);
+        if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img, keep, &bars[0]);
     }
 }
 

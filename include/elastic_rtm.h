@@ -273,7 +273,7 @@ rtm_batch *rtm_batch_create(int nz, int nx, int nt, float dx, float dt, float fp
  * host pointers. */
 int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, int traces_on_device, float *image,
                       int image_on_device);
-/* out[0..42] (pass an array of at least 43 doubles): forward ms, adjoint
+/* out[0..43] (pass an array of at least 44 doubles): forward ms, adjoint
  * ms, cells of the last group, kernels launched, total ms of the last call,
  * forward tile width, forward work items, adjoint tile width; [8..13] the
  * autotuner's best ms per step for tile widths 8, 16, 32 (forward, then
@@ -282,7 +282,7 @@ int rtm_batch_migrate(rtm_batch *b, int shot0, int nshot, const float *traces, i
  * (8, 16, 32) and launch shape (1 stage, 2 stages, each with 256 then 512
  * threads), forward then adjoint, -1 where a shape does not fit in a block;
  * [40..41] threads per CTA of the forward and adjoint pass; [42] checkpoint
- * interval (0 = every level's snapshots kept). */
+ * interval (0 = every level's snapshots kept); [43] 1 with TMA staging. */
 int rtm_batch_stats(const rtm_batch *b, double *out);
 /* Autotuner: times `steps` launches of each pass for every tile width and
  * staging depth on the geometry of shots [shot0, shot0+nshot) and keeps the
@@ -306,6 +306,13 @@ int rtm_batch_set_stages(rtm_batch *b, int fwd, int adj, int threads_fwd, int th
  * k ~ sqrt(10 nt) by itself when every level's snapshots would not fit in 80 %
  * of the free device memory.  out[42] of rtm_batch_stats reports k. */
 int rtm_batch_set_checkpoint(rtm_batch *b, int interval);
+/* on=1 (the default): the step kernels stage their tiles with
+ * tensor-memory-access bulk loads (one thread per tile, completion on a
+ * shared-memory barrier with a time limit; a load that does not complete
+ * fails the call with status 4); on=0: per-thread asynchronous copies.
+ * Results are bit-identical.  out[43] of rtm_batch_stats reports the
+ * setting. */
+int rtm_batch_set_tma(rtm_batch *b, int on);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */
 void *rtm_host_alloc(size_t bytes);

@@ -165,3 +165,37 @@ def test_batch_checkpoint_restart_is_bit_identical(interval):
     assert st0["checkpoint"] == 0 and st["checkpoint"] == interval
     np.testing.assert_array_equal(img, ref)
     assert np.abs(ref).max() > 0
+
+
+@pytest.mark.parametrize("tile,stages,interval", [(8, (1, 1), 0), (16, (2, 2), 0), (8, (2, 1), 7), (32, (1, 1), 0)])
+def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
+    """Staging the step tiles with tensor-memory-access loads (zeros from the
+    hardware fill and the guard columns) gives the images of the per-thread
+    asynchronous copies bit for bit, with one or two staging buffers and in
+    checkpoint-restart mode; most CTAs walk several work items (nz 700)."""
+    nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 700, 700, 40, 10.0, 1e-3, 30.0, 20, 8, 8, 20
+    rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=11, spacing=200, wmin=150,
+                                                 wmax=260)
+
+    def run(tma):
+        n = len(nxs)
+        eng = BatchRTM(nz, nx, nt, dx, dt, fp, abc, rho, lam, mu, x0, nxs, xsrc, np.full(n, zs), np.full(n, zr),
+                       comp_mask=3, group_max=3, nsource=ns)
+        eng.set_graph(True, tile)
+        eng.set_stages(*stages)
+        if interval:
+            eng.set_checkpoint(interval)
+        eng.set_tma(tma)
+        image = np.zeros(3 * nz * nx, np.float32)
+        for s0, g in eng.groups():
+            flat = np.concatenate([np.concatenate([traces[s][c].ravel() for c in range(2)]) for s in range(s0, s0 + g)])
+            eng.migrate(s0, g, flat, image)
+        st = eng.stats()
+        eng.close()
+        return image, st
+
+    ref, st0 = run(False)
+    img, st = run(True)
+    assert st["tma"] and not st0["tma"]
+    np.testing.assert_array_equal(img, ref)
+    assert np.abs(ref).max() > 0
