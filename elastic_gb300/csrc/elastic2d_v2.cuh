@@ -705,9 +705,10 @@ __global__ void __launch_bounds__(v2_max_threads(EXACT)) k_step2d_v2(const __gri
                 atomic_max_abs(a.snap_max_out + 2 * s + 1, wmax1);
             }
         }
-        // the stage is free for the next tile's loads (generic-proxy writes
-        // to it, the adjoint's products, are ordered before async-proxy ones)
-        if (tma) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        // the stage is free for the next tile's loads; the fast adjoint wrote
+        // its products into it, and those generic-proxy writes are ordered
+        // before the next async-proxy (TMA) writes
+        if (tma && ADJ && !EXACT) asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         cur ^= dbuf ? 1 : 0;
         if (!dbuf && tn < a.ntiles) v2_stage<ADJ, TX>(a, tn, stage(0), img, keep, &bars[0]);
