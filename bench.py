@@ -261,6 +261,8 @@ def run_gpu(args):
                    "group_shots": args.group, "checkpoint_interval": st["checkpoint"],
                    "tile_staging": "tensor-memory-access bulk loads" if st["tma"] else "per-thread cp.async",
                    "inputs_vs_l2": "inputs larger than L2 (snapshots or checkpoints ~100+ GB)",
+                   "forward_kernel": "marching strips (8-column chunks, 128 rows)" if st["march"] else "tiles",
+                   "autotune_ms_per_launch_fwd_marching": round(tune["tune_ms_march"], 4),
                    "tile": {"forward_tx": tune["tile_x"], "adjoint_tx": tune["tile_x_adj"], "tz": 128,
                             "forward_stages": tune["stages"], "adjoint_stages": tune["stages_adj"],
                             "forward_threads": tune["threads"], "adjoint_threads": tune["threads_adj"],

@@ -31,6 +31,7 @@
 #include "elastic2d_aux.cuh"
 #include "elastic2d_v2.cuh"
 #include "engine.h"
+#include "march2d.cuh"
 
 using namespace eg;
 
@@ -121,16 +122,16 @@ EncodeTiledFn encode_fn()
 }
 
 // 3D tensor map (ldz rows x cols columns x planes, plane stride plane_elems)
-// with the v2 step's tile box (V2_LZ rows x tx + 2*HALO columns x 1 plane)
+// with a box of box_rows rows x box_cols columns x 1 plane
 int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
-             long long plane_elems, int tx)
+             long long plane_elems, int box_rows, int box_cols)
 {
     EncodeTiledFn fn = encode_fn();
     RTM_CHECK_ARG(fn, "cuTensorMapEncodeTiled is not available from the driver");
     const cuuint64_t es = half ? 2 : 4;
     const cuuint64_t dims[3] = {(cuuint64_t)ldz, (cuuint64_t)cols, (cuuint64_t)planes};
     const cuuint64_t strides[2] = {(cuuint64_t)ldz * es, (cuuint64_t)plane_elems * es};
-    const cuuint32_t box[3] = {(cuuint32_t)V2_LZ, (cuuint32_t)(tx + 2 * HALO), 1};
+    const cuuint32_t box[3] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1};
     const cuuint32_t el[3] = {1, 1, 1};
     const CUresult r = fn(m, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                           const_cast<void *>(base), dims, strides, box, el, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -148,6 +149,56 @@ constexpr int IMG_FOLD = 32;
 // zero guard columns after every shot of a group: a halo read across a shot's
 // edge (5 columns) lands on zeros, so tile staging needs no per-shot masking
 constexpr int GUARD = 5;
+
+// Work of the marching forward kernel for `ctas` CTAs: the units (shot,
+// strip, 8-column chunk) in shot, strip, chunk order, each weighted by the
+// rows it stages plus a fixed share for its compute (a strip's partial last
+// rows still occupy every warp), cut into `ctas` contiguous pieces of equal
+// weight; a piece's units form runs of consecutive chunks of one strip.
+constexpr int M_UNIT_FIXED = 48;
+void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> &runs, std::vector<int> &lo)
+{
+    long long total = 0;
+    for (const HostShot &h : shots)
+        for (int t = 0; t * V2_TZ < h.nz; t++)
+            total += (long long)ceil_div(h.nx, MC) * (std::min(V2_TZ, h.nz - t * V2_TZ) + 2 * V2_ZH + M_UNIT_FIXED);
+    runs.clear();
+    lo.assign(ctas + 1, 0);
+    long long before = 0;
+    int cur = -1;
+    for (size_t s = 0; s < shots.size(); s++) {
+        const HostShot &h = shots[s];
+        const int nch = ceil_div(h.nx, MC);
+        for (int t = 0; t * V2_TZ < h.nz; t++) {
+            const int w = std::min(V2_TZ, h.nz - t * V2_TZ) + 2 * V2_ZH + M_UNIT_FIXED;
+            for (int k = 0; k < nch; k++) {
+                const int cta = (int)(before * ctas / total);
+                before += w;
+                if (cta != cur || runs.back().x != (int)s || runs.back().y != t * V2_TZ) {
+                    runs.push_back(make_int4((int)s, t * V2_TZ, k, k + 1));
+                    for (int c = cur + 1; c <= cta; c++) lo[c] = (int)runs.size() - 1;
+                    cur = cta;
+                } else {
+                    runs.back().w = k + 1;
+                }
+            }
+        }
+    }
+    for (int c = cur + 1; c <= ctas; c++) lo[c] = (int)runs.size();
+}
+
+int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaStream_t st)
+{
+    static bool init = false;
+    if (!init) {
+        RTM_CUDA(cudaFuncSetAttribute(k_fwd_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M_SMEM));
+        init = true;
+    }
+    RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0, "marching forward step: unsupported arguments");
+    k_fwd_march<<<ctas, M_THREADS, M_SMEM, st>>>(a, m);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
 
 }  // namespace
 
@@ -168,6 +219,13 @@ struct rtm_batch {
     int ckpt = 0;
     DevBuf<float> ck;
     bool use_tma = true;   // stage step tiles with tensor-memory-access loads
+    // forward pass by the marching kernel: -1 automatic (the autotuner's
+    // choice, on until it has run), 0 off, 1 on; needs tensor-map staging
+    int march = -1;
+    bool march_tuned = true;
+    double tune_march_ms = -1;
+    DevBuf<int4> mruns;
+    DevBuf<int> mlo;
     DevBuf<int> err;       // set by a step kernel whose tile load never completed
     DevBuf<int> dx0;
     ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
@@ -271,13 +329,32 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         if (!tma_on) return RTM_OK;
         const long long cols = b->cap_cols;
         const long long nlev = b->ckpt ? b->ckpt + 1 : nt;
-        TRY(make_map(&mF, b->F.p, false, ld, cols, 10, gp, txf));
-        TRY(make_map(&mA, b->A.p, false, ld, cols, 10, gp, txa));
-        TRY(make_map(&mC, b->coef.p, false, ld, cols, 5, gp, txa));
-        TRY(make_map(&mS, b->snaps.p, true, ld, cols, 2 * nlev, gp, txa));
+        TRY(make_map(&mF, b->F.p, false, ld, cols, 10, gp, V2_LZ, txf + 2 * HALO));
+        TRY(make_map(&mA, b->A.p, false, ld, cols, 10, gp, V2_LZ, txa + 2 * HALO));
+        TRY(make_map(&mC, b->coef.p, false, ld, cols, 5, gp, V2_LZ, txa + 2 * HALO));
+        TRY(make_map(&mS, b->snaps.p, true, ld, cols, 2 * nlev, gp, V2_LZ, txa + 2 * HALO));
         return RTM_OK;
     };
     TRY(build_maps(b->tab.tx, b->tab_a.tx));
+    // marching forward kernel: its run table and tensor maps
+    const int mctas = device_sm_count();
+    MarchArgs marg;
+    memset(&marg, 0, sizeof marg);
+    if (tma_on) {
+        std::vector<int4> runs;
+        std::vector<int> lo;
+        march_plan(b->tab.shots, mctas, runs, lo);
+        TRY(b->mruns.alloc(runs.size()));
+        TRY(b->mlo.alloc(lo.size()));
+        RTM_CUDA(cudaMemcpy(b->mruns.p, runs.data(), runs.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        RTM_CUDA(cudaMemcpy(b->mlo.p, lo.data(), lo.size() * sizeof(int), cudaMemcpyHostToDevice));
+        marg.runs = b->mruns.p;
+        marg.run_lo = b->mlo.p;
+        TRY(make_map(&marg.tm_nb, b->F.p, false, ld, b->cap_cols, 10, gp, V2_LZ, MC));
+        TRY(make_map(&marg.tm_own, b->F.p, false, ld, b->cap_cols, 10, gp, V2_TZ, MC));
+        TRY(make_map(&marg.tm_coef, b->coef.p, false, ld, b->cap_cols, 5, gp, V2_TZ, MC));
+    }
+    const bool use_march = tma_on && (b->march == 1 || (b->march < 0 && b->march_tuned));
     // ---- coefficients of every shot's subgrid (guard columns and columns of
     // the previous group's shots are zero)
     RTM_CUDA(cudaMemsetAsync(b->coef.p, 0, 5 * gp * sizeof(float), st));
@@ -427,6 +504,36 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                     b->tune_ms[pass][ci][var] = ms / tune_steps;
                     if (ms < best) { best = ms; bx = cand[ci]; bs = ns_; bt = nth; }
                 }
+            if (pass == 0 && tma_on) {
+                // the marching forward kernel on the same levels
+                for (int rep = 0; rep < 2; rep++) {
+                    RTM_CUDA(cudaEventRecord(t0, st));
+                    for (int k = 0; k < tune_steps; k++) {
+                        const int L = 3 + (k & 1);
+                        Step2DArgs<float> a = base_args(false);
+                        MarchArgs m = marg;
+                        for (int f = 0; f < 5; f++) {
+                            a.out[f] = fb(L & 1, f);
+                            a.own2[f] = a.out[f];
+                            a.nb[f] = fb((L + 1) & 1, f);
+                            a.nb_plane[f] = ((L + 1) & 1) * 5 + f;
+                            m.own_plane[f] = (L & 1) * 5 + f;
+                        }
+                        a.sponge = 1;
+                        a.snap_out[0] = snap(1, 0);
+                        a.snap_out[1] = snap(1, 1);
+                        a.snap_max_in = mx(1);
+                        a.snap_max_out = mx(2);
+                        TRY(launch_march(a, m, mctas, st));
+                    }
+                    RTM_CUDA(cudaEventRecord(t1, st));
+                    RTM_CUDA(cudaEventSynchronize(t1));
+                }
+                float ms = 0;
+                RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+                b->tune_march_ms = ms / tune_steps;
+                b->march_tuned = ms < best;
+            }
             if (pass) { b->st_a = bs; b->th_a = bt; } else { b->st_f = bs; b->th_f = bt; }
             if (pass) b->tx_a = bx; else b->tx_f = bx;
         }
@@ -457,7 +564,13 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         a.snap_out[1] = snap(L - 1, 1);
         a.snap_max_in = mx(L - 1);
         a.snap_max_out = mx(L);
-        TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
+        if (use_march) {
+            MarchArgs m = marg;
+            for (int f = 0; f < 5; f++) m.own_plane[f] = (L & 1) * 5 + f;
+            TRY(launch_march(a, m, mctas, st));
+        } else {
+            TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
+        }
         nkern++;
         return RTM_OK;
     };
@@ -786,6 +899,8 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[41] = b->th_a;
     out[42] = b->ckpt;
     out[43] = b->use_tma ? 1 : 0;
+    out[44] = b->use_tma && (b->march == 1 || (b->march < 0 && b->march_tuned)) ? 1 : 0;
+    out[45] = b->tune_march_ms;
     return RTM_OK;
 }
 
@@ -803,6 +918,13 @@ extern "C" int rtm_batch_set_tma(rtm_batch *b, int on)
     RTM_CHECK_ARG(b, "null argument");
     if (on) RTM_CHECK_ARG(encode_fn() != nullptr, "tensor maps are not available from the driver");
     b->use_tma = on != 0;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_set_march(rtm_batch *b, int mode)
+{
+    RTM_CHECK_ARG(b && mode >= -1 && mode <= 1, "mode must be -1, 0 or 1");
+    b->march = mode;
     return RTM_OK;
 }
 
@@ -845,6 +967,8 @@ extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
     b->tx_f = b->tx_a = 0;
     b->st_f = b->st_a = 1;
     b->th_f = b->th_a = 256;
+    b->march_tuned = true;
+    b->tune_march_ms = -1;
     // traces are not read during tuning beyond the receiver row; use the
     // staging buffer content as is
     TRY(batch_group(b, shot0, nshot, b->tstage.p, 1, b->full.p, 1, steps));

@@ -199,3 +199,43 @@ def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
     assert st["tma"] and not st0["tma"]
     np.testing.assert_array_equal(img, ref)
     assert np.abs(ref).max() > 0
+
+
+@pytest.mark.parametrize("nz,nx,nt,interval", [(40, 180, 60, 0), (300, 900, 40, 0), (700, 700, 40, 7)])
+def test_batch_marching_forward_is_bit_identical(nz, nx, nt, interval):
+    """The forward pass by the marching kernel (one CTA per SM walking
+    128-row strips in 8-column chunks through a ring of staged columns)
+    gives the tile kernel's images bit for bit: one strip narrower than the
+    grid of CTAs, several strips with a partial last one, checkpoint-restart
+    mode; the autotuner times it beside the tile variants."""
+    dx, dt, fp, abc, zs, zr, ns = 10.0, 1e-3, 30.0, 20 if nz > 100 else 10, 8, 8, 20
+    wmin, wmax, spacing = (50, 96, 24) if nx < 300 else (150, 400, 200)
+    rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=13, spacing=spacing, wmin=wmin,
+                                                 wmax=wmax)
+
+    def run(march, tune=False):
+        n = len(nxs)
+        eng = BatchRTM(nz, nx, nt, dx, dt, fp, abc, rho, lam, mu, x0, nxs, xsrc, np.full(n, zs), np.full(n, zr),
+                       comp_mask=3, group_max=3, nsource=ns)
+        if interval:
+            eng.set_checkpoint(interval)
+        if tune:
+            eng.autotune(0, 3, steps=2)
+        eng.set_march(march)
+        image = np.zeros(3 * nz * nx, np.float32)
+        for s0, g in eng.groups():
+            flat = np.concatenate([np.concatenate([traces[s][c].ravel() for c in range(2)]) for s in range(s0, s0 + g)])
+            eng.migrate(s0, g, flat, image)
+        st = eng.stats()
+        eng.close()
+        return image, st
+
+    ref, st0 = run(0)
+    img, st = run(1)
+    assert st["march"] and not st0["march"]
+    np.testing.assert_array_equal(img, ref)
+    assert np.abs(ref).max() > 0
+    if nz == 300:
+        img, st = run(-1, tune=True)
+        assert st["tune_ms_march"] > 0
+        np.testing.assert_array_equal(img, ref)
