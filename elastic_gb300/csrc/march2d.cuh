@@ -90,8 +90,8 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
 // Rank of field f among the recorded components (its trace slot).
 __device__ __forceinline__ int rec_slot(int mask, int f) { return __popc(mask & ((1 << f) - 1)); }
 
-// 17 warps x 120 registers fit one SM's register file
-__global__ void __maxnreg__(120) k_fwd_march(const __grid_constant__ Step2DArgs<float> a, const __grid_constant__ MarchArgs m)
+// 17 warps put five on one SM sub-partition: at most 96 registers a thread
+__global__ void __launch_bounds__(M_THREADS, 1) k_fwd_march(const __grid_constant__ Step2DArgs<float> a, const __grid_constant__ MarchArgs m)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *ring = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
