@@ -151,17 +151,15 @@ constexpr int IMG_FOLD = 32;
 constexpr int GUARD = 5;
 
 // Work of the marching forward kernel for `ctas` CTAs: the units (shot,
-// strip, 8-column chunk) in shot, strip, chunk order, each weighted by the
-// rows it stages plus a fixed share for its compute (a strip's partial last
-// rows still occupy every warp), cut into `ctas` contiguous pieces of equal
-// weight; a piece's units form runs of consecutive chunks of one strip.
-constexpr int M_UNIT_FIXED = 48;
+// strip, 8-column chunk) in shot, strip, chunk order, cut into `ctas`
+// contiguous pieces of equal length; a piece's units form runs of
+// consecutive chunks of one strip.  Units weigh the same whatever their
+// strip's depth: a partial last strip moves fewer bytes but keeps every warp
+// issuing the full chunk's instructions.
 void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> &runs, std::vector<int> &lo)
 {
     long long total = 0;
-    for (const HostShot &h : shots)
-        for (int t = 0; t * V2_TZ < h.nz; t++)
-            total += (long long)ceil_div(h.nx, MC) * (std::min(V2_TZ, h.nz - t * V2_TZ) + 2 * V2_ZH + M_UNIT_FIXED);
+    for (const HostShot &h : shots) total += (long long)ceil_div(h.nx, MC) * ceil_div(h.nz, V2_TZ);
     runs.clear();
     lo.assign(ctas + 1, 0);
     long long before = 0;
@@ -169,11 +167,9 @@ void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> 
     for (size_t s = 0; s < shots.size(); s++) {
         const HostShot &h = shots[s];
         const int nch = ceil_div(h.nx, MC);
-        for (int t = 0; t * V2_TZ < h.nz; t++) {
-            const int w = std::min(V2_TZ, h.nz - t * V2_TZ) + 2 * V2_ZH + M_UNIT_FIXED;
-            for (int k = 0; k < nch; k++) {
+        for (int t = 0; t * V2_TZ < h.nz; t++)
+            for (int k = 0; k < nch; k++, before++) {
                 const int cta = (int)(before * ctas / total);
-                before += w;
                 if (cta != cur || runs.back().x != (int)s || runs.back().y != t * V2_TZ) {
                     runs.push_back(make_int4((int)s, t * V2_TZ, k, k + 1));
                     for (int c = cur + 1; c <= cta; c++) lo[c] = (int)runs.size() - 1;
@@ -182,7 +178,6 @@ void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> 
                     runs.back().w = k + 1;
                 }
             }
-        }
     }
     for (int c = cur + 1; c <= ctas; c++) lo[c] = (int)runs.size();
 }
