@@ -263,6 +263,8 @@ def run_gpu(args):
                    "inputs_vs_l2": "inputs larger than L2 (snapshots or checkpoints ~100+ GB)",
                    "forward_kernel": "marching strips (8-column chunks, 128 rows)" if st["march"] else "tiles",
                    "autotune_ms_per_launch_fwd_marching": round(tune["tune_ms_march"], 4),
+                   "adjoint_kernel": "marching strips (8-column chunks, 128 rows)" if st["march_adj"] else "tiles",
+                   "autotune_ms_per_launch_adj_marching": round(tune["tune_ms_march_adj"], 4),
                    "tile": {"forward_tx": tune["tile_x"], "adjoint_tx": tune["tile_x_adj"], "tz": 128,
                             "forward_stages": tune["stages"], "adjoint_stages": tune["stages_adj"],
                             "forward_threads": tune["threads"], "adjoint_threads": tune["threads_adj"],

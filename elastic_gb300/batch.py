@@ -50,6 +50,7 @@ class BatchRTM:
                     tune_ms_fwd=list(out[8:11]), tune_ms_adj=list(out[11:14]),
                     stages=int(out[14]), stages_adj=int(out[15]), threads=int(out[40]), threads_adj=int(out[41]),
                     checkpoint=int(out[42]), tma=bool(out[43]), march=bool(out[44]), tune_ms_march=out[45],
+                    march_adj=bool(out[46]), tune_ms_march_adj=out[47],
                     # per tile width 8, 16, 32: [1 stage, 2 stages, 1 stage 512 threads, 2 stages 512 threads]
                     tune_ms_fwd_variants=[list(out[16 + 4 * i:20 + 4 * i]) for i in range(3)],
                     tune_ms_adj_variants=[list(out[28 + 4 * i:32 + 4 * i]) for i in range(3)])
@@ -77,8 +78,9 @@ class BatchRTM:
         check(load().rtm_batch_set_tma(self.h, int(bool(on))))
 
     def set_march(self, mode):
-        """Forward pass by the marching kernel: -1 the autotuner's choice (on
-        until autotune has run), 0 the tile kernel, 1 the marching kernel."""
+        """Forward and adjoint passes by the marching kernels: -1 the
+        autotuner's choice per pass (on until autotune has run), 0 the tile
+        kernels, 1 the marching kernels."""
         check(load().rtm_batch_set_march(self.h, int(mode)))
 
     def set_checkpoint(self, interval):

@@ -195,6 +195,20 @@ int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaS
     return RTM_OK;
 }
 
+int launch_march_adj(const Step2DArgs<float> &a, const MarchAdjArgs &m, int ctas, cudaStream_t st)
+{
+    static bool init = false;
+    if (!init) {
+        RTM_CUDA(cudaFuncSetAttribute(k_adj_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MA_SMEM));
+        init = true;
+    }
+    RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0 && a.img[0] && !a.imgc[0],
+                  "marching adjoint step: unsupported arguments");
+    k_adj_march<<<ctas, M_THREADS, MA_SMEM, st>>>(a, m);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
 }  // namespace
 
 struct rtm_batch {
@@ -217,8 +231,8 @@ struct rtm_batch {
     // forward pass by the marching kernel: -1 automatic (the autotuner's
     // choice, on until it has run), 0 off, 1 on; needs tensor-map staging
     int march = -1;
-    bool march_tuned = true;
-    double tune_march_ms = -1;
+    bool march_tuned = true, march_tuned_a = true;  // per pass
+    double tune_march_ms = -1, tune_march_ms_a = -1;
     DevBuf<int4> mruns;
     DevBuf<int> mlo;
     DevBuf<int> err;       // set by a step kernel whose tile load never completed
@@ -349,7 +363,18 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         TRY(make_map(&marg.tm_own, b->F.p, false, ld, b->cap_cols, 10, gp, V2_TZ, MC));
         TRY(make_map(&marg.tm_coef, b->coef.p, false, ld, b->cap_cols, 5, gp, V2_TZ, MC));
     }
+    MarchAdjArgs madj;
+    memset(&madj, 0, sizeof madj);
+    if (tma_on) {
+        madj.runs = marg.runs;
+        madj.run_lo = marg.run_lo;
+        const long long nlev = b->ckpt ? b->ckpt + 1 : nt;
+        TRY(make_map(&madj.tm_nb, b->A.p, false, ld, b->cap_cols, 10, gp, V2_LZ, MC));
+        TRY(make_map(&madj.tm_coef, b->coef.p, false, ld, b->cap_cols, 5, gp, V2_LZ, MC));
+        TRY(make_map(&madj.tm_snap, b->snaps.p, true, ld, b->cap_cols, 2 * nlev, gp, V2_LZ, MC));
+    }
     const bool use_march = tma_on && (b->march == 1 || (b->march < 0 && b->march_tuned));
+    const bool use_march_a = tma_on && (b->march == 1 || (b->march < 0 && b->march_tuned_a));
     // ---- coefficients of every shot's subgrid (guard columns and columns of
     // the previous group's shots are zero)
     RTM_CUDA(cudaMemsetAsync(b->coef.p, 0, 5 * gp * sizeof(float), st));
@@ -529,6 +554,35 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                 b->tune_march_ms = ms / tune_steps;
                 b->march_tuned = ms < best;
             }
+            if (pass == 1 && tma_on) {
+                // the marching adjoint kernel on the same levels
+                for (int rep = 0; rep < 2; rep++) {
+                    RTM_CUDA(cudaEventRecord(t0, st));
+                    for (int k = 0; k < tune_steps; k++) {
+                        const int L = 3 + (k & 1);
+                        Step2DArgs<float> a = base_args(true);
+                        for (int f = 0; f < 5; f++) {
+                            a.out[f] = ab(L & 1, f);
+                            a.own2[f] = a.out[f];
+                            a.nb[f] = ab((L + 1) & 1, f);
+                            a.nb_plane[f] = ((L + 1) & 1) * 5 + f;
+                        }
+                        a.snap_plane[0] = 2 * slot(1);
+                        a.snap_plane[1] = 2 * slot(1) + 1;
+                        a.rec = b->traces.p; a.comp_mask = b->comp_mask; a.ncomp = b->ncomp; a.it = 0;
+                        a.isnap0[0] = snap(1, 0); a.isnap0[1] = snap(1, 1); a.imax0 = mx(1);
+                        a.isnap1[0] = snap(2, 0); a.isnap1[1] = snap(2, 1); a.imax1 = mx(2);
+                        set_img(a);
+                        TRY(launch_march_adj(a, madj, mctas, st));
+                    }
+                    RTM_CUDA(cudaEventRecord(t1, st));
+                    RTM_CUDA(cudaEventSynchronize(t1));
+                }
+                float ms = 0;
+                RTM_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+                b->tune_march_ms_a = ms / tune_steps;
+                b->march_tuned_a = ms < best;
+            }
             if (pass) { b->st_a = bs; b->th_a = bt; } else { b->st_f = bs; b->th_f = bt; }
             if (pass) b->tx_a = bx; else b->tx_f = bx;
         }
@@ -618,7 +672,11 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         a.isnap1[1] = L < nt ? snap(L + 1, 1) : snap(L, 1);
         a.imax1 = L < nt ? mx(L + 1) : mx(L);
         set_img(a);
-        TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
+        if (use_march_a) {
+            TRY(launch_march_adj(a, madj, mctas, st));
+        } else {
+            TRY(launch_step<float>(a, true, false, b->tab_a.tx, 0, st, b->tab_a.tz, sta, tha));
+        }
         nkern++;
         if (blocked && ((nt - L + 1) % IMG_FOLD == 0 || L == 1)) {
             TRY(fold());
@@ -896,6 +954,8 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[43] = b->use_tma ? 1 : 0;
     out[44] = b->use_tma && (b->march == 1 || (b->march < 0 && b->march_tuned)) ? 1 : 0;
     out[45] = b->tune_march_ms;
+    out[46] = b->use_tma && (b->march == 1 || (b->march < 0 && b->march_tuned_a)) ? 1 : 0;
+    out[47] = b->tune_march_ms_a;
     return RTM_OK;
 }
 
@@ -962,8 +1022,8 @@ extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
     b->tx_f = b->tx_a = 0;
     b->st_f = b->st_a = 1;
     b->th_f = b->th_a = 256;
-    b->march_tuned = true;
-    b->tune_march_ms = -1;
+    b->march_tuned = b->march_tuned_a = true;
+    b->tune_march_ms = b->tune_march_ms_a = -1;
     // traces are not read during tuning beyond the receiver row; use the
     // staging buffer content as is
     TRY(batch_group(b, shot0, nshot, b->tstage.p, 1, b->full.p, 1, steps));

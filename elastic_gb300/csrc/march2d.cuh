@@ -342,4 +342,399 @@ __global__ void __launch_bounds__(M_THREADS, 1) k_fwd_march(const __grid_constan
     }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint step with the fused imaging condition, by marching z-strips (fast
+// arithmetic, FP32 partial image planes; same per-cell arithmetic as
+// k_step2d_v2's fast adjoint).
+//
+// The adjoint stencils read the seven coefficient x field products of the
+// level above at x and z offsets up to 5, so the CTA keeps those products in
+// a ring of 32 columns (4 chunks) and the level's FP16 source snapshots in a
+// second ring.  A producer warp loads, per chunk, the raw fields and
+// coefficients (144 rows x 8 columns each) into one landing slot and the
+// snapshots straight into their ring; the sixteen compute warps turn the
+// landing slot into products one chunk ahead of need, then update the
+// chunk's cells (warps 0-7 the velocities and the Vx/Vz image, warps 8-15 the
+// stresses and the lambda/mu images).  Own fields, next-level snapshots and
+// image partials are read from global memory, issued before the wait.
+//
+//   products ring [7][32 columns][144 rows] floats  129,024 B
+//   snapshot ring [2][32 columns][144 rows] halves   18,432 B
+//   landing slot  [10][8 columns][144 rows] floats   46,080 B
+//
+// Order (per run of n chunks k0 .. k0+n-1): product passes of chunks k0-1,
+// k0, k0+1, then for each chunk k: wait until every warp has its products
+// through chunk k+1 (pd), compute k, signal (cd), and -- once chunk k-1 is
+// computed by every warp -- the product pass of chunk k+2 into the slot of
+// chunk k-2.  The producer refills the landing slot once every warp has
+// turned it into products, and starts a run only after every chunk of the
+// previous one is computed (rdone).
+struct MarchAdjArgs {
+    const int4 *runs;
+    const int *run_lo;
+    CUtensorMap tm_nb;    // adjoint level planes, box {144 rows, 8 columns, 1}
+    CUtensorMap tm_coef;  // coefficient planes, box {144 rows, 8 columns, 1}
+    CUtensorMap tm_snap;  // FP16 snapshot planes, box {144 rows, 8 columns, 1}
+};
+
+constexpr int MA_PROD = 7 * MRING * V2_LZ;  // floats
+constexpr int MA_SNAP = 2 * MRING * V2_LZ;  // halves
+constexpr int MA_LAND = 10 * MC * V2_LZ;    // floats
+constexpr size_t MA_SMEM = (size_t)MA_PROD * 4 + (size_t)MA_SNAP * 2 + (size_t)MA_LAND * 4 + 128 + 64;
+
+// 4 halves of snapshot ring field f at shot column col, rows z..z+3
+__device__ __forceinline__ float4 rh4(const __half *ring, int f, int col, int z)
+{
+    const uint2 u = *reinterpret_cast<const uint2 *>(ring + f * (MRING * V2_LZ) + (col & (MRING - 1)) * V2_LZ + z + V2_ZH);
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+// adj_fast_x4 on the products ring
+template <bool PTYPE>
+__device__ __forceinline__ void madj_x4(const float *ring, int pa, int x, int z, float v[4])
+{
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int op = PTYPE ? -4 + k : -5 + k, om = PTYPE ? 5 - k : 4 - k;
+        const float4 a = rl4(ring, pa, x + op, z), b = rl4(ring, pa, x + om, z);
+        const float c = StagCoef<float>::c(k);
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = v[j] + c * (f4(a, j) - f4(b, j));
+    }
+}
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(n) : "memory"); }
+
+__global__ void __launch_bounds__(M_THREADS, 1)
+    k_adj_march(const __grid_constant__ Step2DArgs<float> a, const __grid_constant__ MarchAdjArgs m)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *prod = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
+    __half *snap = reinterpret_cast<__half *>(prod + MA_PROD);
+    float *land = reinterpret_cast<float *>(snap + MA_SNAP);
+    unsigned long long *lfull = reinterpret_cast<unsigned long long *>(land + MA_LAND);
+    unsigned long long *pd = lfull + 1, *cd = lfull + 3, *rdone = lfull + 5;
+    const int r0 = m.run_lo[blockIdx.x], r1 = m.run_lo[blockIdx.x + 1];
+    if (r0 >= r1) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(lfull);
+        for (int q = 0; q < 2; q++) {
+            mbar_init_n(&pd[q], M_CONSUMERS);
+            mbar_init_n(&cd[q], M_CONSUMERS);
+        }
+        mbar_init_n(rdone, M_CONSUMERS);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    auto fail = [&]() {
+        if (lane == 0 && a.err) atomicExch(a.err, 1);
+    };
+
+    if (warp == M_CONSUMERS) {
+        // ---- producer: landing group P = product pass P of this CTA's walk
+        if (lane != 0) return;
+        constexpr unsigned NB_BYTES = V2_LZ * MC * 4, SN_BYTES = V2_LZ * MC * 2;
+        int P = 0;
+        for (int r = r0; r < r1; r++) {
+            const int4 R = m.runs[r];
+            const int col0 = (int)(a.shots[R.x].off / a.ldz), n = R.w - R.z;
+            if (r > r0 && !mbar_wait(rdone, (r - r0 - 1) & 1)) return fail();
+            for (int pl = 0; pl <= n + 1; pl++, P++) {
+                const int j = R.z - 1 + pl;
+                if (P > 0 && !mbar_wait(&pd[(P - 1) & 1], ((P - 1) >> 1) & 1)) return fail();
+                mbar_expect_tx(lfull, 10u * NB_BYTES + 2u * SN_BYTES);
+                const int c = col0 + j * MC;
+#pragma unroll
+                for (int f = 0; f < 5; f++) tma_load_3d(land + f * (MC * V2_LZ), &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], lfull);
+#pragma unroll
+                for (int q = 0; q < 5; q++) tma_load_3d(land + (5 + q) * (MC * V2_LZ), &m.tm_coef, R.y - V2_ZH, c, q, lfull);
+                const int dst = ((j * MC) & (MRING - 1)) * V2_LZ;
+#pragma unroll
+                for (int f = 0; f < 2; f++)
+                    tma_load_3d(snap + f * (MRING * V2_LZ) + dst, &m.tm_snap, R.y - V2_ZH, c, a.snap_plane[f], lfull);
+            }
+        }
+        return;
+    }
+
+    // ---- compute warps
+    const bool vel = warp < 8;
+    const int cl = warp & 7;
+    const int z = 4 * lane;
+    int P = 0, C = 0;  // product passes and chunk computes of this CTA so far
+    // product pass P (chunk j): landing slot -> products ring
+    auto products = [&](int j) -> bool {
+        if (!mbar_wait(lfull, P & 1)) return false;
+        const int t = threadIdx.x;
+        constexpr int NQ = V2_LZ / 4;  // 16-byte row groups per column
+        if (t < MC * NQ) {
+            const int col = t / NQ, rq = t - col * NQ;
+            const float4 *L4 = reinterpret_cast<const float4 *>(land) + col * NQ + rq;
+            constexpr int A4 = MC * V2_LZ / 4;  // float4 per landing array
+            float4 fv[5], cv[5];
+#pragma unroll
+            for (int f = 0; f < 5; f++) {
+                fv[f] = L4[f * A4];
+                cv[f] = L4[(5 + f) * A4];
+            }
+            auto mul4 = [](float4 x, float4 y) { return make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w); };
+            constexpr int R4 = MRING * V2_LZ / 4;  // float4 per ring array
+            float4 *P4 = reinterpret_cast<float4 *>(prod) + ((j * MC + col) & (MRING - 1)) * NQ + rq;
+            P4[P_A23XX * R4] = mul4(cv[A23], fv[SXX]);
+            P4[P_A2ZZ * R4] = mul4(cv[A2], fv[SZZ]);
+            P4[P_A3XZ * R4] = mul4(cv[A3], fv[SXZ]);
+            P4[P_A2XX * R4] = mul4(cv[A2], fv[SXX]);
+            P4[P_A23ZZ * R4] = mul4(cv[A23], fv[SZZ]);
+            P4[P_M1XVX * R4] = mul4(cv[M1X], fv[VX]);
+            P4[P_M1ZVZ * R4] = mul4(cv[M1Z], fv[VZ]);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&pd[P & 1]);
+        P++;
+        return true;
+    };
+
+    for (int r = r0; r < r1; r++) {
+        const int4 R = m.runs[r];
+        const int s = R.x, k0 = R.z, n = R.w - R.z;
+        const ShotGeom g = a.shots[s];
+        const int nz = g.nz, nx = g.nx, ldz = a.ldz;
+        const int gz = R.y + z;
+        const int nval = min(4, nz - gz);
+        if (r > r0) named_sync(1, M_CONSUMERS * 32);  // the previous run's chunks are all computed
+        const int P0 = P, C0 = C;
+        for (int pl = 0; pl < 3; pl++)
+            if (!products(k0 - 1 + pl)) return fail();
+        const float d0 = a.imax0[2 * s] * (1.0f / SNAP_Q), d1 = a.imax0[2 * s + 1] * (1.0f / SNAP_Q);
+        for (int c = 0; c < n; c++) {
+            const int gx = (k0 + c) * MC + cl;
+            const bool live = gx < nx && gz < nz;
+            const long long o = g.off + (long long)gx * ldz + gz;
+            // global operands of this chunk, issued before the wait
+            float4 own[3], im[2];
+            uint2 sn1[2];
+            if (live) {
+                if (vel) {
+                    own[0] = ld_f4(a.own2[VX] + o);
+                    own[1] = ld_f4(a.own2[VZ] + o);
+                    im[0] = ld_f4(a.img[0] + o);
+                    if (!a.ilast) {
+                        sn1[0] = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
+                        sn1[1] = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
+                    }
+                } else {
+#pragma unroll
+                    for (int f = 0; f < 3; f++) own[f] = ld_f4(a.own2[SXX + f] + o);
+                    im[0] = ld_f4(a.img[1] + o);
+                    im[1] = ld_f4(a.img[2] + o);
+                }
+            }
+            const int Q = P0 + c + 2;  // product pass of chunk k0 + c + 1
+            if (!mbar_wait(&pd[Q & 1], (Q >> 1) & 1)) return fail();
+            if (live) {
+                float w[20];
+                if (vel) {
+                    float v[2][4];
+#pragma unroll
+                    for (int f = 0; f < 2; f++) {
+                        v[f][0] = own[f].x; v[f][1] = own[f].y; v[f][2] = own[f].z; v[f][3] = own[f].w;
+                    }
+                    if (a.rec && g.rec_iz >= gz && g.rec_iz < gz + 4) {
+                        const int j = g.rec_iz - gz;
+#pragma unroll
+                        for (int f = 0; f < 2; f++)
+                            if (a.comp_mask & (1 << f)) {
+                                const float d = a.rec[g.doff + ((long long)a.it * a.ncomp + rec_slot(a.comp_mask, f)) * nx + gx];
+#pragma unroll
+                                for (int jj = 0; jj < 4; jj++)
+                                    if (jj == j) v[f][jj] = Ar<false>::add(d, v[f][jj]);
+                            }
+                    }
+                    madj_x4<false>(prod, P_A23XX, gx, z, v[VX]);
+                    madj_x4<false>(prod, P_A2ZZ, gx, z, v[VX]);
+                    mzwin(prod, P_A3XZ, gx, z, w);
+                    adj_fast_z4<true>(w, v[VX]);
+                    madj_x4<true>(prod, P_A3XZ, gx, z, v[VZ]);
+                    mzwin(prod, P_A2XX, gx, z, w);
+                    adj_fast_z4<false>(w, v[VZ]);
+                    mzwin(prod, P_A23ZZ, gx, z, w);
+                    adj_fast_z4<false>(w, v[VZ]);
+                    if (a.sponge) {
+#pragma unroll
+                        for (int f = 0; f < 2; f++)
+#pragma unroll
+                            for (int j = 0; j < 4; j++) v[f][j] = sponge_cell<false>(v[f][j], gz + j, gx, nz, nx, a.filt, a.abc2);
+                    }
+                    if (nval == 4) {
+#pragma unroll
+                        for (int f = 0; f < 2; f++)
+                            *reinterpret_cast<float4 *>(a.out[f] + o) = make_float4(v[f][0], v[f][1], v[f][2], v[f][3]);
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < 2; f++)
+                            for (int j = 0; j < nval; j++) a.out[f][o + j] = v[f][j];
+                    }
+                    // imaging, Vx/Vz term (W/image-mod-rtm.f90:146-162)
+                    float s1[4] = {0.f, 0.f, 0.f, 0.f}, s2[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (!a.ilast) {
+                        const float e0 = a.imax1[2 * s] * (1.0f / SNAP_Q), e1 = a.imax1[2 * s + 1] * (1.0f / SNAP_Q);
+                        const float4 wx8 = rh4(snap, 0, gx, z), wz8 = rh4(snap, 1, gx, z);
+                        const float2 a0 = __half22float2(*reinterpret_cast<const __half2 *>(&sn1[0].x));
+                        const float2 a1 = __half22float2(*reinterpret_cast<const __half2 *>(&sn1[0].y));
+                        const float2 b0 = __half22float2(*reinterpret_cast<const __half2 *>(&sn1[1].x));
+                        const float2 b1 = __half22float2(*reinterpret_cast<const __half2 *>(&sn1[1].y));
+                        const float nx4[4] = {a0.x, a0.y, a1.x, a1.y}, nz4[4] = {b0.x, b0.y, b1.x, b1.y};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            s1[j] = a.inv_dt * (nx4[j] * e0 - f4(wx8, j) * d0);
+                            s2[j] = a.inv_dt * (nz4[j] * e1 - f4(wz8, j) * d1);
+                        }
+                    }
+                    float tt[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) tt[j] = v[VX][j] * s1[j] + v[VZ][j] * s2[j];
+                    if (nval == 4) {
+                        float4 sv = im[0];
+                        sv.x += tt[0]; sv.y += tt[1]; sv.z += tt[2]; sv.w += tt[3];
+                        *reinterpret_cast<float4 *>(a.img[0] + o) = sv;
+                    } else {
+                        for (int j = 0; j < nval; j++) a.img[0][o + j] += tt[j];
+                    }
+                } else {
+                    float v[3][4];  // sxx, szz, sxz
+#pragma unroll
+                    for (int f = 0; f < 3; f++) {
+                        v[f][0] = own[f].x; v[f][1] = own[f].y; v[f][2] = own[f].z; v[f][3] = own[f].w;
+                    }
+                    if (a.rec && g.rec_iz >= gz && g.rec_iz < gz + 4) {
+                        const int j = g.rec_iz - gz;
+#pragma unroll
+                        for (int f = 0; f < 3; f++)
+                            if (a.comp_mask & (1 << (2 + f))) {
+                                const float d =
+                                    a.rec[g.doff + ((long long)a.it * a.ncomp + rec_slot(a.comp_mask, 2 + f)) * nx + gx];
+#pragma unroll
+                                for (int jj = 0; jj < 4; jj++)
+                                    if (jj == j) v[f][jj] = Ar<false>::add(d, v[f][jj]);
+                            }
+                    }
+                    madj_x4<true>(prod, P_M1XVX, gx, z, v[0]);
+                    mzwin(prod, P_M1ZVZ, gx, z, w);
+                    adj_fast_z4<true>(w, v[1]);
+                    mzwin(prod, P_M1XVX, gx, z, w);
+                    adj_fast_z4<false>(w, v[2]);
+                    madj_x4<false>(prod, P_M1ZVZ, gx, z, v[2]);
+                    if (a.sponge) {
+#pragma unroll
+                        for (int f = 0; f < 3; f++)
+#pragma unroll
+                            for (int j = 0; j < 4; j++) v[f][j] = sponge_cell<false>(v[f][j], gz + j, gx, nz, nx, a.filt, a.abc2);
+                    }
+                    if (nval == 4) {
+#pragma unroll
+                        for (int f = 0; f < 3; f++)
+                            *reinterpret_cast<float4 *>(a.out[2 + f] + o) = make_float4(v[f][0], v[f][1], v[f][2], v[f][3]);
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < 3; f++)
+                            for (int j = 0; j < nval; j++) a.out[2 + f][o + j] = v[f][j];
+                    }
+                    // imaging, lambda and mu terms: x taps of the snapshots
+                    // (8-byte reads of 4 halves), z taps from 20-row windows
+                    float p4[4] = {0.f, 0.f, 0.f, 0.f}, p7[4] = {0.f, 0.f, 0.f, 0.f};  // x taps: Vx (P), Vz (M)
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        const float c = StagCoef<float>::c(k);
+                        const float4 ap = rh4(snap, 0, gx + 5 - k, z), am = rh4(snap, 0, gx - 4 + k, z);
+                        const float4 bp = rh4(snap, 1, gx + 4 - k, z), bm = rh4(snap, 1, gx - 5 + k, z);
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            p4[j] += c * (f4(ap, j) - f4(am, j));
+                            p7[j] += c * (f4(bp, j) - f4(bm, j));
+                        }
+                    }
+                    float s4v[4], s5v[4], s6v[4];
+                    {
+                        float wz[20];  // source Vz, rows z-8 .. z+11
+#pragma unroll
+                        for (int q = 0; q < 5; q++) {
+                            const float4 t_ = rh4(snap, 1, gx, z - 8 + 4 * q);
+                            wz[4 * q] = t_.x; wz[4 * q + 1] = t_.y; wz[4 * q + 2] = t_.z; wz[4 * q + 3] = t_.w;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int cz = gz + j;
+                            float s4 = 0.f, s5 = 0.f;
+                            if (cz >= 4 && cz <= nz - 6 && gx >= 4 && gx <= nx - 6) {
+                                float p5 = 0.f;
+#pragma unroll
+                                for (int k = 0; k < 5; k++) p5 += StagCoef<float>::c(k) * (wz[8 + j + 5 - k] - wz[8 + j - 4 + k]);
+                                s4 = p4[j] * d0 * a.inv_dx;
+                                s5 = p5 * d1 * a.inv_dx;
+                            }
+                            s4v[j] = s4;
+                            s5v[j] = s5;
+                        }
+                    }
+                    {
+                        float wx[20];  // source Vx, rows z-8 .. z+11
+#pragma unroll
+                        for (int q = 0; q < 5; q++) {
+                            const float4 t_ = rh4(snap, 0, gx, z - 8 + 4 * q);
+                            wx[4 * q] = t_.x; wx[4 * q + 1] = t_.y; wx[4 * q + 2] = t_.z; wx[4 * q + 3] = t_.w;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int cz = gz + j;
+                            float s6 = 0.f;
+                            if (cz >= 5 && cz <= nz - 6 && gx >= 5 && gx <= nx - 6) {
+                                float p6 = 0.f;
+#pragma unroll
+                                for (int k = 0; k < 5; k++) p6 += StagCoef<float>::c(k) * (wx[8 + j + 4 - k] - wx[8 + j - 5 + k]);
+                                s6 = (p6 * d0 + p7[j] * d1) * a.inv_dx;
+                            }
+                            s6v[j] = s6;
+                        }
+                    }
+                    float t1[4], t2[4];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const float s3 = s4v[j] + s5v[j];
+                        t1[j] = -(v[0][j] + v[1][j]) * s3;
+                        t2[j] = -(2.f * v[0][j] * s4v[j] + 2.f * v[1][j] * s5v[j] + v[2][j] * s6v[j]);
+                    }
+                    if (nval == 4) {
+                        float4 sv = im[0], sw = im[1];
+                        sv.x += t1[0]; sv.y += t1[1]; sv.z += t1[2]; sv.w += t1[3];
+                        sw.x += t2[0]; sw.y += t2[1]; sw.z += t2[2]; sw.w += t2[3];
+                        *reinterpret_cast<float4 *>(a.img[1] + o) = sv;
+                        *reinterpret_cast<float4 *>(a.img[2] + o) = sw;
+                    } else {
+                        for (int j = 0; j < nval; j++) {
+                            a.img[1][o + j] += t1[j];
+                            a.img[2][o + j] += t2[j];
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&cd[C & 1]);
+            C++;
+            if (c + 3 <= n + 1) {
+                // product pass of chunk k0 + c + 2 into the slot of chunk
+                // k0 + c - 2, which the compute of chunk k0 + c - 1 read last
+                if (c >= 1) {
+                    const int D = C0 + c - 1;
+                    if (!mbar_wait(&cd[D & 1], (D >> 1) & 1)) return fail();
+                }
+                if (!products(k0 + c + 2)) return fail();
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(rdone);
+    }
+}
+
 }  // namespace eg

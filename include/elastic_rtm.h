@@ -313,13 +313,14 @@ int rtm_batch_set_checkpoint(rtm_batch *b, int interval);
  * Results are bit-identical.  out[43] of rtm_batch_stats reports the
  * setting. */
 int rtm_batch_set_tma(rtm_batch *b, int on);
-/* Forward pass by the marching kernel (one CTA per SM walks 128-row strips
- * column chunk by column chunk, every operand loaded by tensor-map copies one
- * chunk ahead; needs tensor-map staging): mode -1 = the autotuner's choice
- * (on until rtm_batch_autotune has run), 0 = tile kernel, 1 = marching
- * kernel.  Results are bit-identical.  out[44] of rtm_batch_stats reports
- * whether the marching kernel runs, out[45] its autotuner time (ms per
- * launch, -1 when not timed). */
+/* Forward and adjoint passes by the marching kernels (one CTA per SM walks
+ * 128-row strips column chunk by column chunk, operands loaded by tensor-map
+ * copies ahead of the compute; needs tensor-map staging): mode -1 = the
+ * autotuner's choice per pass (on until rtm_batch_autotune has run), 0 =
+ * tile kernels, 1 = marching kernels.  Results are bit-identical.
+ * rtm_batch_stats: out[44] / out[46] whether the forward / adjoint marching
+ * kernel runs, out[45] / out[47] their autotuner times (ms per launch, -1
+ * when not timed). */
 int rtm_batch_set_march(rtm_batch *b, int mode);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */

@@ -202,12 +202,13 @@ def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
 
 
 @pytest.mark.parametrize("nz,nx,nt,interval", [(40, 180, 60, 0), (300, 900, 40, 0), (700, 700, 40, 7)])
-def test_batch_marching_forward_is_bit_identical(nz, nx, nt, interval):
-    """The forward pass by the marching kernel (one CTA per SM walking
-    128-row strips in 8-column chunks through a ring of staged columns)
-    gives the tile kernel's images bit for bit: one strip narrower than the
-    grid of CTAs, several strips with a partial last one, checkpoint-restart
-    mode; the autotuner times it beside the tile variants."""
+def test_batch_marching_kernels_are_bit_identical(nz, nx, nt, interval):
+    """The forward and adjoint passes by the marching kernels (one CTA per SM
+    walking 128-row strips in 8-column chunks through rings of staged
+    columns and adjoint products) give the tile kernels' images bit for bit:
+    one strip narrower than the grid of CTAs, several strips with a partial
+    last one, checkpoint-restart mode; the autotuner times them beside the
+    tile variants."""
     dx, dt, fp, abc, zs, zr, ns = 10.0, 1e-3, 30.0, 20 if nz > 100 else 10, 8, 8, 20
     wmin, wmax, spacing = (50, 96, 24) if nx < 300 else (150, 400, 200)
     rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=13, spacing=spacing, wmin=wmin,
@@ -232,10 +233,10 @@ def test_batch_marching_forward_is_bit_identical(nz, nx, nt, interval):
 
     ref, st0 = run(0)
     img, st = run(1)
-    assert st["march"] and not st0["march"]
+    assert st["march"] and st["march_adj"] and not st0["march"] and not st0["march_adj"]
     np.testing.assert_array_equal(img, ref)
     assert np.abs(ref).max() > 0
     if nz == 300:
         img, st = run(-1, tune=True)
-        assert st["tune_ms_march"] > 0
+        assert st["tune_ms_march"] > 0 and st["tune_ms_march_adj"] > 0
         np.testing.assert_array_equal(img, ref)
