@@ -150,16 +150,20 @@ constexpr int IMG_FOLD = 32;
 // edge (5 columns) lands on zeros, so tile staging needs no per-shot masking
 constexpr int GUARD = 5;
 
-// Work of the marching forward kernel for `ctas` CTAs: the units (shot,
-// strip, 8-column chunk) in shot, strip, chunk order, cut into `ctas`
-// contiguous pieces of equal length; a piece's units form runs of
-// consecutive chunks of one strip.  Units weigh the same whatever their
+// Work of the marching kernels for `ctas` CTAs.  The units (shot, strip,
+// 8-column chunk) are ordered by shot, column block (the shot's chunks in
+// equal blocks of about one CTA's share), strip, chunk, and cut into `ctas` contiguous pieces of equal
+// length; a piece's units form runs of consecutive chunks of one strip.  So
+// the CTAs of vertically adjacent strips march over the same columns at the
+// same time, and the 8-row halo that one strip's tiles share with the next is
+// still in L2 when the second reads it.  Units weigh the same whatever their
 // strip's depth: a partial last strip moves fewer bytes but keeps every warp
 // issuing the full chunk's instructions.
 void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> &runs, std::vector<int> &lo)
 {
     long long total = 0;
     for (const HostShot &h : shots) total += (long long)ceil_div(h.nx, MC) * ceil_div(h.nz, V2_TZ);
+    const double share = (double)total / ctas;  // chunks per CTA
     runs.clear();
     lo.assign(ctas + 1, 0);
     long long before = 0;
@@ -167,17 +171,20 @@ void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> 
     for (size_t s = 0; s < shots.size(); s++) {
         const HostShot &h = shots[s];
         const int nch = ceil_div(h.nx, MC);
-        for (int t = 0; t * V2_TZ < h.nz; t++)
-            for (int k = 0; k < nch; k++, before++) {
-                const int cta = (int)(before * ctas / total);
-                if (cta != cur || runs.back().x != (int)s || runs.back().y != t * V2_TZ) {
-                    runs.push_back(make_int4((int)s, t * V2_TZ, k, k + 1));
-                    for (int c = cur + 1; c <= cta; c++) lo[c] = (int)runs.size() - 1;
-                    cur = cta;
-                } else {
-                    runs.back().w = k + 1;
+        // the shot's columns in nb blocks of equal length
+        const int nb = std::max(1, (int)std::lround(nch / share));
+        for (int q = 0; q < nb; q++)
+            for (int t = 0; t * V2_TZ < h.nz; t++)
+                for (int k = (int)((long long)q * nch / nb); k < (int)((long long)(q + 1) * nch / nb); k++, before++) {
+                    const int cta = (int)(before * ctas / total);
+                    if (cta != cur || runs.back().x != (int)s || runs.back().y != t * V2_TZ || runs.back().w != k) {
+                        runs.push_back(make_int4((int)s, t * V2_TZ, k, k + 1));
+                        for (int c = cur + 1; c <= cta; c++) lo[c] = (int)runs.size() - 1;
+                        cur = cta;
+                    } else {
+                        runs.back().w = k + 1;
+                    }
                 }
-            }
     }
     for (int c = cur + 1; c <= ctas; c++) lo[c] = (int)runs.size();
 }
