@@ -197,7 +197,7 @@ int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaS
         init = true;
     }
     RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0, "marching forward step: unsupported arguments");
-    k_fwd_march<<<ctas, M_THREADS, M_SMEM, st>>>(a, m);
+    k_fwd_march<<<ctas, M_FWD_THREADS, M_SMEM, st>>>(a, m);
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }

@@ -7,17 +7,16 @@
 // column is brought on chip once per strip instead of once per tile plus its
 // 10-column x halo.  Every operand of a chunk -- the neighbour-level chunk
 // one ahead of it, the level's own fields and the five coefficients -- is
-// loaded by tensor-memory-access bulk copies two chunks ahead of the compute.
-// Sixteen warps read shared memory only (eight update the velocities of the
-// chunk's eight columns, eight the stresses); the warp that finishes a chunk
-// last issues the copies that the chunk released, so no warp waits to issue
-// and there are no block-wide barriers.
+// loaded by tensor-memory-access bulk copies that a producer warp issues two
+// chunks ahead of the compute; sixteen compute warps read shared memory only
+// (eight update the velocities of the chunk's eight columns, eight the
+// stresses), and full/empty mbarrier pairs replace block-wide barriers.
 //
 //   ring  [5 fields][32 columns][144 rows]     92,160 B
 //   slots [2][own 5 + coef 5][8 columns][128]  81,920 B
 //
 // Chunk k reads ring columns 8k-5 .. 8k+12 (chunks k-1, k, k+1).  Once chunk
-// k is done the group of chunk k+2 is issued (ring chunk k+3 into the slot
+// k is done the producer issues the group of chunk k+2 (ring chunk k+3 into the slot
 // chunk k-1 held, own/coefficients into the slot chunk k held); the first
 // group of a run (ring chunks k-1, k, k+1) waits until the previous run's
 // last chunk is done.  Zeros beyond the shot come from the engine's zero
@@ -31,11 +30,12 @@ namespace eg {
 
 constexpr int MC = 8;          // columns per chunk
 constexpr int MRING = 32;      // staged neighbour-level columns (power of two)
-constexpr int M_WARPS = 16;  // column (w & 7) of a chunk, lane l rows 4l..4l+3
-constexpr int M_THREADS = M_WARPS * 32;
+constexpr int M_WARPS = 16;  // compute warps: column (w & 7) of a chunk, lane l rows 4l..4l+3
+constexpr int M_FWD_THREADS = (M_WARPS + 1) * 32;  // forward: + one producer warp
+constexpr int M_THREADS = M_WARPS * 32;            // adjoint: the last warp out issues
 constexpr int M_RING = 5 * MRING * V2_LZ;   // floats
 constexpr int M_SLOT = 10 * MC * V2_TZ;     // floats per own/coefficient slot
-constexpr size_t M_SMEM = (size_t)(M_RING + 2 * M_SLOT) * sizeof(float) + 128 + 64;
+constexpr size_t M_SMEM = (size_t)(M_RING + 2 * M_SLOT) * sizeof(float) + 128 + 64;  // + barriers, cursor
 
 struct MarchArgs {
     const int4 *runs;   // (shot, first row of the strip, first chunk, end chunk)
@@ -91,74 +91,80 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
 // Rank of field f among the recorded components (its trace slot).
 __device__ __forceinline__ int rec_slot(int mask, int f) { return __popc(mask & ((1 << f) - 1)); }
 
-// The warp that finishes a step last (a shared-memory counter of arrivals)
-// issues the tensor-map copies that the step released; no warp waits to
-// issue.
-__device__ __forceinline__ bool last_arrival(int *cnt)
+// Arrive on a step's barrier (one arrival per warp); true for the warp whose
+// arrival completes the phase (the pending count before it was 1), which
+// then issues the tensor-map copies that the step released -- no warp waits
+// to issue.  Its wait on the completed phase returns at once and orders the
+// other warps' work (the issue cursor they advanced) before its own.
+__device__ __forceinline__ bool last_arrival(unsigned long long *bar, unsigned parity)
 {
-    __threadfence_block();
-    const int old = atomicAdd(cnt, 1);
-    if (old != M_WARPS - 1) return false;
-    *cnt = 0;
-    __threadfence_block();
-    return true;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+    unsigned pend;
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%1];\n"
+                 " mbarrier.pending_count.b64 %0, st;\n}\n"
+                 : "=r"(pend)
+                 : "r"(a)
+                 : "memory");
+    if (pend != 1) return false;
+    return mbar_wait(bar, parity);
 }
 
-__global__ void __launch_bounds__(M_THREADS, 1) k_fwd_march(const __grid_constant__ Step2DArgs<float> a, const __grid_constant__ MarchArgs m)
+// 17 warps put five on one SM sub-partition: at most 96 registers a thread
+__global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_constant__ Step2DArgs<float> a, const __grid_constant__ MarchArgs m)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *ring = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
     float *slots = ring + M_RING;
     unsigned long long *full = reinterpret_cast<unsigned long long *>(slots + 2 * M_SLOT);
-    int *cnt = reinterpret_cast<int *>(full + 2);  // [2] arrivals per chunk parity
-    int *cur = cnt + 2;                            // issue cursor: run, chunk, groups issued
+    unsigned long long *empty = full + 2;
     const int r0 = m.run_lo[blockIdx.x], r1 = m.run_lo[blockIdx.x + 1];
     if (r0 >= r1) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-
-    constexpr unsigned NB_BYTES = V2_LZ * MC * 4, OWN_BYTES = V2_TZ * MC * 4;
-    // group n: what chunk n of this CTA's walk reads first (full[n & 1],
-    // own/coefficient slot n & 1)
-    auto issue = [&](int r, int k, bool first, int n) {
-        const int4 R = m.runs[r];
-        const int col0 = (int)(a.shots[R.x].off / a.ldz);
-        unsigned long long *bar = &full[n & 1];
-        mbar_expect_tx(bar, (first ? 3u : 1u) * 5u * NB_BYTES + 10u * OWN_BYTES);
-        for (int j = first ? k - 1 : k + 1; j <= k + 1; j++) {
-            const int c = col0 + j * MC, dst = ((j * MC) & (MRING - 1)) * V2_LZ;
-#pragma unroll
-            for (int f = 0; f < 5; f++)
-                tma_load_3d(ring + f * (MRING * V2_LZ) + dst, &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], bar);
-        }
-        float *sl = slots + (n & 1) * M_SLOT;
-#pragma unroll
-        for (int f = 0; f < 5; f++) tma_load_3d(sl + f * (MC * V2_TZ), &m.tm_own, R.y, col0 + k * MC, m.own_plane[f], bar);
-#pragma unroll
-        for (int q = 0; q < 5; q++) tma_load_3d(sl + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + k * MC, q, bar);
-    };
-    // once chunk i is done by every warp: groups up to chunk i + 2 (a run's
-    // first group only up to i + 1, when every chunk before it is done)
-    auto issue_upto = [&](int i) {
-        while (cur[0] < r1 && cur[2] <= i + 2) {
-            const int4 R = m.runs[cur[0]];
-            const bool first = cur[1] == R.z;
-            if (first && cur[2] > i + 1) break;
-            issue(cur[0], cur[1], first, cur[2]);
-            cur[2]++;
-            if (++cur[1] >= R.w && ++cur[0] < r1) cur[1] = m.runs[cur[0]].z;
-        }
-    };
     if (threadIdx.x == 0) {
         mbar_init(&full[0]);
         mbar_init(&full[1]);
+        mbar_init_n(&empty[0], M_WARPS);
+        mbar_init_n(&empty[1], M_WARPS);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        cnt[0] = cnt[1] = 0;
-        cur[0] = r0;
-        cur[1] = m.runs[r0].z;
-        cur[2] = 0;
-        issue_upto(-1);
     }
     __syncthreads();
+
+    if (warp == M_WARPS) {
+        // ---- producer: group n holds what chunk n of this CTA's walk reads
+        // first (full[n & 1], own/coefficient slot n & 1); it is issued once
+        // chunk n - 2 is done (chunk n - 1 for a run's first group)
+        if (lane != 0) return;
+        constexpr unsigned NB_BYTES = V2_LZ * MC * 4, OWN_BYTES = V2_TZ * MC * 4;
+        int n = 0;
+        for (int r = r0; r < r1; r++) {
+            const int4 R = m.runs[r];
+            const int col0 = (int)(a.shots[R.x].off / a.ldz);
+            for (int k = R.z; k < R.w; k++, n++) {
+                const bool first = k == R.z;
+                const int done = first ? n - 1 : n - 2;
+                if (done >= 0 && !mbar_wait(&empty[done & 1], (done >> 1) & 1)) {
+                    if (a.err) atomicExch(a.err, 1);
+                    return;
+                }
+                unsigned long long *bar = &full[n & 1];
+                mbar_expect_tx(bar, (first ? 3u : 1u) * 5u * NB_BYTES + 10u * OWN_BYTES);
+                for (int j = first ? k - 1 : k + 1; j <= k + 1; j++) {
+                    const int c = col0 + j * MC, dst = ((j * MC) & (MRING - 1)) * V2_LZ;
+#pragma unroll
+                    for (int f = 0; f < 5; f++)
+                        tma_load_3d(ring + f * (MRING * V2_LZ) + dst, &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], bar);
+                }
+                float *sl = slots + (n & 1) * M_SLOT;
+#pragma unroll
+                for (int f = 0; f < 5; f++)
+                    tma_load_3d(sl + f * (MC * V2_TZ), &m.tm_own, R.y, col0 + k * MC, m.own_plane[f], bar);
+#pragma unroll
+                for (int q = 0; q < 5; q++)
+                    tma_load_3d(sl + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + k * MC, q, bar);
+            }
+        }
+        return;
+    }
 
     // ---- consumers: warps 0-7 update Vx, Vz of column (warp & 7) of each
     // chunk, warps 8-15 the three stresses of the same column
@@ -339,7 +345,7 @@ __global__ void __launch_bounds__(M_THREADS, 1) k_fwd_march(const __grid_constan
             }
             // this warp's reads of chunk i's ring columns and slot are done
             __syncwarp();
-            if (lane == 0 && last_arrival(&cnt[i & 1])) issue_upto(i);
+            if (lane == 0) mbar_arrive(&empty[i & 1]);
         }
         if (vel && a.snap_out[0]) {
 #pragma unroll
@@ -392,7 +398,7 @@ struct MarchAdjArgs {
 constexpr int MA_PROD = 7 * MRING * V2_LZ;  // floats
 constexpr int MA_SNAP = 2 * MRING * V2_LZ;  // halves
 constexpr int MA_LAND = 10 * MC * V2_LZ;    // floats
-constexpr size_t MA_SMEM = (size_t)MA_PROD * 4 + (size_t)MA_SNAP * 2 + (size_t)MA_LAND * 4 + 128 + 64;
+constexpr size_t MA_SMEM = (size_t)MA_PROD * 4 + (size_t)MA_SNAP * 2 + (size_t)MA_LAND * 4 + 128 + 96;
 
 // 4 halves of snapshot ring field f at shot column col, rows z..z+3
 __device__ __forceinline__ float4 rh4(const __half *ring, int f, int col, int z)
@@ -426,9 +432,10 @@ __global__ void __launch_bounds__(M_THREADS, 1)
     __half *snap = reinterpret_cast<__half *>(prod + MA_PROD);
     float *land = reinterpret_cast<float *>(snap + MA_SNAP);
     unsigned long long *lfull = reinterpret_cast<unsigned long long *>(land + MA_LAND);
-    unsigned long long *pd = lfull + 1, *cd = lfull + 3;
-    int *cnt = reinterpret_cast<int *>(lfull + 5);  // arrivals: [0] product pass, [1] run
-    int *cur = cnt + 2;                             // issue cursor: run, pass of the run, passes issued
+    unsigned long long *pd = lfull + 1, *cd = lfull + 3, *rdone = lfull + 5;
+    // issue cursor: run, pass of the run, passes issued, and the run's first
+    // column, first row, first chunk, chunk count
+    int *cur = reinterpret_cast<int *>(lfull + 6);
     const int r0 = m.run_lo[blockIdx.x], r1 = m.run_lo[blockIdx.x + 1];
     if (r0 >= r1) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -439,10 +446,19 @@ __global__ void __launch_bounds__(M_THREADS, 1)
     // landing group of the cursor's product pass: raw fields and
     // coefficients of its chunk into the landing slot, its snapshots into
     // their ring; then the cursor moves to the next pass
+    auto load_run = [&](int r) {
+        const int4 R = m.runs[r];
+        cur[0] = r;
+        cur[1] = 0;
+        cur[3] = (int)(a.shots[R.x].off / a.ldz);
+        cur[4] = R.y;
+        cur[5] = R.z;
+        cur[6] = R.w - R.z;
+    };
     auto issue_next = [&]() {
-        const int4 R = m.runs[cur[0]];
-        const int col0 = (int)(a.shots[R.x].off / a.ldz);
-        const int j = R.z - 1 + cur[1], c = col0 + j * MC;
+        const int4 R = make_int4(0, cur[4], 0, 0);
+        const int col0 = cur[3];
+        const int j = cur[5] - 1 + cur[1], c = col0 + j * MC;
         mbar_expect_tx(lfull, 10u * NB_BYTES + 2u * SN_BYTES);
 #pragma unroll
         for (int f = 0; f < 5; f++) tma_load_3d(land + f * (MC * V2_LZ), &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], lfull);
@@ -453,7 +469,10 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         for (int f = 0; f < 2; f++)
             tma_load_3d(snap + f * (MRING * V2_LZ) + dst, &m.tm_snap, R.y - V2_ZH, c, a.snap_plane[f], lfull);
         cur[2]++;
-        if (++cur[1] > R.w - R.z + 1 && ++cur[0] < r1) cur[1] = 0;
+        if (++cur[1] > cur[6] + 1) {
+            if (cur[0] + 1 < r1) load_run(cur[0] + 1);
+            else cur[0] = r1;
+        }
     };
     if (threadIdx.x == 0) {
         mbar_init(lfull);
@@ -461,10 +480,9 @@ __global__ void __launch_bounds__(M_THREADS, 1)
             mbar_init_n(&pd[q], M_WARPS);
             mbar_init_n(&cd[q], M_WARPS);
         }
+        mbar_init_n(rdone, M_WARPS);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        cnt[0] = cnt[1] = 0;
-        cur[0] = r0;
-        cur[1] = 0;
+        load_run(r0);
         cur[2] = 0;
         issue_next();
     }
@@ -502,12 +520,10 @@ __global__ void __launch_bounds__(M_THREADS, 1)
             P4[P_M1ZVZ * R4] = mul4(cv[M1Z], fv[VZ]);
         }
         __syncwarp();
-        if (lane == 0) {
-            mbar_arrive(&pd[P & 1]);
-            // the landing slot is free: the last warp out loads the next
-            // pass of this run (a run's first pass waits for the run before)
-            if (last_arrival(&cnt[0]) && cur[0] < r1 && cur[1] != 0) issue_next();
-        }
+        // the landing slot is free once every warp is out: the last one
+        // loads the next pass of this run (a run's first pass waits for the
+        // run before)
+        if (lane == 0 && last_arrival(&pd[P & 1], (P >> 1) & 1) && cur[0] < r1 && cur[1] != 0) issue_next();
         P++;
         return true;
     };
@@ -751,7 +767,7 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         // every chunk of this run is computed once the last warp is out: it
         // loads the first pass of the next run
         __syncwarp();
-        if (lane == 0 && last_arrival(&cnt[1]) && cur[0] < r1) issue_next();
+        if (lane == 0 && last_arrival(rdone, (r - r0) & 1) && cur[0] < r1) issue_next();
     }
 }
 
