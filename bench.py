@@ -281,7 +281,8 @@ def run_gpu(args):
         "gpu_launches": int(kernels),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "kernel": "k_step2d adjoint + fused imaging (112 algorithmic B/cell)" +
+                     "kernel": ("k_adj_march" if st["march_adj"] else "k_step2d_v2") +
+                               " adjoint + fused imaging (112 algorithmic B/cell)" +
                                (" (checkpoint-restart: the adjoint pass time includes the segment recompute)"
                                 if st["checkpoint"] else ""),
                      "traffic": (round(tpc * cells_per_launch) if tpc else None)},
