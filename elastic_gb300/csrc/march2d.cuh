@@ -544,6 +544,28 @@ __global__ void __launch_bounds__(M_THREADS, 1)
             const int gx = (k0 + c) * MC + cl;
             const bool live = gx < nx && gz < nz;
             const long long o = g.off + (long long)gx * ldz + gz;
+            {
+                // the next chunk's global operands to L2 (one lane per
+                // 128-byte line), so their loads there are L2 hits
+                const int gx1 = gx + MC;
+                if (c + 1 < n && gx1 < nx && gz < nz && (lane & 7) == 0) {
+                    const long long o1 = g.off + (long long)gx1 * ldz + gz;
+                    if (vel) {
+                        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.own2[VX] + o1));
+                        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.own2[VZ] + o1));
+                        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[0] + o1));
+                        if (!a.ilast && (lane & 15) == 0) {
+                            asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.isnap1[0] + o1));
+                            asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.isnap1[1] + o1));
+                        }
+                    } else {
+#pragma unroll
+                        for (int f = 0; f < 3; f++) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.own2[SXX + f] + o1));
+                        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[1] + o1));
+                        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[2] + o1));
+                    }
+                }
+            }
             // global operands of this chunk, issued before the wait
             float4 own[3], im[2];
             uint2 sn1[2];
