@@ -540,6 +540,31 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         for (int pl = 0; pl < 3; pl++)
             if (!products(k0 - 1 + pl)) return fail();
         const float d0 = a.imax0[2 * s] * (1.0f / SNAP_Q), d1 = a.imax0[2 * s + 1] * (1.0f / SNAP_Q);
+        // global operands of a chunk (own fields, image partials, next-level
+        // snapshots): loaded at the end of the previous chunk's iteration,
+        // into registers its compute no longer needs
+        float4 own[3], im[2];
+        uint2 sn1[2];
+        auto fetch = [&](int c) {
+            const int gx = (k0 + c) * MC + cl;
+            if (c >= n || gx >= nx || gz >= nz) return;
+            const long long o = g.off + (long long)gx * ldz + gz;
+            if (vel) {
+                own[0] = ld_f4(a.own2[VX] + o);
+                own[1] = ld_f4(a.own2[VZ] + o);
+                im[0] = ld_f4(a.img[0] + o);
+                if (!a.ilast) {
+                    sn1[0] = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
+                    sn1[1] = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
+                }
+            } else {
+#pragma unroll
+                for (int f = 0; f < 3; f++) own[f] = ld_f4(a.own2[SXX + f] + o);
+                im[0] = ld_f4(a.img[1] + o);
+                im[1] = ld_f4(a.img[2] + o);
+            }
+        };
+        fetch(0);
         for (int c = 0; c < n; c++) {
             const int gx = (k0 + c) * MC + cl;
             const bool live = gx < nx && gz < nz;
@@ -564,25 +589,6 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                         asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[1] + o1));
                         asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.img[2] + o1));
                     }
-                }
-            }
-            // global operands of this chunk, issued before the wait
-            float4 own[3], im[2];
-            uint2 sn1[2];
-            if (live) {
-                if (vel) {
-                    own[0] = ld_f4(a.own2[VX] + o);
-                    own[1] = ld_f4(a.own2[VZ] + o);
-                    im[0] = ld_f4(a.img[0] + o);
-                    if (!a.ilast) {
-                        sn1[0] = *reinterpret_cast<const uint2 *>(a.isnap1[0] + o);
-                        sn1[1] = *reinterpret_cast<const uint2 *>(a.isnap1[1] + o);
-                    }
-                } else {
-#pragma unroll
-                    for (int f = 0; f < 3; f++) own[f] = ld_f4(a.own2[SXX + f] + o);
-                    im[0] = ld_f4(a.img[1] + o);
-                    im[1] = ld_f4(a.img[2] + o);
                 }
             }
             const int Q = P0 + c + 2;  // product pass of chunk k0 + c + 1
@@ -773,6 +779,7 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                     }
                 }
             }
+            fetch(c + 1);
             __syncwarp();
             if (lane == 0) mbar_arrive(&cd[C & 1]);
             C++;
