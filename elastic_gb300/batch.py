@@ -78,9 +78,9 @@ class BatchRTM:
         check(load().rtm_batch_set_tma(self.h, int(bool(on))))
 
     def set_march(self, mode):
-        """Forward and adjoint passes by the marching kernels: -1 the
-        autotuner's choice per pass (on until autotune has run), 0 the tile
-        kernels, 1 the marching kernels."""
+        """Passes by the marching kernels: -1 the autotuner's choice per pass
+        (on until autotune has run), else a bit mask -- 1 forward, 2 adjoint
+        (0: tile kernels for both)."""
         check(load().rtm_batch_set_march(self.h, int(mode)))
 
     def set_checkpoint(self, interval):

@@ -235,8 +235,9 @@ struct rtm_batch {
     int ckpt = 0;
     DevBuf<float> ck;
     bool use_tma = true;   // stage step tiles with tensor-memory-access loads
-    // forward pass by the marching kernel: -1 automatic (the autotuner's
-    // choice, on until it has run), 0 off, 1 on; needs tensor-map staging
+    // passes by the marching kernels: -1 automatic (the autotuner's choice
+    // per pass, on until it has run), else bit 0 forward, bit 1 adjoint;
+    // needs tensor-map staging
     int march = -1;
     bool march_tuned = true, march_tuned_a = true;  // per pass
     double tune_march_ms = -1, tune_march_ms_a = -1;
@@ -380,8 +381,8 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         TRY(make_map(&madj.tm_coef, b->coef.p, false, ld, b->cap_cols, 5, gp, V2_LZ, MC));
         TRY(make_map(&madj.tm_snap, b->snaps.p, true, ld, b->cap_cols, 2 * nlev, gp, V2_LZ, MC));
     }
-    const bool use_march = tma_on && (b->march == 1 || (b->march < 0 && b->march_tuned));
-    const bool use_march_a = tma_on && (b->march == 1 || (b->march < 0 && b->march_tuned_a));
+    const bool use_march = tma_on && (b->march < 0 ? b->march_tuned : (b->march & 1) != 0);
+    const bool use_march_a = tma_on && (b->march < 0 ? b->march_tuned_a : (b->march & 2) != 0);
     // ---- coefficients of every shot's subgrid (guard columns and columns of
     // the previous group's shots are zero)
     RTM_CUDA(cudaMemsetAsync(b->coef.p, 0, 5 * gp * sizeof(float), st));
@@ -959,9 +960,9 @@ extern "C" int rtm_batch_stats(const rtm_batch *b, double *out)
     out[41] = b->th_a;
     out[42] = b->ckpt;
     out[43] = b->use_tma ? 1 : 0;
-    out[44] = b->use_tma && (b->march == 1 || (b->march < 0 && b->march_tuned)) ? 1 : 0;
+    out[44] = b->use_tma && (b->march < 0 ? b->march_tuned : (b->march & 1) != 0) ? 1 : 0;
     out[45] = b->tune_march_ms;
-    out[46] = b->use_tma && (b->march == 1 || (b->march < 0 && b->march_tuned_a)) ? 1 : 0;
+    out[46] = b->use_tma && (b->march < 0 ? b->march_tuned_a : (b->march & 2) != 0) ? 1 : 0;
     out[47] = b->tune_march_ms_a;
     return RTM_OK;
 }
@@ -985,7 +986,7 @@ extern "C" int rtm_batch_set_tma(rtm_batch *b, int on)
 
 extern "C" int rtm_batch_set_march(rtm_batch *b, int mode)
 {
-    RTM_CHECK_ARG(b && mode >= -1 && mode <= 1, "mode must be -1, 0 or 1");
+    RTM_CHECK_ARG(b && mode >= -1 && mode <= 3, "mode must be -1 .. 3");
     b->march = mode;
     return RTM_OK;
 }

@@ -395,10 +395,19 @@ struct MarchAdjArgs {
     CUtensorMap tm_snap;  // FP16 snapshot planes, box {144 rows, 8 columns, 1}
 };
 
-constexpr int MA_PROD = 7 * MRING * V2_LZ;  // floats
-constexpr int MA_SNAP = 2 * MRING * V2_LZ;  // halves
-constexpr int MA_LAND = 10 * MC * V2_LZ;    // floats
-constexpr size_t MA_SMEM = (size_t)MA_PROD * 4 + (size_t)MA_SNAP * 2 + (size_t)MA_LAND * 4 + 128 + 96;
+// products kept in the ring: the two pairs that share a stencil are summed
+enum { Q_X = 0,    // a23*sxx + a2*szz   (Vx, x differences)
+       Q_A3 = 1,   // a3*sxz             (Vx z, Vz x)
+       Q_Z = 2,    // a2*sxx + a23*szz   (Vz, z differences)
+       Q_M1X = 3,  // m1x*vx             (sxx x, sxz z)
+       Q_M1Z = 4,  // m1z*vz             (szz z, sxz x)
+       MA_NQ = 5 };
+constexpr int MA_PROD = MA_NQ * MRING * V2_LZ;  // floats
+constexpr int MA_SNAP = 2 * MRING * V2_LZ;      // halves
+// one landing slot: 10 float arrays (fields, coefficients) + 2 half arrays
+// (snapshots), [8 columns][144 rows] each, in floats
+constexpr int MA_LSLOT = 10 * MC * V2_LZ + MC * V2_LZ;
+constexpr size_t MA_SMEM = (size_t)MA_PROD * 4 + (size_t)MA_SNAP * 2 + (size_t)2 * MA_LSLOT * 4 + 128 + 96;
 
 // 4 halves of snapshot ring field f at shot column col, rows z..z+3
 __device__ __forceinline__ float4 rh4(const __half *ring, int f, int col, int z)
@@ -430,9 +439,9 @@ __global__ void __launch_bounds__(M_THREADS, 1)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *prod = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
     __half *snap = reinterpret_cast<__half *>(prod + MA_PROD);
-    float *land = reinterpret_cast<float *>(snap + MA_SNAP);
-    unsigned long long *lfull = reinterpret_cast<unsigned long long *>(land + MA_LAND);
-    unsigned long long *pd = lfull + 1, *cd = lfull + 3, *rdone = lfull + 5;
+    float *land = reinterpret_cast<float *>(snap + MA_SNAP);  // two landing slots
+    unsigned long long *lfull = reinterpret_cast<unsigned long long *>(land + 2 * MA_LSLOT);
+    unsigned long long *pd = lfull + 2, *cd = lfull + 4;
     // issue cursor: run, pass of the run, passes issued, and the run's first
     // column, first row, first chunk, chunk count
     int *cur = reinterpret_cast<int *>(lfull + 6);
@@ -443,9 +452,10 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         if (lane == 0 && a.err) atomicExch(a.err, 1);
     };
     constexpr unsigned NB_BYTES = V2_LZ * MC * 4, SN_BYTES = V2_LZ * MC * 2;
-    // landing group of the cursor's product pass: raw fields and
-    // coefficients of its chunk into the landing slot, its snapshots into
-    // their ring; then the cursor moves to the next pass
+    // landing group of the cursor's product pass P: raw fields,
+    // coefficients and FP16 snapshots of its chunk into landing slot P & 1;
+    // then the cursor moves to the next pass (runs follow one another: the
+    // landing slots are the only thing a group writes)
     auto load_run = [&](int r) {
         const int4 R = m.runs[r];
         cur[0] = r;
@@ -456,18 +466,19 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         cur[6] = R.w - R.z;
     };
     auto issue_next = [&]() {
-        const int4 R = make_int4(0, cur[4], 0, 0);
-        const int col0 = cur[3];
+        const int row0 = cur[4] - V2_ZH, col0 = cur[3];
         const int j = cur[5] - 1 + cur[1], c = col0 + j * MC;
-        mbar_expect_tx(lfull, 10u * NB_BYTES + 2u * SN_BYTES);
+        const int slot = cur[2] & 1;
+        float *ls = land + slot * MA_LSLOT;
+        __half *lh = reinterpret_cast<__half *>(ls + 10 * MC * V2_LZ);
+        unsigned long long *bar = &lfull[slot];
+        mbar_expect_tx(bar, 10u * NB_BYTES + 2u * SN_BYTES);
 #pragma unroll
-        for (int f = 0; f < 5; f++) tma_load_3d(land + f * (MC * V2_LZ), &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], lfull);
+        for (int f = 0; f < 5; f++) tma_load_3d(ls + f * (MC * V2_LZ), &m.tm_nb, row0, c, a.nb_plane[f], bar);
 #pragma unroll
-        for (int q = 0; q < 5; q++) tma_load_3d(land + (5 + q) * (MC * V2_LZ), &m.tm_coef, R.y - V2_ZH, c, q, lfull);
-        const int dst = ((j * MC) & (MRING - 1)) * V2_LZ;
+        for (int q = 0; q < 5; q++) tma_load_3d(ls + (5 + q) * (MC * V2_LZ), &m.tm_coef, row0, c, q, bar);
 #pragma unroll
-        for (int f = 0; f < 2; f++)
-            tma_load_3d(snap + f * (MRING * V2_LZ) + dst, &m.tm_snap, R.y - V2_ZH, c, a.snap_plane[f], lfull);
+        for (int f = 0; f < 2; f++) tma_load_3d(lh + f * (MC * V2_LZ), &m.tm_snap, row0, c, a.snap_plane[f], bar);
         cur[2]++;
         if (++cur[1] > cur[6] + 1) {
             if (cur[0] + 1 < r1) load_run(cur[0] + 1);
@@ -475,16 +486,16 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         }
     };
     if (threadIdx.x == 0) {
-        mbar_init(lfull);
         for (int q = 0; q < 2; q++) {
+            mbar_init(&lfull[q]);
             mbar_init_n(&pd[q], M_WARPS);
             mbar_init_n(&cd[q], M_WARPS);
         }
-        mbar_init_n(rdone, M_WARPS);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         load_run(r0);
         cur[2] = 0;
         issue_next();
+        if (cur[0] < r1) issue_next();
     }
     __syncthreads();
 
@@ -493,14 +504,16 @@ __global__ void __launch_bounds__(M_THREADS, 1)
     const int cl = warp & 7;
     const int z = 4 * lane;
     int P = 0, C = 0;  // product passes and chunk computes of this CTA so far
-    // product pass P (chunk j): landing slot -> products ring
+    // product pass P (chunk j): landing slot P & 1 -> products ring and
+    // snapshot ring
     auto products = [&](int j) -> bool {
-        if (!mbar_wait(lfull, P & 1)) return false;
+        if (!mbar_wait(&lfull[P & 1], (P >> 1) & 1)) return false;
         const int t = threadIdx.x;
         constexpr int NQ = V2_LZ / 4;  // 16-byte row groups per column
         if (t < MC * NQ) {
             const int col = t / NQ, rq = t - col * NQ;
-            const float4 *L4 = reinterpret_cast<const float4 *>(land) + col * NQ + rq;
+            const float *ls = land + (P & 1) * MA_LSLOT;
+            const float4 *L4 = reinterpret_cast<const float4 *>(ls) + col * NQ + rq;
             constexpr int A4 = MC * V2_LZ / 4;  // float4 per landing array
             float4 fv[5], cv[5];
 #pragma unroll
@@ -509,21 +522,25 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                 cv[f] = L4[(5 + f) * A4];
             }
             auto mul4 = [](float4 x, float4 y) { return make_float4(x.x * y.x, x.y * y.y, x.z * y.z, x.w * y.w); };
+            auto add4 = [](float4 x, float4 y) { return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w); };
             constexpr int R4 = MRING * V2_LZ / 4;  // float4 per ring array
-            float4 *P4 = reinterpret_cast<float4 *>(prod) + ((j * MC + col) & (MRING - 1)) * NQ + rq;
-            P4[P_A23XX * R4] = mul4(cv[A23], fv[SXX]);
-            P4[P_A2ZZ * R4] = mul4(cv[A2], fv[SZZ]);
-            P4[P_A3XZ * R4] = mul4(cv[A3], fv[SXZ]);
-            P4[P_A2XX * R4] = mul4(cv[A2], fv[SXX]);
-            P4[P_A23ZZ * R4] = mul4(cv[A23], fv[SZZ]);
-            P4[P_M1XVX * R4] = mul4(cv[M1X], fv[VX]);
-            P4[P_M1ZVZ * R4] = mul4(cv[M1Z], fv[VZ]);
+            const int rc = ((j * MC + col) & (MRING - 1)) * NQ + rq;
+            float4 *P4 = reinterpret_cast<float4 *>(prod) + rc;
+            P4[Q_X * R4] = add4(mul4(cv[A23], fv[SXX]), mul4(cv[A2], fv[SZZ]));
+            P4[Q_A3 * R4] = mul4(cv[A3], fv[SXZ]);
+            P4[Q_Z * R4] = add4(mul4(cv[A2], fv[SXX]), mul4(cv[A23], fv[SZZ]));
+            P4[Q_M1X * R4] = mul4(cv[M1X], fv[VX]);
+            P4[Q_M1Z * R4] = mul4(cv[M1Z], fv[VZ]);
+            // the chunk's FP16 snapshots into their ring
+            const uint2 *LH = reinterpret_cast<const uint2 *>(ls + 10 * MC * V2_LZ) + col * NQ + rq;
+            uint2 *S2 = reinterpret_cast<uint2 *>(snap) + rc;
+#pragma unroll
+            for (int f = 0; f < 2; f++) S2[f * R4] = LH[f * A4];
         }
         __syncwarp();
-        // the landing slot is free once every warp is out: the last one
-        // loads the next pass of this run (a run's first pass waits for the
-        // run before)
-        if (lane == 0 && last_arrival(&pd[P & 1], (P >> 1) & 1) && cur[0] < r1 && cur[1] != 0) issue_next();
+        // landing slot P & 1 is free once every warp is out: the last one
+        // loads pass P + 2 into it
+        if (lane == 0 && last_arrival(&pd[P & 1], (P >> 1) & 1) && cur[0] < r1) issue_next();
         P++;
         return true;
     };
@@ -612,14 +629,11 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                                     if (jj == j) v[f][jj] = Ar<false>::add(d, v[f][jj]);
                             }
                     }
-                    madj_x4<false>(prod, P_A23XX, gx, z, v[VX]);
-                    madj_x4<false>(prod, P_A2ZZ, gx, z, v[VX]);
-                    mzwin(prod, P_A3XZ, gx, z, w);
+                    madj_x4<false>(prod, Q_X, gx, z, v[VX]);
+                    mzwin(prod, Q_A3, gx, z, w);
                     adj_fast_z4<true>(w, v[VX]);
-                    madj_x4<true>(prod, P_A3XZ, gx, z, v[VZ]);
-                    mzwin(prod, P_A2XX, gx, z, w);
-                    adj_fast_z4<false>(w, v[VZ]);
-                    mzwin(prod, P_A23ZZ, gx, z, w);
+                    madj_x4<true>(prod, Q_A3, gx, z, v[VZ]);
+                    mzwin(prod, Q_Z, gx, z, w);
                     adj_fast_z4<false>(w, v[VZ]);
                     if (a.sponge) {
 #pragma unroll
@@ -680,12 +694,12 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                                     if (jj == j) v[f][jj] = Ar<false>::add(d, v[f][jj]);
                             }
                     }
-                    madj_x4<true>(prod, P_M1XVX, gx, z, v[0]);
-                    mzwin(prod, P_M1ZVZ, gx, z, w);
+                    madj_x4<true>(prod, Q_M1X, gx, z, v[0]);
+                    mzwin(prod, Q_M1Z, gx, z, w);
                     adj_fast_z4<true>(w, v[1]);
-                    mzwin(prod, P_M1XVX, gx, z, w);
+                    mzwin(prod, Q_M1X, gx, z, w);
                     adj_fast_z4<false>(w, v[2]);
-                    madj_x4<false>(prod, P_M1ZVZ, gx, z, v[2]);
+                    madj_x4<false>(prod, Q_M1Z, gx, z, v[2]);
                     if (a.sponge) {
 #pragma unroll
                         for (int f = 0; f < 3; f++)
@@ -793,10 +807,6 @@ __global__ void __launch_bounds__(M_THREADS, 1)
                 if (!products(k0 + c + 2)) return fail();
             }
         }
-        // every chunk of this run is computed once the last warp is out: it
-        // loads the first pass of the next run
-        __syncwarp();
-        if (lane == 0 && last_arrival(rdone, (r - r0) & 1) && cur[0] < r1) issue_next();
     }
 }
 

@@ -316,11 +316,14 @@ int rtm_batch_set_tma(rtm_batch *b, int on);
 /* Forward and adjoint passes by the marching kernels (one CTA per SM walks
  * 128-row strips column chunk by column chunk, operands loaded by tensor-map
  * copies ahead of the compute; needs tensor-map staging): mode -1 = the
- * autotuner's choice per pass (on until rtm_batch_autotune has run), 0 =
- * tile kernels, 1 = marching kernels.  Results are bit-identical.
- * rtm_batch_stats: out[44] / out[46] whether the forward / adjoint marching
- * kernel runs, out[45] / out[47] their autotuner times (ms per launch, -1
- * when not timed). */
+ * autotuner's choice per pass (on until rtm_batch_autotune has run), else a
+ * bit mask: 1 forward, 2 adjoint (0 = tile kernels for both).  The marching
+ * forward is bit-identical to the tile kernel; the marching adjoint sums the
+ * two pairs of coefficient x field products that share a stencil before
+ * differencing them, which agrees with the tile kernel to rounding (fast
+ * arithmetic).  rtm_batch_stats: out[44] / out[46] whether the forward /
+ * adjoint marching kernel runs, out[45] / out[47] their autotuner times (ms
+ * per launch, -1 when not timed). */
 int rtm_batch_set_march(rtm_batch *b, int mode);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */

@@ -16,6 +16,13 @@ pytestmark = pytest.mark.gpu
 # this relative L2 (observed values are printed by the test).
 RTOL_SNAP = 5e-3
 
+# The marching adjoint sums the two pairs of coefficient x field products
+# that share a stencil before differencing them (a23*sxx + a2*szz under the
+# x difference of Vx, a2*sxx + a23*szz under the z difference of Vz); against
+# the tile kernel, which differences each product, the images agree to this
+# relative L2 (observed values are printed).
+RTOL_REASSOC = 1e-5
+
 
 def rel_l2(a, b):
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
@@ -46,7 +53,7 @@ def oracle_stack(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, ab
 
 
 def run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group, graph=True,
-              tile_x=0, tune=False, stages=None):
+              tile_x=0, tune=False, stages=None, march=None):
     n = len(nxs)
     eng = BatchRTM(nz, nx, nt, dx, dt, fp, abc, rho, lam, mu, x0, nxs, xsrc, np.full(n, zs), np.full(n, zr),
                    comp_mask=3, group_max=group, nsource=ns)
@@ -55,6 +62,8 @@ def run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, 
     eng.set_graph(graph, tile_x)
     if stages:
         eng.set_stages(*stages)
+    if march is not None:
+        eng.set_march(march)
     image = np.zeros(3 * nz * nx, np.float32)
     for s0, k in eng.groups():
         flat = np.concatenate([np.concatenate([traces[s][c].ravel() for c in range(2)]) for s in range(s0, s0 + k)])
@@ -97,17 +106,20 @@ def test_batch_tile_widths_and_autotuner_are_bit_identical():
     the arithmetic of any cell."""
     nz, nx, nt, dx, dt, fp, abc, zs, zr, ns = 40, 180, 60, 10.0, 1e-3, 30.0, 10, 6, 6, 40
     rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=5)
-    ref, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3, tile_x=8)
+    ref, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3, tile_x=8,
+                       march=0)
     for tx, stages in ((16, None), (8, (2, 2)), (16, (2, 2)), (16, (1, 2, 512, 512)), (32, (2, 1, 512, 512))):
         # two staging buffers (next tile staged during the current one) do
         # not change the arithmetic either; where they do not fit the
         # launcher keeps one
         img, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
-                           tile_x=tx, stages=stages)
+                           tile_x=tx, stages=stages, march=0)
         np.testing.assert_array_equal(img, ref)
+    # the autotuner may also pick the marching kernels (forward bit for
+    # bit, adjoint to rounding)
     img, st = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
                         tune=True)
-    np.testing.assert_array_equal(img, ref)
+    assert max(rel_l2(img[i], ref[i]) for i in range(3)) < RTOL_REASSOC
     assert st["tile_x"] in (8, 16, 32) and st["tile_x_adj"] in (8, 16, 32)
     # -1 marks a tile width that does not fit in shared memory
     assert all(t > 0 or t == -1 for t in st["tune_ms_fwd"] + st["tune_ms_adj"])
@@ -126,14 +138,14 @@ def test_batch_staging_depth_with_several_tiles_per_cta_is_bit_identical():
                                                  wmax=400)
     for tx in (8, 16):
         ref, st = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
-                            tile_x=tx, stages=(1, 1))
+                            tile_x=tx, stages=(1, 1), march=0)
         assert st["work_items"] > 2 * 152  # more work items than resident CTAs
         assert np.isfinite(ref).all() and np.abs(ref).max() > 0
         for stages in ((2, 2), (1, 1, 512, 512), (2, 2, 512, 512)):
             if tx == 8 and len(stages) > 2:
                 continue  # 512 threads need tile width >= 16
             img, _ = run_batch(rho, lam, mu, x0, nxs, xsrc, traces, nz, nx, nt, dx, dt, fp, abc, zs, zr, ns, group=3,
-                               tile_x=tx, stages=stages)
+                               tile_x=tx, stages=stages, march=0)
             np.testing.assert_array_equal(img, ref)
 
 
@@ -186,6 +198,7 @@ def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
         if interval:
             eng.set_checkpoint(interval)
         eng.set_tma(tma)
+        eng.set_march(0)  # the tile kernels, staged both ways
         image = np.zeros(3 * nz * nx, np.float32)
         for s0, g in eng.groups():
             flat = np.concatenate([np.concatenate([traces[s][c].ravel() for c in range(2)]) for s in range(s0, s0 + g)])
@@ -202,13 +215,13 @@ def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
 
 
 @pytest.mark.parametrize("nz,nx,nt,interval", [(40, 180, 60, 0), (300, 900, 40, 0), (700, 700, 40, 7)])
-def test_batch_marching_kernels_are_bit_identical(nz, nx, nt, interval):
-    """The forward and adjoint passes by the marching kernels (one CTA per SM
-    walking 128-row strips in 8-column chunks through rings of staged
-    columns and adjoint products) give the tile kernels' images bit for bit:
-    one strip narrower than the grid of CTAs, several strips with a partial
-    last one, checkpoint-restart mode; the autotuner times them beside the
-    tile variants."""
+def test_batch_marching_kernels_match_tile_kernels(nz, nx, nt, interval):
+    """The passes by the marching kernels (one CTA per SM walking 128-row
+    strips in 8-column chunks through rings of staged columns and adjoint
+    products): the forward gives the tile kernel's images bit for bit, the
+    adjoint agrees to rounding; one strip narrower than the grid of CTAs,
+    several strips with a partial last one, checkpoint-restart mode; the
+    autotuner times them beside the tile variants."""
     dx, dt, fp, abc, zs, zr, ns = 10.0, 1e-3, 30.0, 20 if nz > 100 else 10, 8, 8, 20
     wmin, wmax, spacing = (50, 96, 24) if nx < 300 else (150, 400, 200)
     rho, lam, mu, x0, nxs, xsrc, traces = survey(nshots=3, nz=nz, nx=nx, nt=nt, seed=13, spacing=spacing, wmin=wmin,
@@ -229,14 +242,20 @@ def test_batch_marching_kernels_are_bit_identical(nz, nx, nt, interval):
             eng.migrate(s0, g, flat, image)
         st = eng.stats()
         eng.close()
-        return image, st
+        return image.reshape(3, nx, nz), st
 
     ref, st0 = run(0)
-    img, st = run(1)
-    assert st["march"] and st["march_adj"] and not st0["march"] and not st0["march_adj"]
-    np.testing.assert_array_equal(img, ref)
+    fwd, st1 = run(1)
+    both, st3 = run(3)
+    assert not st0["march"] and not st0["march_adj"]
+    assert st1["march"] and not st1["march_adj"]
+    assert st3["march"] and st3["march_adj"]
+    np.testing.assert_array_equal(fwd, ref)
     assert np.abs(ref).max() > 0
+    errs = [rel_l2(both[i], ref[i]) for i in range(3)]
+    print("marching adjoint vs tile adjoint, rel. L2 per image:", errs)
+    assert max(errs) < RTOL_REASSOC
     if nz == 300:
         img, st = run(-1, tune=True)
         assert st["tune_ms_march"] > 0 and st["tune_ms_march_adj"] > 0
-        np.testing.assert_array_equal(img, ref)
+        assert max(rel_l2(img[i], ref[i]) for i in range(3)) < RTOL_REASSOC
