@@ -78,6 +78,14 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, in
         : "memory");
 }
 
+// Prefetch of one 3D tile box into L2 (no shared memory written).
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap *tm, int c0, int c1, int c2)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];\n" ::"l"(tm), "r"(c0), "r"(c1),
+                 "r"(c2)
+                 : "memory");
+}
+
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool valid)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);

@@ -161,6 +161,16 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
 #pragma unroll
                 for (int q = 0; q < 5; q++)
                     tma_load_3d(sl + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + k * MC, q, bar);
+                // the group two chunks further on, to L2: its loads then
+                // wait on L2 rather than HBM latency
+                if (k + 2 < R.w) {
+#pragma unroll
+                    for (int f = 0; f < 5; f++) tma_prefetch_3d(&m.tm_nb, R.y - V2_ZH, col0 + (k + 3) * MC, a.nb_plane[f]);
+#pragma unroll
+                    for (int f = 0; f < 5; f++) tma_prefetch_3d(&m.tm_own, R.y, col0 + (k + 2) * MC, m.own_plane[f]);
+#pragma unroll
+                    for (int q = 0; q < 5; q++) tma_prefetch_3d(&m.tm_coef, R.y, col0 + (k + 2) * MC, q);
+                }
             }
         }
         return;
