@@ -70,6 +70,7 @@ SIGNATURES = {
     "rtm_batch_set_checkpoint": (_c_int, [_P, _c_int]),
     "rtm_batch_set_tma": (_c_int, [_P, _c_int]),
     "rtm_batch_set_march": (_c_int, [_P, _c_int]),
+    "rtm_debug_march_plan": (_c_int, [_c_int, _P, _c_int, _c_int, _P, _c_int, _P]),
     "rtm_batch_set_stages": (_c_int, [_P, _c_int, _c_int, _c_int, _c_int]),
     "rtm_batch_destroy": (None, [_P]),
     "rtm_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),

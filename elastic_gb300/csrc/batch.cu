@@ -1041,6 +1041,34 @@ extern "C" int rtm_batch_autotune(rtm_batch *b, int shot0, int nshot, int steps)
 
 extern "C" void rtm_batch_destroy(rtm_batch *b) { delete b; }
 
+// Diagnostic: the marching kernels' work plan for shots of widths nxs[] and
+// depth nz over `ctas` CTAs (not part of the public header; no device use).
+// runs[4 * i ..] = (shot, first row, first chunk, end chunk) of run i, lo[b]
+// = first run of CTA b (ctas + 1 entries).  Returns the number of runs, or -1
+// when max_runs is too small.
+extern "C" int rtm_debug_march_plan(int nshots, const int *nxs, int nz, int ctas, int *runs, int max_runs, int *lo)
+{
+    if (nshots < 1 || nz < 1 || ctas < 1 || !nxs || !runs || !lo) return -1;
+    std::vector<HostShot> shots(nshots);
+    for (int i = 0; i < nshots; i++) {
+        shots[i] = HostShot{};
+        shots[i].nz = nz;
+        shots[i].nx = nxs[i];
+    }
+    std::vector<int4> r;
+    std::vector<int> l;
+    march_plan(shots, ctas, r, l);
+    if ((int)r.size() > max_runs) return -1;
+    for (size_t i = 0; i < r.size(); i++) {
+        runs[4 * i] = r[i].x;
+        runs[4 * i + 1] = r[i].y;
+        runs[4 * i + 2] = r[i].z;
+        runs[4 * i + 3] = r[i].w;
+    }
+    for (int b = 0; b <= ctas; b++) lo[b] = l[b];
+    return (int)r.size();
+}
+
 // Diagnostic: the pending CUDA error of this library's runtime and where it
 // was first seen (not part of the public header).
 extern "C" int rtm_debug_peek(char *where, int n)
