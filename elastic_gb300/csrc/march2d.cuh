@@ -597,10 +597,10 @@ __global__ void __launch_bounds__(M_THREADS, 1)
             const bool live = gx < nx && gz < nz;
             const long long o = g.off + (long long)gx * ldz + gz;
             {
-                // the next chunk's global operands to L2 (one lane per
-                // 128-byte line), so their loads there are L2 hits
-                const int gx1 = gx + MC;
-                if (c + 1 < n && gx1 < nx && gz < nz && (lane & 7) == 0) {
+                // the global operands of the chunk after next to L2 (one
+                // lane per 128-byte line), so their loads are L2 hits
+                const int gx1 = gx + 2 * MC;
+                if (c + 2 < n && gx1 < nx && gz < nz && (lane & 7) == 0) {
                     const long long o1 = g.off + (long long)gx1 * ldz + gz;
                     if (vel) {
                         asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.own2[VX] + o1));
