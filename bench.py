@@ -23,6 +23,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -94,7 +95,10 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); directory from
+        # ELASTIC_CLOCKS_DIR, else the system's temporary directory
+        self.path = os.path.join(os.environ.get("ELASTIC_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"elastic_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         os.makedirs(os.path.dirname(self.path), exist_ok=True)

@@ -497,7 +497,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
                     ShotTable &tb = pass ? b->tab_a : b->tab;
                     TRY(tb.build(cand[ci], tz));
                     TRY(build_maps(b->tab.tx, b->tab_a.tx));
-                    for (int rep = 0; rep < 2; rep++) {  // first round warms up
+                    for (int rep = 0; rep < 2; rep++) {  // the first repetition warms up
                         RTM_CUDA(cudaEventRecord(t0, st));
                         for (int k = 0; k < tune_steps; k++) {
                             const int L = 3 + (k & 1);
