@@ -1,7 +1,7 @@
 """Benchmark: batched multi-shot 2D elastic RTM (the reference's RTM path,
 W/rtm-mod-adj.f90:132-496, run for a survey of shots) on GB300.
 
-Workload (BASELINE configuration 2): full grid nx=2000 x nz=800, dx=5 m,
+Workload (the 64-shot survey): full grid nx=2000 x nz=800, dx=5 m,
 dt=0.5 ms, nt=6000, 40-cell sponge, 15 Hz Ricker; seeded smooth random Vp
 1800-4000 m/s (Gaussian filter, 200 m correlation), Vs=Vp/1.73, Gardner
 density; 64 shots 75 m apart, each on its own subgrid 600-2000 cells wide;
@@ -33,16 +33,16 @@ sys.path.insert(0, ROOT)
 
 CFG = dict(nz=800, nx=2000, dx=5.0, dt=5e-4, nt=6000, abc=40, fp=15.0, nsource=250, nshots=64, spacing=15,
            wmin=600, wmax=2000, zsrc=10, zrec=10, comp_mask=3, seed=2,
-           desc="batched multi-shot 2D elastic RTM, BASELINE config 2: 2000x800 grid, dx=5 m, dt=0.5 ms, nt=6000, "
+           desc="batched multi-shot 2D elastic RTM, 64-shot survey: 2000x800 grid, dx=5 m, dt=0.5 ms, nt=6000, "
                 "64 shots on 600-2000-cell subgrids")
-# BASELINE configuration 5 (end-to-end imaging survey): 6000 x 2000 cells,
+# The 256-shot end-to-end imaging survey: 6000 x 2000 cells,
 # dx=5 m, dt=0.4 ms, nt=10000, 256 shots on 1000-6000-cell subgrids; the
 # FP16 snapshots of every level would need ~1 TB per 4-shot group, so the
 # engine runs in checkpoint-restart mode.  A bounded sample of groups is
 # timed (the whole survey is ~64 groups).
 CFG5 = dict(nz=2000, nx=6000, dx=5.0, dt=4e-4, nt=10000, abc=40, fp=15.0, nsource=250, nshots=256, spacing=23,
             wmin=1000, wmax=6000, zsrc=10, zrec=10, comp_mask=3, seed=5,
-            desc="batched multi-shot 2D elastic RTM, BASELINE config 5: 6000x2000 grid, dx=5 m, dt=0.4 ms, "
+            desc="batched multi-shot 2D elastic RTM, 256-shot survey: 6000x2000 grid, dx=5 m, dt=0.4 ms, "
                  "nt=10000, 256 shots on 1000-6000-cell subgrids (smooth random background), checkpoint-restart "
                  "of the source wavefield")
 BYTES_FWD = 80     # algorithmic bytes per forward cell-update
@@ -357,7 +357,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"], "unit": "Gcell/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched multi-shot 2D elastic RTM, BASELINE config 2 (CPU sample: "
+            "config": {"workload": "batched multi-shot 2D elastic RTM, 64-shot survey on a 2000x800 grid (CPU sample: "
                                    + cb["sample"] + ")"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -371,7 +371,7 @@ CFL_LIMIT_3D = 0.4419  # 2 / sqrt(3 * 6.8267): leapfrog limit of the 10th-order 
 
 
 def run_acoustic3d(args):
-    """BASELINE configuration 4: 3D acoustic 10th-order forward modelling,
+    """3D acoustic 10th-order forward modelling,
     1024 x 1024 x 512 cells, dx=10 m, dt=1 ms, 20 Hz Ricker point source,
     1024 x 1024 surface receivers (interior), 30-cell sponge.  One step = a
     window of nt/10 time steps from rest (10 steps = the full nt)."""
@@ -428,7 +428,7 @@ def run_acoustic3d(args):
     line = {"metric": "Gcell-updates/s", "value": round(rate, 2), "unit": "Gcell/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"3D acoustic 10th-order forward modelling (BASELINE config 4), {n1}x{n2}x{n3}, "
+            "config": {"workload": f"3D acoustic 10th-order forward modelling, {n1}x{n2}x{n3}, "
                                    f"one step = {window} time steps, receivers on plane z={c['zr']}",
                        "vmax_realised": round(float(vmax), 1), "cfl": round(float(vmax) * c["dt"] / c["d"], 4),
                        "cfl_limit": CFL_LIMIT_3D, "tile_x": args.tile3d, "inputs_vs_l2": "inputs larger than L2"},
@@ -463,7 +463,7 @@ def unet_train_flops(table, batch):
 
 
 def run_precond(args):
-    """BASELINE configuration 3: the learned preconditioner.  (Reflectivity,
+    """The learned preconditioner workload.  (Reflectivity,
     migrated image) pairs from the project's Born modelling and migration on
     256 x 256 windows of the smoothed single-shot background, U-Net training
     (Adam, batch 32) on the GPU; one step = one training step.  Then the
@@ -532,7 +532,7 @@ def run_precond(args):
     line = {"metric": "training images/s (learned preconditioner)", "value": round(rate, 2), "unit": "images/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * train_s / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": f"learned preconditioner (BASELINE config 3): 3->3 channel 4-level U-Net, "
+            "config": {"workload": f"learned preconditioner: 3->3 channel 4-level U-Net, "
                                    f"{pc.net.nparam} parameters, {c['nx']}x{c['nz']} patches, batch {c['batch']}, "
                                    f"Adam lr {c['lr']}; {ntr} training pairs (Born-modelled then migrated, one shot, "
                                    f"Vx/Vz receivers, nt={c['nt']})",
