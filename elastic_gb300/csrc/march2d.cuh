@@ -1,27 +1,28 @@
-// Forward step of the batched RTM by marching z-strips (float, fast
-// arithmetic; same per-cell arithmetic as k_step2d_v2's forward).
+// Steps of the batched RTM by marching z-strips (float, fast arithmetic).
 //
-// A persistent CTA per SM owns a list of runs: (shot, 128-row strip, range of
-// 8-column chunks).  It walks each run left to right with the neighbour level
-// held in a ring of 32 staged columns (4 chunks, 8-row aligned z halo), so a
-// column is brought on chip once per strip instead of once per tile plus its
-// 10-column x halo.  Every operand of a chunk -- the neighbour-level chunk
-// one ahead of it, the level's own fields and the five coefficients -- is
-// loaded by tensor-memory-access bulk copies that a producer warp issues two
-// chunks ahead of the compute; sixteen compute warps read shared memory only
-// (eight update the velocities of the chunk's eight columns, eight the
-// stresses), and full/empty mbarrier pairs replace block-wide barriers.
+// Forward (k_fwd_march, same per-cell arithmetic as k_step2d_v2's forward):
+// a persistent CTA per SM owns a list of runs -- (shot, 128-row strip, range
+// of 8-column chunks) -- and walks each run left to right with the
+// neighbour level held in a ring of 32 staged columns (4 chunks, 8-row
+// aligned z halo), so a column is brought on chip once per strip instead of
+// once per tile plus its 10-column x halo.  Every operand of a chunk -- the
+// neighbour-level chunk one ahead of it, the level's own fields and the five
+// coefficients -- is loaded by tensor-memory-access bulk copies that a
+// producer warp issues two chunks ahead of the compute (and prefetches to L2
+// one chunk further); sixteen compute warps read shared memory only (eight
+// update the velocities of the chunk's eight columns, eight the stresses),
+// and full/empty mbarrier pairs replace block-wide barriers.
 //
 //   ring  [5 fields][32 columns][144 rows]     92,160 B
 //   slots [2][own 5 + coef 5][8 columns][128]  81,920 B
 //
 // Chunk k reads ring columns 8k-5 .. 8k+12 (chunks k-1, k, k+1).  Once chunk
-// k is done the producer issues the group of chunk k+2 (ring chunk k+3 into the slot
-// chunk k-1 held, own/coefficients into the slot chunk k held); the first
-// group of a run (ring chunks k-1, k, k+1) waits until the previous run's
-// last chunk is done.  Zeros beyond the shot come from the engine's zero
-// guard columns and the tensor maps' out-of-range fill, exactly as for the
-// tile kernel.  Every wait gives up after about a second and reports it
+// k is done the producer issues the group of chunk k+2 (ring chunk k+3 into
+// the slot chunk k-1 held, own/coefficients into the slot chunk k held); the
+// first group of a run (ring chunks k-1, k, k+1) waits until the previous
+// run's last chunk is done.  Zeros beyond the shot come from the engine's
+// zero guard columns and the tensor maps' out-of-range fill, exactly as for
+// the tile kernel.  Every wait gives up after about a second and reports it
 // through the error flag.
 #pragma once
 #include "elastic2d_v2.cuh"
@@ -373,30 +374,36 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
 
 // ---------------------------------------------------------------------------
 // Adjoint step with the fused imaging condition, by marching z-strips (fast
-// arithmetic, FP32 partial image planes; same per-cell arithmetic as
-// k_step2d_v2's fast adjoint).
+// arithmetic, FP32 partial image planes; the operator of k_step2d_v2's fast
+// adjoint).
 //
-// The adjoint stencils read the seven coefficient x field products of the
-// level above at x and z offsets up to 5, so the CTA keeps those products in
-// a ring of 32 columns (4 chunks) and the level's FP16 source snapshots in a
-// second ring.  Per chunk, the raw fields and coefficients (144 rows x 8
-// columns each) are loaded into one landing slot and the snapshots straight
-// into their ring; the sixteen warps turn the landing slot into products one
-// chunk ahead of need, then update the chunk's cells (warps 0-7 the
-// velocities and the Vx/Vz image, warps 8-15 the stresses and the lambda/mu
-// images).  Own fields, next-level snapshots and image partials are read
-// from global memory, issued before the wait.
+// The adjoint stencils read coefficient x field products of the level above
+// at x and z offsets up to 5, so the CTA keeps those products in a ring of
+// 32 columns (4 chunks) and the level's FP16 source snapshots in a second
+// ring.  The two pairs of products that share a stencil are summed before
+// they are differenced (a23*sxx + a2*szz under the x difference of Vx,
+// a2*sxx + a23*szz under the z difference of Vz): the same operator, rounded
+// differently from the tile kernel, which differences each product.  Per
+// chunk, the raw fields, coefficients and FP16 snapshots (144 rows x 8
+// columns each) land in one of two landing slots; the sixteen warps turn a
+// slot into the chunk's products and snapshot-ring columns one chunk ahead
+// of need, then update the chunk's cells (warps 0-7 the velocities and the
+// Vx/Vz image term, warps 8-15 the stresses and the lambda/mu terms).  Own
+// fields, next-level snapshots and image partials are read from global
+// memory at the end of the previous chunk, their lines prefetched to L2 two
+// chunks ahead.
 //
-//   products ring [7][32 columns][144 rows] floats  129,024 B
-//   snapshot ring [2][32 columns][144 rows] halves   18,432 B
-//   landing slot  [10][8 columns][144 rows] floats   46,080 B
+//   products ring [5][32 columns][144 rows] floats      92,160 B
+//   snapshot ring [2][32 columns][144 rows] halves      18,432 B
+//   landing slots 2 x ([10][8][144] floats + [2][8][144] halves)  101,376 B
 //
 // Order (per run of n chunks k0 .. k0+n-1): product passes of chunks k0-1,
 // k0, k0+1, then for each chunk k: wait until every warp has its products
 // through chunk k+1 (pd), compute k, signal (cd), and -- once chunk k-1 is
-// computed by every warp -- the product pass of chunk k+2 into the slot of
-// chunk k-2.  The last warp out of a product pass refills the landing slot;
-// the last warp out of a run loads the next run's first pass.
+// computed by every warp -- the product pass of chunk k+2 into the ring
+// slot of chunk k-2.  The warp whose arrival completes a product pass loads
+// the pass two ahead into the landing slot that pass freed (runs follow one
+// another: the landing slots are all a load writes).
 struct MarchAdjArgs {
     const int4 *runs;
     const int *run_lo;
