@@ -189,6 +189,27 @@ void march_plan(const std::vector<HostShot> &shots, int ctas, std::vector<int4> 
     for (int c = cur + 1; c <= ctas; c++) lo[c] = (int)runs.size();
 }
 
+// Launch with programmatic stream serialisation: the kernel may start
+// before the previous kernel in the stream has finished (the marching
+// kernels wait for it in their prologue, griddepcontrol.wait).
+template <typename Args>
+cudaError_t launch_pdl(void (*kernel)(Step2DArgs<float>, Args), int ctas, int threads, size_t smem, cudaStream_t st,
+                       const Step2DArgs<float> &a, const Args &m)
+{
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, a, m);
+}
+
 int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaStream_t st)
 {
     static bool init = false;
@@ -197,8 +218,7 @@ int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaS
         init = true;
     }
     RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0, "marching forward step: unsupported arguments");
-    k_fwd_march<<<ctas, M_FWD_THREADS, M_SMEM, st>>>(a, m);
-    RTM_CUDA(cudaGetLastError());
+    RTM_CUDA(launch_pdl(k_fwd_march, ctas, M_FWD_THREADS, M_SMEM, st, a, m));
     return RTM_OK;
 }
 
@@ -211,8 +231,7 @@ int launch_march_adj(const Step2DArgs<float> &a, const MarchAdjArgs &m, int ctas
     }
     RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0 && a.img[0] && !a.imgc[0],
                   "marching adjoint step: unsupported arguments");
-    k_adj_march<<<ctas, M_THREADS, MA_SMEM, st>>>(a, m);
-    RTM_CUDA(cudaGetLastError());
+    RTM_CUDA(launch_pdl(k_adj_march, ctas, M_THREADS, MA_SMEM, st, a, m));
     return RTM_OK;
 }
 

@@ -80,6 +80,17 @@ __device__ __forceinline__ void mzwin(const float *ring, int f, int x, int z, fl
     }
 }
 
+// Programmatic dependent launch: the next level's launch may start on SMs
+// this one has left; it initialises its barriers, then waits here until the
+// previous grid has completed and its writes are visible, before any global
+// load or store.  It lets its own dependents launch only after that wait, so
+// the level two steps back is complete before anyone reads it.
+__device__ __forceinline__ void wait_previous_level()
+{
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void mbar_init_n(unsigned long long *bar, unsigned count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"((unsigned)__cvta_generic_to_shared(bar)), "r"(count));
@@ -129,6 +140,7 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
+    wait_previous_level();
 
     if (warp == M_WARPS) {
         // ---- producer: group n holds what chunk n of this CTA's walk reads
@@ -511,10 +523,13 @@ __global__ void __launch_bounds__(M_THREADS, 1)
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         load_run(r0);
         cur[2] = 0;
+    }
+    __syncthreads();
+    wait_previous_level();
+    if (threadIdx.x == 0) {
         issue_next();
         if (cur[0] < r1) issue_next();
     }
-    __syncthreads();
 
     // ---- compute warps
     const bool vel = warp < 8;
