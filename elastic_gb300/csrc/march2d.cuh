@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
-    wait_previous_level();
+    if (warp != M_WARPS) wait_previous_level();
 
     if (warp == M_WARPS) {
         // ---- producer: group n holds what chunk n of this CTA's walk reads
@@ -148,6 +148,19 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
         // chunk n - 2 is done (chunk n - 1 for a run's first group)
         if (lane != 0) return;
         constexpr unsigned NB_BYTES = V2_LZ * MC * 4, OWN_BYTES = V2_TZ * MC * 4;
+        {
+            // group 0's own fields (written two levels back) and coefficients
+            // go out before the wait for the previous level
+            const int4 R = m.runs[r0];
+            const int col0 = (int)(a.shots[R.x].off / a.ldz);
+            mbar_expect_tx(&full[0], 3u * 5u * NB_BYTES + 10u * OWN_BYTES);
+#pragma unroll
+            for (int f = 0; f < 5; f++) tma_load_3d(slots + f * (MC * V2_TZ), &m.tm_own, R.y, col0 + R.z * MC, m.own_plane[f], &full[0]);
+#pragma unroll
+            for (int q = 0; q < 5; q++)
+                tma_load_3d(slots + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + R.z * MC, q, &full[0]);
+        }
+        wait_previous_level();
         int n = 0;
         for (int r = r0; r < r1; r++) {
             const int4 R = m.runs[r];
@@ -160,20 +173,22 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
                     return;
                 }
                 unsigned long long *bar = &full[n & 1];
-                mbar_expect_tx(bar, (first ? 3u : 1u) * 5u * NB_BYTES + 10u * OWN_BYTES);
+                if (n > 0) mbar_expect_tx(bar, (first ? 3u : 1u) * 5u * NB_BYTES + 10u * OWN_BYTES);
                 for (int j = first ? k - 1 : k + 1; j <= k + 1; j++) {
                     const int c = col0 + j * MC, dst = ((j * MC) & (MRING - 1)) * V2_LZ;
 #pragma unroll
                     for (int f = 0; f < 5; f++)
                         tma_load_3d(ring + f * (MRING * V2_LZ) + dst, &m.tm_nb, R.y - V2_ZH, c, a.nb_plane[f], bar);
                 }
-                float *sl = slots + (n & 1) * M_SLOT;
+                if (n > 0) {
+                    float *sl = slots + (n & 1) * M_SLOT;
 #pragma unroll
-                for (int f = 0; f < 5; f++)
-                    tma_load_3d(sl + f * (MC * V2_TZ), &m.tm_own, R.y, col0 + k * MC, m.own_plane[f], bar);
+                    for (int f = 0; f < 5; f++)
+                        tma_load_3d(sl + f * (MC * V2_TZ), &m.tm_own, R.y, col0 + k * MC, m.own_plane[f], bar);
 #pragma unroll
-                for (int q = 0; q < 5; q++)
-                    tma_load_3d(sl + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + k * MC, q, bar);
+                    for (int q = 0; q < 5; q++)
+                        tma_load_3d(sl + (5 + q) * (MC * V2_TZ), &m.tm_coef, R.y, col0 + k * MC, q, bar);
+                }
                 // the group two chunks further on, to L2: its loads then
                 // wait on L2 rather than HBM latency
                 if (k + 2 < R.w) {
