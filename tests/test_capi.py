@@ -57,3 +57,8 @@ def test_argument_checks_before_device_work(lib):
     assert st == 1 and b"too small" in lib.rtm_last_error()
     assert lib.rtm_abc_c_(-1, p) == 1
     assert lib.rtm_source_c_(0, 1e-3, 15.0, 250, p) == 1
+    # batch-engine switches reject bad handles and modes before any device use
+    assert lib.rtm_batch_set_march(None, 1) == 1
+    assert lib.rtm_batch_set_tma(None, 1) == 1
+    assert lib.rtm_batch_set_stages(None, 1, 1, 256, 256) == 1
+    assert lib.rtm_batch_set_checkpoint(None, 4) == 1

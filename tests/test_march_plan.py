@@ -245,3 +245,13 @@ def test_adjoint_protocol_has_no_deadlock_and_no_stale_read(lib, nxs, nz, ctas):
         if lo[b] < lo[b + 1] and tried < 4:
             assert adjoint_protocol(runs, lo[b], lo[b + 1], seed=b)
             tried += 1
+
+
+def test_plan_rejects_bad_arguments(lib):
+    nxs = np.array([100, 200], np.int32)
+    runs = np.zeros(4 * 64, np.int32)
+    lo = np.zeros(5, np.int32)
+    assert lib.rtm_debug_march_plan(0, _lib.ptr(nxs), 100, 4, _lib.ptr(runs), 64, _lib.ptr(lo)) == -1
+    assert lib.rtm_debug_march_plan(2, _lib.ptr(nxs), 100, 0, _lib.ptr(runs), 64, _lib.ptr(lo)) == -1
+    # more runs than the output holds
+    assert lib.rtm_debug_march_plan(2, _lib.ptr(nxs), 1000, 4, _lib.ptr(runs), 1, _lib.ptr(lo)) == -1
