@@ -212,10 +212,14 @@ cudaError_t launch_pdl(void (*kernel)(Step2DArgs<float>, Args), int ctas, int th
 
 int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaStream_t st)
 {
-    static bool init = false;
-    if (!init) {
-        RTM_CUDA(cudaFuncSetAttribute(k_fwd_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M_SMEM));
-        init = true;
+    static bool init[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!init[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(k_fwd_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)M_SMEM));
+            init[dev] = true;
+        }
     }
     RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0, "marching forward step: unsupported arguments");
     RTM_CUDA(launch_pdl(k_fwd_march, ctas, M_FWD_THREADS, M_SMEM, st, a, m));
@@ -224,10 +228,14 @@ int launch_march(const Step2DArgs<float> &a, const MarchArgs &m, int ctas, cudaS
 
 int launch_march_adj(const Step2DArgs<float> &a, const MarchAdjArgs &m, int ctas, cudaStream_t st)
 {
-    static bool init = false;
-    if (!init) {
-        RTM_CUDA(cudaFuncSetAttribute(k_adj_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MA_SMEM));
-        init = true;
+    static bool init[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!init[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(k_adj_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MA_SMEM));
+            init[dev] = true;
+        }
     }
     RTM_CHECK_ARG(!a.inplane[0] && a.tma && a.ldz % 4 == 0 && a.img[0] && !a.imgc[0],
                   "marching adjoint step: unsupported arguments");

@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <mutex>
+
 // Status codes returned by every int-returning entry point of the C-ABI.
 enum RtmStatus {
     RTM_OK = 0,
@@ -62,6 +64,27 @@ struct StagCoef {
                       : T(19845.0 / 16384.0);
     }
 };
+
+// One-time per-device settings (kernel attributes such as the dynamic
+// shared-memory limit, occupancy-derived grid sizes, device attributes) are
+// kept per CUDA device, indexed by the caller's current device, and set
+// under one process-wide lock, so a process that launches on several
+// devices, from several threads, sets each of them once on every device.
+constexpr int RTM_MAX_DEVICES = 64;
+static inline int rtm_current_device()
+{
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= RTM_MAX_DEVICES) {
+        cudaGetLastError();
+        d = 0;
+    }
+    return d;
+}
+static inline std::mutex &rtm_device_state_lock()
+{
+    static std::mutex m;
+    return m;
+}
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 

@@ -52,14 +52,15 @@ int ensure_device()
 
 int device_sm_count()
 {
-    static int nsm = 0;
-    if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-        if (nsm <= 0) nsm = 1;
+    static int nsm[RTM_MAX_DEVICES] = {};
+    const int dev = rtm_current_device();
+    std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+    if (!nsm[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        nsm[dev] = v > 0 ? v : 1;
     }
-    return nsm;
+    return nsm[dev];
 }
 
 // ------------------------------------------------------------ step launch
@@ -69,15 +70,22 @@ static int launch_step_tx(const Step2DArgs<T> &a, int grid_cap, cudaStream_t st)
     auto kern = k_step2d<T, EXACT, ADJ, TZ_TILE, TX>;
     const bool img = ADJ && a.img[0] != nullptr;
     const size_t smem = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>(img);
-    static int grid_max[2] = {0, 0};
-    if (!grid_max[img]) {
-        const size_t smax = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>(true);
-        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
-        int nb = 0;
-        RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
-        grid_max[img] = (nb > 0 ? nb : 1) * device_sm_count();
+    static int grid_max[RTM_MAX_DEVICES][2] = {};
+    const int dev = rtm_current_device();
+    const int nsm = device_sm_count();
+    int gm;
+    {
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!grid_max[dev][img]) {
+            const size_t smax = step2d_smem<T, EXACT, ADJ, TZ_TILE, TX>(true);
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax));
+            int nb = 0;
+            RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 256, smem));
+            grid_max[dev][img] = (nb > 0 ? nb : 1) * nsm;
+        }
+        gm = grid_max[dev][img];
     }
-    int grid = a.ntiles < grid_max[img] ? a.ntiles : grid_max[img];
+    int grid = a.ntiles < gm ? a.ntiles : gm;
     if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;
     if (grid <= 0) return RTM_OK;
     kern<<<grid, 256, smem, st>>>(a);
@@ -98,14 +106,15 @@ static int launch_step_e(const Step2DArgs<T> &a, int tx, int grid_cap, cudaStrea
 
 int max_smem_optin()
 {
-    static int v = 0;
-    if (!v) {
-        int dev = 0;
-        cudaGetDevice(&dev);
+    static int optin[RTM_MAX_DEVICES] = {};
+    const int dev = rtm_current_device();
+    std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+    if (!optin[dev]) {
+        int v = 0;
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (v <= 0) v = 48 * 1024;
+        optin[dev] = v > 0 ? v : 48 * 1024;
     }
-    return v;
+    return optin[dev];
 }
 
 template <int TX>
@@ -147,17 +156,25 @@ static int launch_v2_tx(const Step2DArgs<float> &a, int grid_cap, cudaStream_t s
     RTM_CHECK_ARG(v2_fits(ADJ, EXACT, TX, stages, threads),
                   "tile width %d with %d stages and %d threads does not fit in a block", TX, stages, threads);
     const size_t smem = (size_t)stages * v2_smem<ADJ, EXACT, TX>(img) + V2_SMEM_EXTRA;
-    static bool attr_set = false;
-    static int grid_max[2][2][2] = {};
-    if (!attr_set) {
-        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin()));
-        attr_set = true;
-    }
-    int &gm = grid_max[img][stages - 1][threads == 512];
-    if (!gm) {
-        int nb = 0;
-        RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem));
-        gm = (nb > 0 ? nb : 1) * device_sm_count();
+    static bool attr_set[RTM_MAX_DEVICES] = {};
+    static int grid_max[RTM_MAX_DEVICES][2][2][2] = {};
+    const int dev = rtm_current_device();
+    const int optin = max_smem_optin();
+    const int nsm = device_sm_count();
+    int gm;
+    {
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr_set[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+            attr_set[dev] = true;
+        }
+        int &g = grid_max[dev][img][stages - 1][threads == 512];
+        if (!g) {
+            int nb = 0;
+            RTM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem));
+            g = (nb > 0 ? nb : 1) * nsm;
+        }
+        gm = g;
     }
     int grid = a.ntiles < gm ? a.ntiles : gm;
     if (grid_cap > 0 && grid > grid_cap) grid = grid_cap;

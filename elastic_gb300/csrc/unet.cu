@@ -270,10 +270,14 @@ int gemm_launch(const GemmArgs &g, int splits, cudaStream_t st)
     constexpr int BM = 32 * WM;
     using S = GemmSmem<A_T, B_T, BM, BN>;
     auto kern = k_gemm<A_T, B_T, BN, WM, EPI>;
-    static bool attr = false;
-    if (!attr) {
-        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES));
-        attr = true;
+    static bool attr[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES));
+            attr[dev] = true;
+        }
     }
     dim3 grid((g.M + BM - 1) / BM, (g.N + BN - 1) / BN, splits);
     kern<<<grid, GTHREADS, S::BYTES, st>>>(g);

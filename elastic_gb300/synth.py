@@ -7,6 +7,9 @@ benchmark configurations (no public data is used).
   noise with the given correlation length.
 * ``uneven_survey`` -- shots at a fixed spacing, each on a subgrid of seeded
   width in [wmin, wmax] centred on the source and clipped to the grid.
+* ``single_shot_models`` -- the plain single-shot RTM case: migration model
+  (smoothed three-layer Lame parameters) and the Born perturbation that the
+  5% Gaussian blob of the true model adds to it.
 """
 import numpy as np
 
@@ -57,3 +60,26 @@ def synthetic_traces(n, seed=0):
     """Seeded float32 trace samples (content does not affect the cost)."""
     rng = np.random.default_rng(seed)
     return (1e-3 * rng.standard_normal(n)).astype(np.float32)
+
+
+def gaussian_smooth(a, sigma):
+    """Gaussian smoothing of a plane (sigma in cells), edges extended by their
+    last value so the smoothing does not bend the model at the border."""
+    from scipy.ndimage import gaussian_filter
+    return gaussian_filter(np.asarray(a, np.float64), sigma, mode="nearest")
+
+
+def single_shot_models(nz=200, nx=400, seed=0, blob=0.05, smooth_cells=5.0):
+    """Migration model and true-model perturbation of the single-shot RTM
+    case: three layers Vp 2000/2800/3500 m/s smoothed by a Gaussian of
+    `smooth_cells` cells, Vs = Vp/1.73, Gardner density; the true model
+    multiplies the smoothed Vp by a seeded Gaussian blob of relative size
+    `blob`.  Returns ((rho, lam, mu), (drho, dlam, dmu)) as float32 [nx, nz]
+    planes (z fastest), the perturbation being true minus migration model."""
+    layers = layered_model(nz, nx, seed=seed, blob=0.0)
+    vp0 = gaussian_smooth(layers, smooth_cells)
+    vp1 = layered_model(nz, nx, seed=seed, blob=blob) / layers * vp0
+    m0 = lame_from_vp(vp0)
+    m1 = lame_from_vp(vp1)
+    dm = tuple((b.astype(np.float64) - a.astype(np.float64)).astype(np.float32) for a, b in zip(m0, m1))
+    return m0, dm

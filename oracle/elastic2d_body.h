@@ -671,6 +671,159 @@ void FN(ora_rtm_op2)(int adj, int nz, int nx, int nt, R dx, R dt, int zsrc, int 
     free(m2); free(m3); free(m1_x); free(m1_z); free(a2); free(a3); free(a23); free(src); free(filt);
 }
 
+/* ------------------------------------------------- a6..a13, low memory ---- */
+/* The RTM of ora_rtm_op2 (adj=1) with the working set cut from 11 full
+   histories to 2 (Vx and Vz of the source wavefield, which image_init
+   differentiates in time): the forward stresses and the five adjoint fields
+   live in 3-level windows and S1..S6 are formed one level at a time.  Every
+   level is computed with the same operations in the same order as
+   ora_rtm_op2; only the imaging sums run over it = nt..1 instead of 1..nt,
+   so in double precision the images agree with ora_rtm_op2 to rounding
+   (~1e-15).  Used as the float64 reference where full histories would not
+   fit in host memory (the 2000 x 800 survey geometry). */
+static void FN(s_level)(int nz, int nx, int nt, int it, R dx, R dt, const R *Vx, const R *Vz, R *S)
+{
+    /* S1..S6 of level it (1-based) into S[0..5]; W/image-mod-rtm.f90:26-67 */
+    size_t n = PLANE, i;
+    int iz, ix, k;
+    const R c[5] = {FN(c1), FN(c2), FN(c3), FN(c4), FN(c5)};
+    R at = (R)1.0 / dt, ax = (R)1.0 / dx;
+    const R *vx = Vx + (size_t)(it - 1) * n, *vz = Vz + (size_t)(it - 1) * n;
+    R *S1 = S, *S2 = S + n, *S3 = S + 2 * n, *S4 = S + 3 * n, *S5 = S + 4 * n, *S6 = S + 5 * n;
+    for (i = 0; i < 6 * n; i++) S[i] = 0;
+    if (it <= nt - 1)
+        for (i = 0; i < n; i++) {
+            S1[i] = S1[i] + at * (vx[i + n] - vx[i]);
+            S2[i] = S2[i] + at * (vz[i + n] - vz[i]);
+        }
+#define P2(a, z, x) (a)[I2(z, x)]
+    for (ix = 5; ix <= nx - 5; ix++)
+        for (iz = 5; iz <= nz - 5; iz++) {
+            R p = 0;
+            for (k = 0; k < 5; k++) {
+                R t = c[k] * (P2(vx, iz, ix + 5 - k) - P2(vx, iz, ix - 4 + k));
+                p = k == 0 ? t : p + t;
+            }
+            S4[I2(iz, ix)] = S4[I2(iz, ix)] + p * ax;
+        }
+    for (ix = 5; ix <= nx - 5; ix++)
+        for (iz = 5; iz <= nz - 5; iz++) {
+            R p = 0;
+            for (k = 0; k < 5; k++) {
+                R t = c[k] * (P2(vz, iz + 5 - k, ix) - P2(vz, iz - 4 + k, ix));
+                p = k == 0 ? t : p + t;
+            }
+            S5[I2(iz, ix)] = S5[I2(iz, ix)] + p * ax;
+        }
+    for (i = 0; i < n; i++) S3[i] = S4[i] + S5[i];
+    for (ix = 6; ix <= nx - 5; ix++)
+        for (iz = 6; iz <= nz - 5; iz++) {
+            R p = 0;
+            for (k = 0; k < 5; k++) {
+                R t = c[k] * (P2(vx, iz + 4 - k, ix) - P2(vx, iz - 5 + k, ix));
+                p = k == 0 ? t : p + t;
+            }
+            S6[I2(iz, ix)] = S6[I2(iz, ix)] + p * ax;
+        }
+    for (ix = 6; ix <= nx - 5; ix++)
+        for (iz = 6; iz <= nz - 5; iz++) {
+            R p = 0;
+            for (k = 0; k < 5; k++) {
+                R t = c[k] * (P2(vz, iz, ix + 4 - k) - P2(vz, iz, ix - 5 + k));
+                p = k == 0 ? t : p + t;
+            }
+            S6[I2(iz, ix)] = S6[I2(iz, ix)] + p * ax;
+        }
+#undef P2
+}
+
+void FN(ora_rtm_lowmem)(int nz, int nx, int nt, R dx, R dt, int zsrc, int xsrc, int zrec, R fp, int nsource,
+                        int abc, const R *rho, const R *lambda, const R *mu, R *dm1, R *dm2, R *dm3,
+                        const R *dVx, const R *dVz, const R *dsxx, const R *dszz, const R *dsxz, int exact)
+{
+    size_t n = PLANE, i;
+    int it, ix, f;
+    R *m2 = (R *)malloc(n * sizeof(R)), *m3 = (R *)malloc(n * sizeof(R));
+    R *m1_x = (R *)calloc(n, sizeof(R)), *m1_z = (R *)calloc(n, sizeof(R));
+    R *a2 = (R *)malloc(n * sizeof(R)), *a3 = (R *)malloc(n * sizeof(R)), *a23 = (R *)malloc(n * sizeof(R));
+    R *src = (R *)malloc((size_t)nt * sizeof(R)), *filt = (R *)malloc((size_t)(abc + 5) * sizeof(R));
+    R *Vx = (R *)calloc(n * (size_t)nt, sizeof(R)), *Vz = (R *)calloc(n * (size_t)nt, sizeof(R));
+    R *w = (R *)calloc(3 * 3 * n, sizeof(R));  /* forward stress windows: levels it-2, it-1, it */
+    R *A[5], *S = (R *)malloc(6 * n * sizeof(R));
+    const R *dd[5] = {dVx, dVz, dsxx, dszz, dsxz};
+    for (f = 0; f < 5; f++) A[f] = (R *)calloc(3 * n, sizeof(R));  /* adjoint windows: levels it, it+1, it+2 */
+    memcpy(m2, lambda, n * sizeof(R));
+    memcpy(m3, mu, n * sizeof(R));
+    FN(ora_model_op)(nz, nx, rho, m2, m3, m1_x, m1_z);
+    FN(ora_source_op2)(nt, dt, fp, nsource, src);
+    FN(ora_abc_init)(abc, filt);
+    FN(ora_rtmmod_init)(nz, nx, dx, dt, m1_x, m1_z, m2, m3, a2, a3, a23);
+
+    /* source wavefield (ora_forward): level 1 zero, level 2 the source */
+    if (nt >= 2) {
+        w[n + I2(zsrc, xsrc)] = w[n + I2(zsrc, xsrc)] + dt * src[0];
+        w[3 * n + n + I2(zsrc, xsrc)] = w[3 * n + n + I2(zsrc, xsrc)] + dt * src[0];
+    }
+    for (it = 3; it <= nt; it++) {
+        FN(fwd_level)(nz, nx, 3, 0, Vx + (size_t)(it - 3) * n, Vz + (size_t)(it - 3) * n, w, w + 3 * n,
+                      w + 6 * n, m1_x, m1_z, a2, a3, a23, abc, filt, 1, dt * src[it - 2], zsrc, xsrc);
+        for (f = 0; f < 3; f++) memmove(w + 3 * n * f, w + 3 * n * f + n, 2 * n * sizeof(R));
+    }
+
+    /* adjoint (ora_rtm_op3) with the imaging condition (ora_image_op2) level by level */
+    for (i = 0; i < n; i++) dm1[i] = dm2[i] = dm3[i] = 0;
+#define INJ1(plane, it_)                                                                     \
+    for (ix = 1; ix <= nx; ix++)                                                             \
+        for (f = 0; f < 5; f++)                                                              \
+            A[f][(plane) * n + I2(zrec, ix)] = dd[f][(size_t)((it_) - 1) + (size_t)nt * (size_t)(ix - 1)];
+#define KLEV1(plane)                                                                         \
+    if (exact)                                                                               \
+        for (f = 0; f < 5; f++) FN(ora_K)(nz, nx, abc, filt, A[f] + (plane) * n);
+#define IMG1(plane, it_)                                                                     \
+    FN(s_level)(nz, nx, nt, it_, dx, dt, Vx, Vz, S);                                         \
+    for (i = 0; i < n; i++) {                                                                \
+        size_t a = (plane) * n + i;                                                          \
+        dm1[i] = (dm1[i] + (A[0][a] * S[i])) + (A[1][a] * S[n + i]);                         \
+        dm2[i] = (dm2[i] - (A[2][a] * S[2 * n + i])) - (A[3][a] * S[2 * n + i]);             \
+        dm3[i] = ((dm3[i] - ((A[2][a] * (R)2.0) * S[3 * n + i])) - ((A[3][a] * (R)2.0) * S[4 * n + i])) \
+                 - (A[4][a] * S[5 * n + i]);                                                 \
+    }
+    INJ1(1, nt);
+    KLEV1(1);
+    if (nt >= 2) {
+        INJ1(0, nt - 1);
+        FN(ora_D_c)(nz, nx, A[0], A[2] + n, a23);
+        FN(ora_F_c)(nz, nx, A[0], A[3] + n, a2);
+        FN(ora_H_c)(nz, nx, A[0], A[4] + n, a3);
+        FN(ora_E_c)(nz, nx, A[1], A[2] + n, a2);
+        FN(ora_G_c)(nz, nx, A[1], A[3] + n, a23);
+        FN(ora_J_c)(nz, nx, A[1], A[4] + n, a3);
+        FN(ora_Ax_c)(nz, nx, A[2], A[0] + n, m1_x);
+        FN(ora_Bz_c)(nz, nx, A[3], A[1] + n, m1_z);
+        FN(ora_Bx_c)(nz, nx, A[4], A[0] + n, m1_x);
+        FN(ora_Az_c)(nz, nx, A[4], A[1] + n, m1_z);
+        KLEV1(0);
+    }
+    IMG1(1, nt);
+    if (nt >= 2) { IMG1(0, nt - 1); }
+    for (it = nt - 2; it >= 1; it--) {
+        for (f = 0; f < 5; f++) {
+            memmove(A[f] + n, A[f], 2 * n * sizeof(R));
+            memset(A[f], 0, n * sizeof(R));
+        }
+        INJ1(0, it);
+        FN(ora_rtm_op3_c)(3, nz, nx, A[0], A[1], A[2], A[3], A[4], m1_x, m1_z, a2, a3, a23);
+        KLEV1(0);
+        IMG1(0, it);
+    }
+#undef INJ1
+#undef KLEV1
+#undef IMG1
+    for (f = 0; f < 5; f++) free(A[f]);
+    free(S); free(w); free(Vx); free(Vz);
+    free(m2); free(m3); free(m1_x); free(m1_z); free(a2); free(a3); free(a23); free(src); free(filt);
+}
+
 #undef I2
 #undef I3
 #undef PLANE

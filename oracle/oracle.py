@@ -18,10 +18,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "librefc.so")
-REF_ROOT = "/root/reference"
+REF90_PATH = os.path.join(HERE, "_ref", "libref90.so")
+REF_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
 
 _lib = None
 _ref = None
+_ref90 = None
 
 
 def build(ref=False):
@@ -42,6 +44,10 @@ def lib():
 
 def ref_available():
     return os.path.exists(REF_PATH) or os.path.isdir(REF_ROOT)
+
+
+def ref90_available():
+    return os.path.exists(REF90_PATH) or os.path.isdir(REF_ROOT)
 
 
 def ref():
@@ -211,6 +217,22 @@ def rtm_op2(adj, rho, lam, mu, dm, D, dx, dt, nt, zsrc, xsrc, zrec, fp, abc, nso
     return dm, D
 
 
+def rtm_lowmem(rho, lam, mu, D, dx, dt, nt, zsrc, xsrc, zrec, fp, abc, nsource=250, exact=False):
+    """The RTM of rtm_op2(adj=True) holding 2 histories instead of 11 (see
+    ora_rtm_lowmem): images (drho, dlambda, dmu) of the 5 gathers D [nx,nt].
+    Same arithmetic per level; the imaging sums run backwards in time."""
+    d = rho.dtype
+    nx, nz = rho.shape
+    R = _R(d)
+    dm = [np.zeros((nx, nz), d) for _ in range(3)]
+    D = [np.ascontiguousarray(x, d) for x in D]
+    getattr(lib(), "ora_rtm_lowmem" + _sfx(d))(nz, nx, nt, R(dx), R(dt), zsrc, xsrc, zrec, R(fp), nsource, abc,
+                                               _p(rho), _p(np.ascontiguousarray(lam, d)),
+                                               _p(np.ascontiguousarray(mu, d)), *[_p(x) for x in dm],
+                                               *[_p(x) for x in D], int(exact))
+    return dm
+
+
 # ------------------------------------------------------------------ reference C
 def ref_rtm_op3_c(H, coefs, zrec=1):
     """Run the reference's own rtm_op3_c_ (CPU-only build) in place on float32 histories."""
@@ -221,6 +243,67 @@ def ref_rtm_op3_c(H, coefs, zrec=1):
     f(ctypes.c_int(nt), ctypes.c_int(nz), ctypes.c_int(nx), ctypes.c_int(zrec), *[_p(h) for h in H],
       *[_p(c) for c in coefs])
     return H
+
+
+# ------------------------------------------------------------------ reference Fortran (translated)
+def ref90():
+    """The reference's Fortran RTM modules translated to C (f90c.py), linked
+    with its rtmlib-modC.c and driven like its main program (ref90_driver.c)."""
+    global _ref90
+    if _ref90 is None:
+        if not os.path.exists(REF90_PATH):
+            build(ref=True)
+        _ref90 = ctypes.CDLL(REF90_PATH)
+        _ref90.ref90_get.restype = ctypes.c_long
+    return _ref90
+
+
+REF90_STATE = ("rtm_mod_adj.m1_x", "rtm_mod_adj.m1_z", "rtm_mod_adj.aux_m2_c", "rtm_mod_adj.aux_m3_c",
+               "rtm_mod_adj.aux_m2m3_c", "rtm_mod_adj.source", "abc_mod.filter", "image_mod_rtm.s1",
+               "image_mod_rtm.s2", "image_mod_rtm.s3", "image_mod_rtm.s4", "image_mod_rtm.s5", "image_mod_rtm.s6")
+
+
+def ref90_get(name, shape):
+    r = ref90()
+    out = np.zeros(shape, np.float32)
+    n = r.ref90_get(name.encode(), _p(out), ctypes.c_long(out.size))
+    if n != out.size:
+        raise ValueError("%s holds %d values, %d expected" % (name, n, out.size))
+    return out
+
+
+def ref90_rtm(adj, rho, lam, mu, dm, D, dx, dt, nt, zsrc, xsrc, zrec, fp, abc, forward=False, state=()):
+    """One rtm_init + rtm_op of the reference's own Fortran, as its main
+    program calls them (rtm.f90:150-156), lame=.true., float32.
+
+    adj=True: D (5 gathers [nx,nt]) -> images (drho, dlambda, dmu);
+    adj=False: dm (3 planes [nx,nz]) -> 5 Born gathers.  Returns a dict with
+    "dm", "D", the source-wavefield histories "fwd" ([nt,nx,nz] x5) when
+    forward=True, and the module arrays named in `state` after the call."""
+    r = ref90()
+    nx, nz = rho.shape
+    m = [np.array(x, np.float32, order="C") for x in (rho, lam, mu)]
+    dm = [np.array(x, np.float32, order="C") for x in dm]
+    D = [np.array(x, np.float32, order="C") for x in D]
+    fwd = [np.zeros((nt, nx, nz), np.float32) for _ in range(5)] if forward else None
+    arr = (ctypes.c_void_p * 5)(*[_p(f).value for f in fwd]) if forward else None
+    F = ctypes.c_float
+    st = r.ref90_rtm(int(adj), 1, nz, nx, nt, F(dx), F(dx), F(dt), xsrc, zsrc, zrec, F(fp), abc,
+                     *[_p(x) for x in m], *[_p(x) for x in dm], *[_p(x) for x in D], arr)
+    if st != 0:
+        raise RuntimeError("reference rtm_op returned %d" % st)
+    out = {"dm": dm, "D": D, "fwd": fwd}
+    for name in state:
+        if name.startswith("image_mod_rtm.s"):
+            shape = (nt, nx, nz)
+        elif name == "rtm_mod_adj.source":
+            shape = (nt,)
+        elif name == "abc_mod.filter":
+            shape = (abc + 5,)
+        else:
+            shape = (nx, nz)
+        out[name] = ref90_get(name, shape)
+    return out
 
 
 # ------------------------------------------------------------------ 3D acoustic

@@ -10,7 +10,9 @@ The test calls the entry point through the C-ABI twice in a row (different
 sizes and data, so the second call must not depend on what the first left
 in the shared scratch) and compares each result with rtm_op3_c_, the
 existing host-buffer entry point, in exact arithmetic: the outputs must be
-bit-identical, the tolerance of every exact-mode parity test here.
+bit-identical, the tolerance of every exact-mode parity test here.  A
+third call, repeating the second (so no kernel is loaded for the first time
+during it), must leave the device's free memory unchanged.
 """
 import numpy as np
 import pytest
@@ -43,6 +45,11 @@ def test_noalloc_matches_rtm_op3_c_on_two_calls():
         check(lib.rtm_op3_dev_noalloc(nt, nz, nx, *[ptr(t) for t in Hd], *[ptr(t) for t in Cd], None))
         for got, want in zip(Hd, ref):
             np.testing.assert_array_equal(got.cpu().numpy(), want)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    check(lib.rtm_op3_dev_noalloc(nt, nz, nx, *[ptr(t) for t in Hd], *[ptr(t) for t in Cd], None))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
