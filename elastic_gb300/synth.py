@@ -7,6 +7,9 @@ benchmark configurations (no public data is used).
   noise with the given correlation length.
 * ``uneven_survey`` -- shots at a fixed spacing, each on a subgrid of seeded
   width in [wmin, wmax] centred on the source and clipped to the grid.
+* ``dipping_reflectivity`` -- a seeded relative perturbation of a few
+  dipping reflectors and point scatterers, the "true model minus background"
+  of the survey workloads.
 * ``single_shot_models`` -- the plain single-shot RTM case: migration model
   (smoothed three-layer Lame parameters) and the Born perturbation that the
   5% Gaussian blob of the true model adds to it.
@@ -83,3 +86,21 @@ def single_shot_models(nz=200, nx=400, seed=0, blob=0.05, smooth_cells=5.0):
     m1 = lame_from_vp(vp1)
     dm = tuple((b.astype(np.float64) - a.astype(np.float64)).astype(np.float32) for a, b in zip(m0, m1))
     return m0, dm
+
+
+def dipping_reflectivity(nz, nx, seed=0, n_layers=6, n_points=20, amp=0.05, top=20):
+    """Relative perturbation [nx, nz]: `n_layers` dipping reflectors (one
+    cell thick, slopes within +-15 degrees, amplitudes within +-amp) and
+    `n_points` point scatterers, all below row `top`."""
+    rng = np.random.default_rng(seed)
+    r = np.zeros((nx, nz))
+    x = np.arange(nx)
+    for _ in range(n_layers):
+        z0 = rng.uniform(top, nz - 10)
+        slope = np.tan(np.radians(rng.uniform(-15.0, 15.0)))
+        z = np.round(z0 + slope * (x - nx / 2)).astype(int)
+        ok = (z >= top) & (z < nz - 5)
+        r[x[ok], z[ok]] += rng.uniform(-amp, amp)
+    for _ in range(n_points):
+        r[rng.integers(5, nx - 5), rng.integers(top, nz - 5)] += rng.uniform(-amp, amp)
+    return r

@@ -159,6 +159,7 @@ static void FN(fwd_op)(int nz, int nx, const R *coef, const R *model, R *data, i
 {
     int iz, ix, k;
     const R c[5] = {FN(c1), FN(c2), FN(c3), FN(c4), FN(c5)};
+#pragma omp parallel for private(iz, k) schedule(static)
     for (ix = ixlo; ix <= nx - 5; ix++)
         for (iz = izlo; iz <= nz - 5; iz++) {
             R poly = 0;
@@ -251,28 +252,33 @@ static void FN(fwd_level)(int nz, int nx, int it, int born, R *Vx, R *Vz, R *sxx
     const R *xx2 = sxx + (size_t)(it - 3) * n, *zz2 = szz + (size_t)(it - 3) * n, *xz2 = sxz + (size_t)(it - 3) * n;
 
     /* Vx */
+#pragma omp parallel for schedule(static)
     for (i = 0; i < n; i++) vx[i] = born ? (have2 ? vx[i] + vx2[i] : vx[i]) : (have2 ? vx2[i] : 0);
     FN(ora_Ax)(nz, nx, m1_x, xx1, vx);
     FN(ora_Bx)(nz, nx, m1_x, xz1, vx);
     if (sponge) FN(ora_K)(nz, nx, abc, filter, vx);
     /* Vz */
+#pragma omp parallel for schedule(static)
     for (i = 0; i < n; i++) vz[i] = born ? (have2 ? vz[i] + vz2[i] : vz[i]) : (have2 ? vz2[i] : 0);
     FN(ora_Az)(nz, nx, m1_z, xz1, vz);
     FN(ora_Bz)(nz, nx, m1_z, zz1, vz);
     if (sponge) FN(ora_K)(nz, nx, abc, filter, vz);
     /* sigmaxx */
+#pragma omp parallel for schedule(static)
     for (i = 0; i < n; i++) xx[i] = born ? (have2 ? xx[i] + xx2[i] : xx[i]) : (have2 ? xx2[i] : 0);
     if (!born) xx[I2(zsrc, xsrc)] = xx[I2(zsrc, xsrc)] + srcval;
     FN(ora_D)(nz, nx, aux_m2m3, vx1, xx);
     FN(ora_E)(nz, nx, aux_m2, vz1, xx);
     if (sponge) FN(ora_K)(nz, nx, abc, filter, xx);
     /* sigmazz */
+#pragma omp parallel for schedule(static)
     for (i = 0; i < n; i++) zz[i] = born ? (have2 ? zz[i] + zz2[i] : zz[i]) : (have2 ? zz2[i] : 0);
     if (!born) zz[I2(zsrc, xsrc)] = zz[I2(zsrc, xsrc)] + srcval;
     FN(ora_F)(nz, nx, aux_m2, vx1, zz);
     FN(ora_G)(nz, nx, aux_m2m3, vz1, zz);
     if (sponge) FN(ora_K)(nz, nx, abc, filter, zz);
     /* sigmaxz */
+#pragma omp parallel for schedule(static)
     for (i = 0; i < n; i++) xz[i] = born ? (have2 ? xz[i] + xz2[i] : xz[i]) : (have2 ? xz2[i] : 0);
     FN(ora_H)(nz, nx, aux_m3, vx1, xz);
     FN(ora_J)(nz, nx, aux_m3, vz1, xz);
@@ -505,6 +511,7 @@ void FN(ora_rtm_op3_c)(int nt, int nz, int nx, R *Vx0, R *Vz0, R *sxx0, R *szz0,
 #define M1Z(z, x) FN(mask_get)(nz, nx, m1_z, z, x, 5, zhi, xlo4, xhi)
 #define FLD(f, z, x, t) (((z) < 0 || (z) >= nz || (x) < 0 || (x) >= nx) ? (R)0 : (f)[(size_t)(z) + (size_t)nz * (size_t)(x) + n * (size_t)(t)])
     for (it = nt - 3; it >= 0; it--) {
+#pragma omp parallel for private(iz, k) schedule(static)
         for (ix = 0; ix < nx; ix++)
             for (iz = 0; iz < nz; iz++) {
                 size_t o = (size_t)iz + (size_t)nz * (size_t)ix + n * (size_t)it;
@@ -697,6 +704,7 @@ static void FN(s_level)(int nz, int nx, int nt, int it, R dx, R dt, const R *Vx,
             S2[i] = S2[i] + at * (vz[i + n] - vz[i]);
         }
 #define P2(a, z, x) (a)[I2(z, x)]
+#pragma omp parallel for private(iz, k) schedule(static)
     for (ix = 5; ix <= nx - 5; ix++)
         for (iz = 5; iz <= nz - 5; iz++) {
             R p = 0;
@@ -706,6 +714,7 @@ static void FN(s_level)(int nz, int nx, int nt, int it, R dx, R dt, const R *Vx,
             }
             S4[I2(iz, ix)] = S4[I2(iz, ix)] + p * ax;
         }
+#pragma omp parallel for private(iz, k) schedule(static)
     for (ix = 5; ix <= nx - 5; ix++)
         for (iz = 5; iz <= nz - 5; iz++) {
             R p = 0;
@@ -716,6 +725,7 @@ static void FN(s_level)(int nz, int nx, int nt, int it, R dx, R dt, const R *Vx,
             S5[I2(iz, ix)] = S5[I2(iz, ix)] + p * ax;
         }
     for (i = 0; i < n; i++) S3[i] = S4[i] + S5[i];
+#pragma omp parallel for private(iz, k) schedule(static)
     for (ix = 6; ix <= nx - 5; ix++)
         for (iz = 6; iz <= nz - 5; iz++) {
             R p = 0;
@@ -725,6 +735,7 @@ static void FN(s_level)(int nz, int nx, int nt, int it, R dx, R dt, const R *Vx,
             }
             S6[I2(iz, ix)] = S6[I2(iz, ix)] + p * ax;
         }
+#pragma omp parallel for private(iz, k) schedule(static)
     for (ix = 6; ix <= nx - 5; ix++)
         for (iz = 6; iz <= nz - 5; iz++) {
             R p = 0;
@@ -781,6 +792,7 @@ void FN(ora_rtm_lowmem)(int nz, int nx, int nt, R dx, R dt, int zsrc, int xsrc, 
         for (f = 0; f < 5; f++) FN(ora_K)(nz, nx, abc, filt, A[f] + (plane) * n);
 #define IMG1(plane, it_)                                                                     \
     FN(s_level)(nz, nx, nt, it_, dx, dt, Vx, Vz, S);                                         \
+    _Pragma("omp parallel for schedule(static)")                                             \
     for (i = 0; i < n; i++) {                                                                \
         size_t a = (plane) * n + i;                                                          \
         dm1[i] = (dm1[i] + (A[0][a] * S[i])) + (A[1][a] * S[n + i]);                         \

@@ -20,17 +20,32 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "librefc.so")
 REF90_PATH = os.path.join(HERE, "_ref", "libref90.so")
 REF_ROOT = os.environ.get("REFERENCE_ROOT", "/root/reference")
+# unmodified copy of the reference's source files of this path (make stage)
+STAGED_ROOT = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
 
 _lib = None
 _ref = None
 _ref90 = None
 
 
+def ref_root():
+    """The reference tree, else its staged copy in baseline/_ref, else None."""
+    for r in (REF_ROOT, STAGED_ROOT):
+        if os.path.isdir(os.path.join(r, "2d_rtm_restart", "Src_working")):
+            return r
+    return None
+
+
 def build(ref=False):
-    """Compile liboracle.so (and, when the reference tree exists, _ref)."""
+    """Compile liboracle.so (and, when the reference's sources exist, _ref).
+    Where the reference tree exists its sources are also staged into
+    baseline/_ref for machines that lack it."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     if ref and os.path.isdir(REF_ROOT):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFROOT=" + REF_ROOT], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "stage", "REFROOT=" + REF_ROOT], check=True)
+    root = ref_root() if ref else None
+    if root:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REFROOT=" + os.path.abspath(root)], check=True)
 
 
 def lib():
@@ -43,11 +58,11 @@ def lib():
 
 
 def ref_available():
-    return os.path.exists(REF_PATH) or os.path.isdir(REF_ROOT)
+    return os.path.exists(REF_PATH) or ref_root() is not None
 
 
 def ref90_available():
-    return os.path.exists(REF90_PATH) or os.path.isdir(REF_ROOT)
+    return os.path.exists(REF90_PATH) or ref_root() is not None
 
 
 def ref():
