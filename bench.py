@@ -14,9 +14,24 @@ fused imaging condition, stacking.  The default --steps 16 covers the 64-shot
 survey once.  Metric: Gcell-updates/s counting the forward and the adjoint
 propagation (2 x nz x width x nt per shot); shots/s is reported beside it.
 
---impl reference times the reference's CPU path (the C restatement of the
-Fortran/C in oracle/, or oracle/_ref where the reference compiled) on the host
-cores: one shot per core on the same grid over a truncated time window.
+The same JSON line carries, from the same run:
+- error_vs_fp64: the headline path's error (FP16 snapshots, FP32 fields)
+  against the float64 oracle, per image, on the survey's widest group over a
+  truncated window, with Born-modelled traces;
+- secondary: bounded samples of the other workloads, each with its own
+  clocks and roofline -- the 3D acoustic propagator (1024 x 1024 x 512), the
+  learned preconditioner (training rate and learned-vs-LSRTM-10 time to
+  residual, reduced pair count) and one group of the 256-shot survey
+  (checkpoint-restart);
+- cpu_baseline: the reference's own RTM path on the host cores.
+
+--impl reference times the reference's CPU path on the host cores: its
+Fortran modules executed through oracle/f90c.py with its C recursion
+(oracle/_ref, built where the reference's sources are present), else the
+oracle's C restatement; one shot per core on the survey grid over a
+truncated time window.  It also times the reference's own CUDA adjoint
+kernel (rtmlib-modC-gpu.cu built for sm_103a) beside this library's on the
+single-shot grid.
 """
 import argparse
 import json
@@ -292,19 +307,114 @@ def run_gpu(args):
                      "traffic": (round(tpc * cells_per_launch) if tpc else None)},
         "clocks": clocks,
     }
-    if world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
-    print(json.dumps(line), flush=True)
+    line["_survey"] = (rho, lam, mu, x0, nxs, xsrc, zs, zr, widest, st["march"], st["march_adj"])
+    eng.close()
+    del traces_dev, img_dev
+    torch.cuda.empty_cache()
+    return line
+
+
+# --------------------------------------------------------------- error block
+def _fp64_shot(spec):
+    """float64 RTM of one shot (oracle, ora_rtm_lowmem) for error_block."""
+    nthreads, rho, lam, mu, D, kw = spec
+    os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    return O.rtm_lowmem(rho, lam, mu, D, **kw)
+
+
+def error_block(survey, nt_err=600):
+    """The headline path's error against the float64 oracle.
+
+    The widest group of the survey is migrated by the batch engine on the
+    kernels the autotuner chose (FP32 fields, FP16 source snapshots, Kahan
+    imaging) over a truncated window of nt_err levels, from the Vx, Vz traces
+    that the drop-in Born operator (rtm_op_c_, linear) models from the true
+    model: the background times a dipping-reflector perturbation between
+    rows 46 and 90 (synth.dipping_reflectivity: just below the 45-row sponge,
+    so that its reflections reach the receivers within the window).  Every
+    shot is migrated by the float64
+    oracle (ora_rtm_lowmem: the reference's RTM algorithm in double
+    precision) and stacked; the relative L2 error of each image is
+    reported.  The full window (nt = 6000) would need 100 GB of float64
+    history per shot in the oracle.  The oracle's shots run in parallel
+    processes (spawned), their threads sharing the host cores."""
+    import multiprocessing as mp
+    from elastic_gb300 import rtm as R
+    from elastic_gb300 import synth
+    from elastic_gb300.batch import BatchRTM
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    c = CFG
+    rho, lam, mu, x0, nxs, xsrc, zs, zr, widest, march_f, march_a = survey
+    s0, k = widest
+    sel = list(range(s0, s0 + k))
+    nz, nx, dx, dt = c["nz"], c["nx"], c["dx"], c["dt"]
+    refl = synth.dipping_reflectivity(nz, nx, seed=c["seed"], top=46, bottom=90)
+    traces = []
+    R.set_exact(False)
+    try:
+        for s in sel:
+            a, w = int(x0[s] - 1), int(nxs[s])
+            sl = lambda m: np.ascontiguousarray(m[a:a + w])
+            op = R.RtmOperator(nz, dx, w, dx, dt, int(xsrc[s] - a), int(zs[s]), int(zr[s]), c["fp"], nt_err, c["abc"],
+                               sl(rho), sl(lam), sl(mu), nsource=c["nsource"], linear=True)
+            dm = [np.ascontiguousarray((refl[a:a + w] * m[a:a + w]).astype(np.float32)) for m in (rho, lam, mu)]
+            D = [np.zeros((w, nt_err), np.float32) for _ in range(5)]
+            op.rtm_op(False, *dm, *D)
+            traces.append(D[:2])
+    finally:
+        R.set_exact(True)
+    eng = BatchRTM(nz, nx, nt_err, dx, dt, c["fp"], c["abc"], rho, lam, mu, x0[sel], nxs[sel], xsrc[sel], zs[sel],
+                   zr[sel], comp_mask=3, group_max=k, nsource=c["nsource"])
+    eng.set_march((1 if march_f else 0) | (2 if march_a else 0))
+    img = np.zeros(3 * nz * nx, np.float32)
+    eng.migrate(0, k, np.concatenate([np.concatenate([t[0].ravel(), t[1].ravel()]) for t in traces]), img)
+    eng.close()
+    img = img.reshape(3, nx, nz)
+    t0 = time.perf_counter()
+    nthreads = max(1, (os.cpu_count() or 1) // len(sel))
+    specs = []
+    for j, s in enumerate(sel):
+        a, w = int(x0[s] - 1), int(nxs[s])
+        sl = lambda m: np.ascontiguousarray(m[a:a + w], np.float64)
+        D = [traces[j][0].astype(np.float64), traces[j][1].astype(np.float64)] + [np.zeros((w, nt_err))] * 3
+        kw = dict(dx=dx, dt=dt, nt=nt_err, zsrc=int(zs[s]), xsrc=int(xsrc[s] - a), zrec=int(zr[s]), fp=c["fp"],
+                  abc=c["abc"], nsource=c["nsource"])
+        specs.append((nthreads, sl(rho), sl(lam), sl(mu), D, kw))
+    with mp.get_context("spawn").Pool(len(sel)) as pool:
+        dms = pool.map(_fp64_shot, specs)
+    ref = [np.zeros((nx, nz)) for _ in range(3)]
+    for j, s in enumerate(sel):
+        a, w = int(x0[s] - 1), int(nxs[s])
+        for i in range(3):
+            ref[i][a:a + w] += dms[j][i]
+    oracle_s = time.perf_counter() - t0
+    rel = [float(np.linalg.norm(img[i].astype(np.float64) - ref[i]) / np.linalg.norm(ref[i])) for i in range(3)]
+    return {"drho": float("%.3g" % rel[0]), "dlambda": float("%.3g" % rel[1]), "dmu": float("%.3g" % rel[2]),
+            "measure": "relative L2 of each stacked image against the float64 oracle",
+            "window_nt": nt_err, "of_nt": c["nt"], "shots": [int(v) for v in nxs[sel]],
+            "path": "batch engine as benchmarked: FP32 fields, FP16 per-level-scaled source snapshots, "
+                    "Kahan-compensated imaging; %s forward, %s adjoint" % ("marching" if march_f else "tile",
+                                                                           "marching" if march_a else "tile"),
+            "traces": "Vx, Vz Born-modelled (linear, rtm_op_c_) from the background times a dipping-reflector "
+                      "perturbation (seeded) between rows 46 and 90",
+            "oracle": "ora_rtm_lowmem float64 (the reference's RTM algorithm), %d host threads, %.0f s"
+                      % (os.cpu_count() or 1, oracle_s)}
 
 
 # --------------------------------------------------------------- CPU arm
 def _cpu_worker(spec):
-    """One shot of the RTM on its subgrid, truncated to nt steps, in the C
-    oracle (the reference's algorithm: full-history forward, image_init,
-    rtm_op3 + C recursion, imaging)."""
+    """One shot of the RTM (forward source wavefield, image_init, adjoint
+    recursion, imaging) on its subgrid, truncated to nt levels.  kind
+    "reference": the reference's own Fortran modules (executed through
+    oracle/f90c.py) and its C recursion, exactly as its main program calls
+    them; kind "port": the oracle's C restatement of the same code."""
+    os.environ["OMP_NUM_THREADS"] = "1"
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    nz, w, nt, seed = spec
+    nz, w, nt, seed, kind = spec
     c = CFG
     from elastic_gb300 import synth
     vp = synth.smooth_random_model(nz, w, c["dx"], 200.0, 1800.0, 4000.0, seed=seed)
@@ -313,40 +423,135 @@ def _cpu_worker(spec):
     D = [(1e-3 * rng.standard_normal((w, nt))).astype(np.float32) for _ in range(5)]
     dm = [np.zeros((w, nz), np.float32) for _ in range(3)]
     t0 = time.perf_counter()
-    O.rtm_op2(True, rho, lam, mu, dm, D, np.float32(c["dx"]), np.float32(c["dt"]), nt, c["zsrc"], w // 2,
-              c["zrec"], np.float32(c["fp"]), c["abc"], c["nsource"])
+    if kind == "reference":
+        O.ref90_rtm(True, rho, lam, mu, dm, D, c["dx"], c["dt"], nt, c["zsrc"], w // 2, c["zrec"], c["fp"], c["abc"])
+    else:
+        O.rtm_op2(True, rho, lam, mu, dm, D, np.float32(c["dx"]), np.float32(c["dt"]), nt, c["zsrc"], w // 2,
+                  c["zrec"], np.float32(c["fp"]), c["abc"], c["nsource"])
     return time.perf_counter() - t0, 2 * nz * w * nt
 
 
 def cpu_baseline(seconds_target=15.0):
+    """The reference's RTM path on the host cores, one shot per core (as many
+    as the memory of its full histories allows), over a truncated window of
+    nt = 59 levels (the reference's C divides by nt/59 in its progress
+    output, so 59 is its shortest window)."""
     import multiprocessing as mp
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    O.build()
-    cores = os.cpu_count() or 1
-    nz, w = CFG["nz"], 1300  # the mean subgrid width of the survey
-    # calibrate the window on one core, then one shot per core
-    t, cells = _cpu_worker((nz, w, 8, 0))
-    rate1 = cells / t
-    nt = int(max(8, min(96, seconds_target * rate1 / (2 * nz * w))))
-    mem_gb = 11 * nz * w * nt * 4 / 1e9
+    O.build(ref=True)
+    kind = "reference" if os.path.exists(O.REF90_PATH) else "port"
+    nproc = os.cpu_count() or 1
+    nz, w, nt = CFG["nz"], 1300, 59  # 1300: the mean subgrid width of the survey
+    # full histories: 11 volumes of nz*w*nt (plus 5 padded copies in the reference's C)
+    mem_gb = (16 if kind == "reference" else 11) * nz * w * nt * 4 / 1e9
     try:
         avail = os.sysconf("SC_AVPHYS_PAGES") * os.sysconf("SC_PAGE_SIZE") / 1e9
     except Exception:
         avail = 64.0
-    procs = int(max(1, min(cores, 0.5 * avail // max(mem_gb, 1e-3))))
+    procs = int(max(1, min(nproc, 0.5 * avail // max(mem_gb, 1e-3))))
     ctx = mp.get_context("spawn")
+    res, rounds = [], 0
     t0 = time.perf_counter()
     with ctx.Pool(procs) as pool:
-        res = pool.map(_cpu_worker, [(nz, w, nt, s) for s in range(procs)])
+        # rounds of one shot per process until the sample lasts seconds_target
+        while rounds < 8 and (rounds == 0 or time.perf_counter() - t0 < seconds_target):
+            res += pool.map(_cpu_worker, [(nz, w, nt, rounds * procs + s, kind) for s in range(procs)])
+            rounds += 1
     wall = time.perf_counter() - t0
     total = sum(r[1] for r in res)
-    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "librefc.so")) else "port"
-    return {"value": round(total / wall / 1e9, 5), "unit": "Gcell/s", "cores": procs, "kind": "port",
-            "sample": f"{procs} shots (one per core) of the RTM (forward + adjoint + imaging, full-history "
-                      f"reference algorithm, C oracle restating the Fortran and rtmlib-modC.c) on {nz}x{w} "
-                      f"subgrids, nt window {nt} of 6000 (per-step rate)",
-            "ref_c_built_here": kind == "reference"}
+    what = ("the reference's own Fortran modules (executed through oracle/f90c.py) with its C recursion "
+            "rtmlib-modC.c" if kind == "reference" else "the oracle's C restatement of the reference's Fortran and C")
+    return {"value": round(total / wall / 1e9, 5), "unit": "Gcell/s", "cores": procs, "nproc": nproc, "kind": kind,
+            "sample": f"{len(res)} shots ({rounds} rounds of one per process, {procs} processes, single-threaded as "
+                      f"the reference) of the RTM "
+                      f"(forward + adjoint + imaging, full histories) by {what}, on {nz}x{w} subgrids of the "
+                      f"survey, nt window {nt} of {CFG['nt']} (per-level rate); {wall:.0f} s"}
+
+
+def _ref_gpu_worker(which):
+    """The adjoint recursion rtm_op3_c_ on the single-shot grid (200 x 400,
+    nt = 2000) through `which`'s library: "reference" = the reference's
+    rtmlib-modC.c with its own gpu.h (levels nt-3..nt-9 on the CPU, the rest
+    by its CUDA kernel rtmlib-modC-gpu.cu, whole histories copied to the
+    device and back); "ours" = libelastic_rtm.so's drop-in rtm_op3_c_ (exact
+    arithmetic) and, on the reference's padded layout, its rtm_gpu_func.
+    Returns wall seconds of the whole call and device seconds per level."""
+    import ctypes
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from elastic_gb300 import synth
+    nz, nx, nt = 200, 400, 2000
+    (rho, lam, mu), _ = synth.single_shot_models(nz=nz, nx=nx)
+    coefs = O.coefficients(rho, lam, mu, np.float32(10.0), np.float32(1e-3))
+    rng = np.random.default_rng(1)
+    H = [(1e-3 * rng.standard_normal((nt, nx, nz))).astype(np.float32) for _ in range(5)]
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    out = {}
+    if which == "reference":
+        lib = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "librefgpu.so"))
+        err = tempfile.TemporaryFile(mode="w+b")
+        saved = os.dup(2)
+        os.dup2(err.fileno(), 2)
+        try:
+            t0 = time.perf_counter()
+            lib.rtm_op3_c_(nt, nz, nx, 1, *[P(h) for h in H], *[P(c) for c in coefs])
+            out["wall_s"] = time.perf_counter() - t0
+        finally:
+            os.dup2(saved, 2)
+        err.seek(0)
+        text = err.read().decode(errors="replace")
+        for ln in text.splitlines():
+            if ln.startswith("GPU time per step"):
+                out["device_s_per_level"] = float(ln.split()[-1])
+        out["levels_on_gpu"] = nt - 9
+    else:
+        from elastic_gb300 import rtm as R
+        from elastic_gb300._lib import load
+        R.set_exact(True)
+        t0 = time.perf_counter()
+        R.rtm_op3(nt, nz, nx, 1, *H, *coefs)
+        out["wall_s"] = time.perf_counter() - t0
+        # rtm_gpu_func on the reference's padded layout, levels nt-10..0
+        pad = lambda a: np.pad(a, [(5, 5)] * a.ndim)
+        Hp = [pad(h) for h in H]
+        Cp = [pad(c) for c in coefs]
+        lib = load()
+        ps = np.zeros(1, np.float64)
+        lib.rtm_gpu_init(nt, nz, nx)
+        lib.rtm_gpu_func(nt - 10, nt, nz, nx, *[P(h) for h in Hp], *[P(c) for c in Cp], None, P(ps))
+        lib.rtm_gpu_final()
+        out["device_s_per_level"] = float(ps[0])
+        out["levels_on_gpu"] = nt - 9
+    return out
+
+
+def ref_gpu_comparison():
+    """The reference's CUDA adjoint and this library's, same machine, same
+    grid; each in a process of its own."""
+    import multiprocessing as mp
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "librefgpu.so")):
+        return {"unavailable": "the reference's CUDA file was not built (its sources are absent)"}
+    ctx = mp.get_context("spawn")
+    res = {}
+    for which in ("reference", "ours"):
+        with ctx.Pool(1) as pool:
+            res[which] = pool.apply(_ref_gpu_worker, (which,))
+    cells = 200 * 400
+    r, o = res["reference"], res["ours"]
+    return {"workload": "adjoint recursion rtm_op3_c_ on the single-shot grid 200 x 400, nt = 2000, host "
+                        "histories in and out",
+            "reference_kernel": "rtmlib-modC-gpu.cu built unchanged for sm_103a (cudaThreadSynchronize mapped to "
+                                "cudaDeviceSynchronize); 20x20 tiles, one launch and synchronisation per level",
+            "reference_device_ms_per_level": round(1e3 * r.get("device_s_per_level", float("nan")), 4),
+            "ours_device_ms_per_level": round(1e3 * o["device_s_per_level"], 4),
+            "reference_gcells_per_level_device": round(cells / r.get("device_s_per_level", float("nan")) / 1e9, 3),
+            "ours_gcells_per_level_device": round(cells / o["device_s_per_level"] / 1e9, 3),
+            "reference_whole_call_s": round(r["wall_s"], 3), "ours_whole_call_s": round(o["wall_s"], 3),
+            "note": "device time per level: the reference's own CUDA-event timing of its kernel loop and this "
+                    "library's rtm_gpu_func on the same padded layout; whole call: rtm_op3_c_ wall time including "
+                    "padding, host-device copies of all histories and the reference's CPU levels"}
 
 
 def run_reference(args):
@@ -361,6 +566,11 @@ def run_reference(args):
                                    + cb["sample"] + ")"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_ref_gpu:
+        try:
+            line["reference_gpu"] = ref_gpu_comparison()
+        except Exception as e:  # the comparator is informative; the CPU arm stands without it
+            line["reference_gpu"] = {"unavailable": "%s: %s" % (type(e).__name__, e)}
     print(json.dumps(line), flush=True)
 
 
@@ -370,7 +580,7 @@ CFG4 = dict(n1=512, n2=1024, n3=1024, d=10.0, dt=1e-3, nt=3000, vmin=1500.0, vma
 CFL_LIMIT_3D = 0.4419  # 2 / sqrt(3 * 6.8267): leapfrog limit of the 10th-order 3D Laplacian
 
 
-def run_acoustic3d(args):
+def acoustic3d_block(args, steps, warmup, nt=None, n3=None):
     """3D acoustic 10th-order forward modelling,
     1024 x 1024 x 512 cells, dx=10 m, dt=1 ms, 20 Hz Ricker point source,
     1024 x 1024 surface receivers (interior), 30-cell sponge.  One step = a
@@ -379,10 +589,10 @@ def run_acoustic3d(args):
     from elastic_gb300 import acoustic3d as A
     from elastic_gb300._lib import load
     c = dict(CFG4)
-    if args.n3:
-        c["n3"] = args.n3
-    if args.nt:
-        c["nt"] = args.nt
+    if n3:
+        c["n3"] = n3
+    if nt:
+        c["nt"] = nt
     n1, n2, n3 = c["n1"], c["n2"], c["n3"]
     dev = "cuda:0"
     g = torch.Generator(device=dev).manual_seed(c["seed"])
@@ -407,13 +617,13 @@ def run_acoustic3d(args):
     wav = R.source_op2(window, c["dt"], c["fp"], 50)
     src = (11, n2 // 2, n3 // 2)
     A.set_shape(args.tile3d, 0)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         A.forward(vel2, (c["d"],) * 3, c["damp_a"], c["damp_b"], src, wav[:8], c["zr"], on_device=True)
     torch.cuda.synchronize()
     cells = (n1 - 10) * (n2 - 10) * (n3 - 10)
     total_ms = 0.0
     with ClockSampler(0) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             _, _, _, ms = A.forward(vel2, (c["d"],) * 3, c["damp_a"], c["damp_b"], src, wav, c["zr"], on_device=True)
             total_ms += ms
         torch.cuda.synchronize()
@@ -423,10 +633,12 @@ def run_acoustic3d(args):
     te = time.perf_counter()
     A.forward(vel_h, (c["d"],) * 3, c["damp_a"], c["damp_b"], src, wav, c["zr"])
     e2e_s = time.perf_counter() - te
+    del vel2
+    torch.cuda.empty_cache()
     peak, kind = measured_peaks()
-    rate = cells * window * args.steps / (total_ms * 1e-3) / 1e9
+    rate = cells * window * steps / (total_ms * 1e-3) / 1e9
     line = {"metric": "Gcell-updates/s", "value": round(rate, 2), "unit": "Gcell/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 2),
+            "steps": steps, "warmup": warmup, "ms_per_step": round(total_ms / steps, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"3D acoustic 10th-order forward modelling, {n1}x{n2}x{n3}, "
                                    f"one step = {window} time steps, receivers on plane z={c['zr']}",
@@ -434,12 +646,16 @@ def run_acoustic3d(args):
                        "cfl_limit": CFL_LIMIT_3D, "tile_x": args.tile3d, "inputs_vs_l2": "inputs larger than L2"},
             "e2e": {"value": round(cells * window / e2e_s / 1e9, 2), "unit": "Gcell/s",
                     "h2d_bytes_per_step": 4 * n1 * n2 * n3, "d2h_bytes_per_step": 4 * window * n2 * n3 + 8 * n1 * n2 * n3},
-            "gpu_launches": window * args.steps,
+            "gpu_launches": window * steps,
             "roofline": {"bound": "hbm", "achieved": round(rate * 16, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(rate * 16 / peak, 4), "peak_kind": kind, "kernel": "k_acoustic3d_p (16 B/cell)",
                          "traffic": None},
             "clocks": clocks}
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_acoustic3d(args):
+    print(json.dumps(acoustic3d_block(args, args.steps, args.warmup, args.nt, args.n3)), flush=True)
 
 
 # --------------------------------------------------------------- config 3
@@ -462,7 +678,7 @@ def unet_train_flops(table, batch):
     return f
 
 
-def run_precond(args):
+def precond_block(args, steps, warmup, pairs=None, train_steps=None, ntest=None, nt=None):
     """The learned preconditioner workload.  (Reflectivity,
     migrated image) pairs from the project's Born modelling and migration on
     256 x 256 windows of the smoothed single-shot background, U-Net training
@@ -472,10 +688,14 @@ def run_precond(args):
     import torch
     from elastic_gb300 import precond as PC
     c = dict(CFG3)
-    if args.pairs:
-        c["pairs"] = args.pairs
-    if args.nt:
-        c["nt"] = args.nt
+    if pairs:
+        c["pairs"] = pairs
+    if train_steps:
+        c["train_steps"] = train_steps
+    if ntest:
+        c["ntest"] = ntest
+    if nt:
+        c["nt"] = nt
     rho, lam, mu = PC.background_window(c["nx"], c["nz"], nz_model=c["nz_model"])
     pb = PC.Problem(rho, lam, mu, c["dx"], c["dt"], c["nt"], c["nx"] // 2 + 1, c["zsrc"], c["zrec"], c["fp"], c["abc"],
                     c["nsource"])
@@ -497,18 +717,20 @@ def run_precond(args):
         idx = torch.randint(0, ntr, (c["batch"],), generator=g).cuda()
         return pc.net.train_step(x.index_select(0, idx).contiguous(), y.index_select(0, idx).contiguous(), lr=c["lr"])
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        losses = [step() for _ in range(args.steps)]
+        losses = [step() for _ in range(steps)]
         torch.cuda.synchronize()
         train_s = time.perf_counter() - t0
     clocks = clk.summary()
     # rest of the training budget (untimed)
-    for _ in range(max(0, c["train_steps"] - args.steps - args.warmup)):
+    t1 = time.perf_counter()
+    for _ in range(max(0, c["train_steps"] - steps - warmup)):
         losses.append(step())
+    rest_s = time.perf_counter() - t1
     # learned migration vs LSRTM-10 on held-out pairs
     res_nn, res_ls, res_rtm, t_nn, t_ls, refl_err = [], [], [], [], [], []
     for k in range(nte):
@@ -525,21 +747,25 @@ def run_precond(args):
         t_ls.append(tl)
     table = pc.net.layer_table()
     flops = unet_train_flops(table, c["batch"])
-    tflops = flops * args.steps / train_s / 1e12
+    tflops = flops * steps / train_s / 1e12
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, kind = (json.load(open(pk))["bf16_tflops"], "measured") if os.path.exists(pk) else (1900.0, "fallback")
-    rate = c["batch"] * args.steps / train_s
+    rate = c["batch"] * steps / train_s
+    train_gb = x.numel() * 8 / 1e9
+    del x, y
+    torch.cuda.empty_cache()
     line = {"metric": "training images/s (learned preconditioner)", "value": round(rate, 2), "unit": "images/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * train_s / args.steps, 3),
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": round(1e3 * train_s / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": f"learned preconditioner: 3->3 channel 4-level U-Net, "
                                    f"{pc.net.nparam} parameters, {c['nx']}x{c['nz']} patches, batch {c['batch']}, "
                                    f"Adam lr {c['lr']}; {ntr} training pairs (Born-modelled then migrated, one shot, "
                                    f"Vx/Vz receivers, nt={c['nt']})",
-                       "pair_generation_s": round(gen_s, 1), "train_steps": len(losses) + args.warmup,
+                       "pair_generation_s": round(gen_s, 1), "train_steps": len(losses) + warmup,
+                       "training_s": round(train_s + rest_s, 1),
                        "input_normalisation": "per channel and depth row RMS over the imaging region, clipped to +-20",
                        "loss_first_last": [round(losses[0], 5), round(float(np.mean(losses[-50:])), 5)],
-                       "inputs_vs_l2": "training set (%.1f GB) larger than L2" % (x.numel() * 8 / 1e9)},
+                       "inputs_vs_l2": "training set (%.1f GB) larger than L2" % train_gb},
             "time_to_residual": {"learned_residual": round(float(np.mean(res_nn)), 4),
                                  "lsrtm10_residual": round(float(np.mean(res_ls)), 4),
                                  "rtm_residual": round(float(np.mean(res_rtm)), 4),
@@ -557,6 +783,93 @@ def run_precond(args):
                          "frac": round(tflops / peak, 4), "peak_kind": kind + " bf16 (cuBLAS burst)",
                          "kernel": "k_gemm (mma.sync m16n8k16 BF16) over the whole training step", "traffic": None},
             "clocks": clocks}
+    return line
+
+
+def run_precond(args):
+    print(json.dumps(precond_block(args, args.steps, args.warmup, pairs=args.pairs, nt=args.nt)), flush=True)
+
+
+# --------------------------------------------------------------- config 5 sample
+def c5_block(args, warmup=1, steps=1):
+    """One 4-shot group of the 256-shot survey (6000 x 2000 cells, dx=5 m,
+    dt=0.4 ms, nt=10000, subgrids 1000-6000 wide) migrated end to end in
+    checkpoint-restart mode (all levels' FP16 snapshots would need ~1 TB), on
+    the marching kernels; timed like the headline (device time of the group,
+    forward and adjoint counted)."""
+    import torch
+    from elastic_gb300 import synth
+    from elastic_gb300.batch import BatchRTM
+    c = dict(CFG5)
+    vp = synth.smooth_random_model(c["nz"], c["nx"], c["dx"], 200.0, 1800.0, 4000.0, seed=c["seed"])
+    rho, lam, mu = synth.lame_from_vp(vp)
+    x0, nxs, xsrc = synth.uneven_survey(c["nx"], c["nshots"], c["spacing"], c["wmin"], c["wmax"], seed=c["seed"])
+    n = len(nxs)
+    zs, zr = np.full(n, c["zsrc"], np.int32), np.full(n, c["zrec"], np.int32)
+    eng = BatchRTM(c["nz"], c["nx"], c["nt"], c["dx"], c["dt"], c["fp"], c["abc"], rho, lam, mu, x0, nxs, xsrc, zs, zr,
+                   comp_mask=c["comp_mask"], group_max=4, nsource=c["nsource"])
+    eng.set_march(3)
+    groups = eng.groups()
+    # a group of mean width: the sample stands for the survey's average group
+    mean_w = float(nxs.sum()) / len(groups)
+    g = min(groups, key=lambda q: abs(int(nxs[q[0]:q[0] + q[1]].sum()) - mean_w))
+    tmax = eng.trace_count(*g)
+    traces = torch.from_numpy(synth.synthetic_traces(tmax, seed=c["seed"])).cuda()
+    img = torch.zeros(3 * c["nz"] * c["nx"], dtype=torch.float32, device="cuda")
+    for _ in range(warmup):
+        eng.migrate(g[0], g[1], traces, img, traces_on_device=True, image_on_device=True)
+    torch.cuda.synchronize()
+    dev_ms = fwd_ms = adj_ms = 0.0
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            eng.migrate(g[0], g[1], traces, img, traces_on_device=True, image_on_device=True)
+            st = eng.stats()
+            dev_ms += st["total_ms"]
+            fwd_ms += st["fwd_ms"]
+            adj_ms += st["adj_ms"]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    eng.close()
+    del traces, img
+    torch.cuda.empty_cache()
+    cells = 2 * st["cells"] * c["nt"] * steps
+    return {"metric": "Gcell-updates/s", "value": round(cells / (dev_ms * 1e-3) / 1e9, 3), "unit": "Gcell/s",
+            "steps": steps, "warmup": warmup, "ms_per_step": round(dev_ms / steps, 1),
+            "shots_per_s": round(g[1] * steps / (dev_ms * 1e-3), 4),
+            "config": {"workload": c["desc"] + "; one step = one group of %d shots (widths %s)"
+                                   % (g[1], [int(v) for v in nxs[g[0]:g[0] + g[1]]]),
+                       "checkpoint_interval": st["checkpoint"],
+                       "fwd_ms_per_step": round(fwd_ms / steps, 1), "adj_ms_per_step": round(adj_ms / steps, 1),
+                       "note": "the adjoint pass includes the recomputation of each checkpoint segment (one more "
+                               "forward propagation), not counted in the cell-updates",
+                       "survey_estimate_s": round(dev_ms / steps * 1e-3 * len(groups), 1), "wall_s": round(wall, 2)},
+            "clocks": clocks}
+
+
+def run_default(args):
+    """The headline (the 64-shot survey) and, at N=1, the blocks measured
+    beside it in the same run."""
+    line = run_gpu(args)
+    if line is None:
+        return
+    survey = line.pop("_survey")
+    if line["n_gpus"] == 1:
+        if not args.no_error:
+            line["error_vs_fp64"] = error_block(survey)
+        if not args.no_secondary:
+            sec = {}
+            sec["acoustic3d"] = acoustic3d_block(args, steps=3, warmup=3)
+            sec["rtm2d_256shot_group"] = c5_block(args)
+            sec["precond"] = precond_block(args, steps=100, warmup=5, pairs=args.sec_pairs,
+                                           train_steps=args.sec_train_steps, ntest=2)
+            sec["precond"]["config"]["reduced"] = (
+                "bounded sample: %d training pairs (of 4096) and %d Adam steps (of 3000), %d held-out pairs"
+                % (args.sec_pairs, args.sec_train_steps, 2))
+            line["secondary"] = sec
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     print(json.dumps(line), flush=True)
 
 
@@ -575,6 +888,11 @@ def main():
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workload blocks")
+    ap.add_argument("--no-ref-gpu", action="store_true", help="reference arm: skip the reference CUDA comparator")
+    ap.add_argument("--sec-pairs", type=int, default=512, help="training pairs of the secondary precond block")
+    ap.add_argument("--sec-train-steps", type=int, default=1500, help="Adam steps of the secondary precond block")
     ap.add_argument("--nt", type=int, default=None, help="override nt (profiling captures only)")
     ap.add_argument("--shots", type=int, default=None, help="override the shot count (profiling captures only)")
     args = ap.parse_args()
@@ -590,8 +908,13 @@ def main():
         run_acoustic3d(args)
     elif args.workload == "precond":
         run_precond(args)
+    elif args.workload == "rtm2d":
+        run_default(args)
     else:
-        run_gpu(args)
+        line = run_gpu(args)
+        if line is not None:
+            line.pop("_survey")
+            print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -70,6 +70,7 @@ SIGNATURES = {
     "rtm_batch_set_checkpoint": (_c_int, [_P, _c_int]),
     "rtm_batch_set_tma": (_c_int, [_P, _c_int]),
     "rtm_batch_set_march": (_c_int, [_P, _c_int]),
+    "rtm_batch_set_test_stall": (_c_int, [_P, _c_int]),
     "rtm_debug_march_plan": (_c_int, [_c_int, _P, _c_int, _c_int, _P, _c_int, _P]),
     "rtm_batch_set_stages": (_c_int, [_P, _c_int, _c_int, _c_int, _c_int]),
     "rtm_batch_destroy": (None, [_P]),
@@ -80,6 +81,10 @@ SIGNATURES = {
     "acoustic3d_rtm_c_": (_c_int, [_c_int] * 4 + [_c_float] * 3 + [_P, _c_int, _c_float, _c_int, _c_int, _c_int, _P,
                                    _c_int, _P, _c_int, _P, _c_int, _P]),
     "acoustic3d_set": (_c_int, [_c_int, _c_int]),
+    "acoustic3d_set_kernel": (_c_int, [_c_int]),
+    "rtm_debug_umma_desc": (_c_int, [_c_int, _c_int, _c_int, _c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
+                                     ctypes.c_uint, _P]),
+    "rtm_debug_umma_probe": (_c_int, [_c_int, ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),
 }
 
 _lib = None

@@ -15,6 +15,12 @@ def set_shape(tile_x=16, ychunks=0):
     check(load().acoustic3d_set(tile_x, ychunks))
 
 
+def set_kernel(ring=True):
+    """Step kernel for n1 % 4 == 0: the slice-ring kernel fed by bulk tensor
+    copies (default) or the cp.async-pipelined kernel with a register queue."""
+    check(load().acoustic3d_set_kernel(1 if ring else 0))
+
+
 def forward(vel2, d, damp_a, damp_b, src, wavelet, zr, record=True, on_device=False):
     """Returns (traces [nt, n3, n2] or None, level nt-2, level nt-1, device ms)."""
     n3, n2, n1 = vel2.shape

@@ -83,6 +83,11 @@ class BatchRTM:
         (0: tile kernels for both)."""
         check(load().rtm_batch_set_march(self.h, int(mode)))
 
+    def set_test_stall(self, on):
+        """Test hook: make the next migrations' first forward marching launch
+        wait on a flag that nothing sets, so they return status 4."""
+        check(load().rtm_batch_set_test_stall(self.h, int(bool(on))))
+
     def set_checkpoint(self, interval):
         """0: keep every level's FP16 snapshots; k: checkpoint the forward
         state every k levels and recompute segments in the adjoint pass."""

@@ -10,12 +10,15 @@ Fortran/C callers link directly.
 """
 import concurrent.futures as cf
 import os
+import platform
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-OBJ = os.path.join(HERE, "_build")
+# objects per host architecture: a working tree copied between an x86 and an
+# Arm machine never links the other's objects
+OBJ = os.path.join(HERE, "_build", platform.machine() or "host")
 LIB = os.path.join(HERE, "libelastic_rtm.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,8 +56,16 @@ def build(verbose=False, force=False):
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(run, jobs))
     objs = [os.path.join(OBJ, s[:-3] + ".o") for s in sources()]
-    if force or jobs or _newer(LIB, objs):
+    # the stamp holds the modification time of the library this
+    # architecture's objects last linked: a library linked elsewhere (another
+    # architecture sharing the tree) does not match and is relinked
+    stamp = os.path.join(OBJ, "lib.stamp")
+    linked = open(stamp).read().strip() if os.path.exists(stamp) else ""
+    current = repr(os.path.getmtime(LIB)) if os.path.exists(LIB) else "none"
+    if force or jobs or _newer(LIB, objs) or linked != current:
         run([NVCC, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs])
+        with open(stamp, "w") as f:
+            f.write(repr(os.path.getmtime(LIB)))
     return LIB
 
 

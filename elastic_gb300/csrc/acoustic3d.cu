@@ -30,6 +30,7 @@
 
 #include "../../include/elastic_rtm.h"
 #include "common.cuh"
+#include "elastic2d_v2.cuh"
 #include "engine.h"
 
 using namespace eg;
@@ -59,6 +60,9 @@ struct Ac3DArgs {
     const float *simg;
     int y0, y1;        // y range of the march handled by a CTA chunk: [y0, y1)
     int ychunks;       // number of y chunks
+    int *err;          // set by a kernel whose bounded wait ran out (ring kernel)
+    int raw_out;       // store p2 undamped: the last level of a run, which the
+                       // reference leaves raw (no later step damps it)
 };
 
 __device__ __forceinline__ int edge_dist(int i, int n)
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(TX * 32) k_acoustic3d(const __grid_constant__ 
                 if (a.rec_out) a.rec_out[ri] = v;
             }
             if (a.img && zz < n1 - AR) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
-            outv[j] = f == 1.f ? v : fm<EXACT>(f, v);
+            outv[j] = (f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v);
         }
 #pragma unroll
         for (int j = 0; j < 4; j++)
@@ -333,7 +337,7 @@ __global__ void __launch_bounds__(TX * 32, TX == 8 ? 2 : 1) k_acoustic3d_p(const
                     if (a.rec_out) a.rec_out[ri] = v;
                 }
                 if (inside && a.img) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
-                out[j] = inside ? (f == 1.f ? v : fm<EXACT>(f, v)) : 0.f;
+                out[j] = inside ? ((f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v)) : 0.f;
             }
             *reinterpret_cast<float4 *>(a.p2 + o) = make_float4(out[0], out[1], out[2], out[3]);
         }
@@ -355,9 +359,191 @@ __global__ void k_inject(float *p, long long o, float v)
     if (threadIdx.x == 0 && blockIdx.x == 0) p[o] = p[o] + v;
 }
 
+// Ring kernel (default for n1 % 4 == 0): the same tiles, per-cell arithmetic
+// and march as k_acoustic3d_p, with every tap read from shared memory.  A
+// ring of T3_NR slices of p1 -- each the tile's 144 rows (8-row z halo) by
+// T3_LX columns (5-column x halo) -- is filled by one tensor-memory-access
+// box load per slice, issued by one thread seven slices ahead of the
+// compute; slice y's x and z taps come from its ring slot, its y taps from
+// the slots of slices y-5 .. y+5 (no register queue to shift).  The sponge
+// factor, the source and the receiver row are resolved per thread before the
+// march (a thread whose 4 cells and column lie outside the sponge needs no
+// factor on interior slices).  One CTA-wide barrier per slice, which also
+// carries the bounded waits' outcome: a CTA whose slice load did not land
+// within about a second records it in the error flag and stops.
+constexpr int T3_TX = 16;
+constexpr int T3_LX = T3_TX + 2 * AR;   // staged columns (26)
+constexpr int T3_NR = 13;               // slices y-5 .. y+5 in use, y+6 and y+7 loading
+constexpr int T3_SLICE = A_LZ * T3_LX;  // floats per staged slice
+constexpr size_t T3_SMEM = (size_t)T3_NR * T3_SLICE * sizeof(float) + 128 + T3_NR * 8;
+
+struct Ac3DTArgs {
+    Ac3DArgs a;
+    int src_z, src_x, src_y;  // source cell (0-based), src_y = -1: none
+    CUtensorMap tm;           // p1: n1 x n2 x n3, box {A_LZ, T3_LX, 1}
+};
+
+template <bool EXACT, bool IMG>
+__global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_constant__ Ac3DTArgs A)
+{
+    const Ac3DArgs &a = A.a;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *ring = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(ring + T3_NR * T3_SLICE);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3;
+    const int ntz = (n1 - 9 + A_TZ - 1) / A_TZ;  // rows 4 .. n1-6 (interior plus row 4)
+    int b = blockIdx.x;
+    const int yc = b % a.ychunks;
+    b /= a.ychunks;
+    const int tzi = b % ntz, txi = b / ntz;
+    const int z0 = 4 + tzi * A_TZ, x0 = AR + txi * T3_TX;
+    const int ylen = (n3 - 2 * AR + a.ychunks - 1) / a.ychunks;
+    const int ya = AR + yc * ylen, yb = min(n3 - AR, ya + ylen);
+    if (ya >= yb) return;
+    const int z = z0 + 4 * lane, x = x0 + warp;
+    const bool grp = x < n2 - AR && z < n1;  // this thread's float4 exists
+    const long long s3 = (long long)n1 * n2;
+    const long long ocol = (long long)x * n1 + z;
+    // per-thread constants: sponge distance of the 4 rows and the column,
+    // source and receiver rows within the 4 cells (-1: none)
+    int ezx = edge_dist(x, n2);
+#pragma unroll
+    for (int j = 0; j < 4; j++) ezx = min(ezx, edge_dist(z + j, n1));
+    const int sj = (A.src_y >= 0 && A.src_x == x && A.src_z >= z && A.src_z < z + 4) ? A.src_z - z : -1;
+    const int rj = (a.zr >= AR && a.zr < n1 - AR && a.zr >= z && a.zr < z + 4 && (a.rec_in || a.rec_out)) ? a.zr - z : -1;
+    auto slot = [&](int s) { return (s - (ya - AR)) % T3_NR; };
+    auto issue = [&](int s) {
+        const int k = slot(s);
+        mbar_expect_tx(&full[k], (unsigned)(T3_SLICE * sizeof(float)));
+        tma_load_3d(ring + k * T3_SLICE, &A.tm, z0 - A_ZH, x0 - AR, s, &full[k]);
+    };
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < T3_NR; k++) mbar_init(&full[k]);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const int last = yb - 1 + AR;  // last slice the march reads
+    if (threadIdx.x == 0)
+        for (int s = ya - AR; s <= min(ya + 6, last); s++) issue(s);
+    auto L4 = [&](const float *p, long long o) -> float4 {
+        return grp ? __ldg(reinterpret_cast<const float4 *>(p + o)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    float4 p0c = L4(a.p0, ocol + (long long)ya * s3), velc = L4(a.vel, ocol + (long long)ya * s3);
+    const float *coef = a.coef;
+    const int cofs = (warp + AR) * A_LZ + (4 * lane + A_ZH);  // this thread's float4 within a slice
+    for (int y = ya; y < yb; y++) {
+        // slices y-5 .. y+5 resident: wait for y+5 (and, first, for y-5 .. y+4)
+        bool ok = true;
+        for (int s = (y == ya ? ya - AR : y + AR); s <= y + AR; s++) {
+            const int u = s - (ya - AR);
+            ok = ok && mbar_wait(&full[u % T3_NR], (unsigned)((u / T3_NR) & 1));
+        }
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+            return;
+        }
+        // every thread is past slice y-1, so the slot of slice y-6 (first
+        // iteration: a slot not used yet) takes slice y+7
+        if (threadIdx.x == 0 && y + 7 <= last) issue(y + 7);
+        float4 p0n = make_float4(0.f, 0.f, 0.f, 0.f), veln = p0n;
+        if (y + 1 < yb) {
+            p0n = L4(a.p0, ocol + (long long)(y + 1) * s3);
+            veln = L4(a.vel, ocol + (long long)(y + 1) * s3);
+        }
+        if (grp) {
+            const float *cz = ring + slot(y) * T3_SLICE + cofs;
+            float w[20];
+#pragma unroll
+            for (int i = 0; i < 20; i += 4) {
+                const float4 t = *reinterpret_cast<const float4 *>(cz - 8 + i);
+                w[i] = t.x; w[i + 1] = t.y; w[i + 2] = t.z; w[i + 3] = t.w;
+            }
+            float accv[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) accv[j] = fm<EXACT>(coef[0], w[8 + j]);
+#pragma unroll
+            for (int k = 1; k <= AR; k++) {
+                const float4 xm = *reinterpret_cast<const float4 *>(cz - k * A_LZ);
+                const float4 xp = *reinterpret_cast<const float4 *>(cz + k * A_LZ);
+                const float4 ym = *reinterpret_cast<const float4 *>(ring + slot(y - k) * T3_SLICE + cofs);
+                const float4 yq = *reinterpret_cast<const float4 *>(ring + slot(y + k) * T3_SLICE + cofs);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float zp = fa<EXACT>(w[8 + j + k], w[8 + j - k]);
+                    const float xq = fa<EXACT>(e4(xp, j), e4(xm, j));
+                    const float yp = fa<EXACT>(e4(yq, j), e4(ym, j));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[1 + 3 * (k - 1)], zp));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[2 + 3 * (k - 1)], xq));
+                    accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[3 + 3 * (k - 1)], yp));
+                }
+            }
+            const bool nodamp = !a.damp || min(ezx, edge_dist(y, n3)) >= a.damp_a;
+            const long long o = ocol + (long long)y * s3;
+            float out[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int zz = z + j;
+                const float p = w[8 + j];
+                const bool inside = zz >= AR && zz < n1 - AR;
+                const float f = nodamp ? 1.f : damp_of<EXACT>(a, zz, x, y);
+                const float p0v = e4(p0c, j);
+                const float p0d = f == 1.f ? p0v : fm<EXACT>(f, p0v);
+                float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), accv[j]), p), p), p0d);
+                if (j == sj && y == A.src_y) v = fa<EXACT>(v, a.src_val);
+                if (j == rj) {
+                    const long long ri = (long long)y * n2 + x;
+                    if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
+                    if (a.rec_out) a.rec_out[ri] = v;
+                }
+                if (IMG && inside) a.img[o + j] = fa<EXACT>(a.img[o + j], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[o + j]));
+                out[j] = inside ? ((f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v)) : 0.f;
+            }
+            *reinterpret_cast<float4 *>(a.p2 + o) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+        p0c = p0n;
+        velc = veln;
+    }
+}
+
+int g_ac_ring = 1;  // 1: ring kernel where n1 % 4 == 0; 0: cp.async pipelined kernel
+
+template <bool EXACT>
+int launch_ac_ring(const Ac3DArgs &a0, int ychunks, cudaStream_t st)
+{
+    Ac3DTArgs t;
+    memset(&t, 0, sizeof t);
+    t.a = a0;
+    t.a.ychunks = ychunks;
+    t.src_z = t.src_x = t.src_y = -1;
+    if (a0.src_o >= 0) {
+        const long long s3 = (long long)a0.n1 * a0.n2;
+        t.src_y = (int)(a0.src_o / s3);
+        t.src_x = (int)((a0.src_o % s3) / a0.n1);
+        t.src_z = (int)(a0.src_o % a0.n1);
+    }
+    TRY(make_map(&t.tm, a0.p1, false, a0.n1, a0.n2, a0.n3, (long long)a0.n1 * a0.n2, A_LZ, T3_LX));
+    auto kern = a0.img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>;
+    static bool attr[RTM_MAX_DEVICES][2] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr[dev][a0.img != nullptr]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T3_SMEM));
+            attr[dev][a0.img != nullptr] = true;
+        }
+    }
+    const int ntz = (a0.n1 - 9 + A_TZ - 1) / A_TZ;
+    const int ntx = (a0.n2 - 2 * AR + T3_TX - 1) / T3_TX;
+    kern<<<ntz * ntx * ychunks, T3_TX * 32, T3_SMEM, st>>>(t);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
 template <bool EXACT>
 int launch_ac(const Ac3DArgs &a0, int tx, int ychunks, cudaStream_t st)
 {
+    if (a0.n1 % 4 == 0 && g_ac_ring && tensor_maps_available()) return launch_ac_ring<EXACT>(a0, ychunks, st);
     Ac3DArgs a = a0;
     a.ychunks = ychunks;
     const int ntx = (a.n2 - 2 * AR + tx - 1) / tx;
@@ -386,6 +572,7 @@ struct Ac3D {
     int n1, n2, n3, nt;
     size_t vol;
     DevBuf<float> vel, buf, damp, rec, img;
+    DevBuf<int> err;
     float coef[16];
     int damp_a = 0;
     int tx = 16, ych = 2;
@@ -393,7 +580,7 @@ struct Ac3D {
     cudaStream_t st = 0;
 
     int step(const float *p0, const float *p1, float *p2, bool damped, long long src_o, float src_val, int zr,
-             float *rec_out, const float *rec_in, float *img, const float *simg)
+             float *rec_out, const float *rec_in, float *img, const float *simg, bool raw_out = false)
     {
         Ac3DArgs a;
         memset(&a, 0, sizeof a);
@@ -405,7 +592,21 @@ struct Ac3D {
         a.src_o = src_o; a.src_val = src_val;
         a.zr = zr; a.rec_out = rec_out; a.rec_in = rec_in;
         a.img = img; a.simg = simg;
+        a.err = err.p;
+        a.raw_out = raw_out;
         return exact ? launch_ac<true>(a, tx, ych, st) : launch_ac<false>(a, tx, ych, st);
+    }
+    // status 4 when a kernel's bounded wait ran out during the run
+    int check_waits()
+    {
+        int e = 0;
+        RTM_CUDA(cudaMemcpy(&e, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) {
+            RTM_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+            rtm_set_error("a 3D step kernel's slice load did not complete within its time limit");
+            return RTM_ERR_TIMEOUT;
+        }
+        return RTM_OK;
     }
 };
 
@@ -440,23 +641,30 @@ int ac_setup(Ac3D &m, int n1, int n2, int n3, int nt, float d1, float d2, float 
     }
     const char *e = getenv("ELASTIC_RTM_EXACT3D");
     m.exact = e && atoi(e) == 1;
+    TRY(m.err.alloc(1));
+    RTM_CUDA(cudaMemset(m.err.p, 0, sizeof(int)));
     return RTM_OK;
 }
 
 int g_ac_tx = 16, g_ac_ych = 0;  // tile width and y chunks (0: chosen from the SM count)
+int g_ac_n3 = 512;                // n3 of the run being set up (y-chunk choice)
+int n3_hint() { return g_ac_n3; }
 
 int pick_ychunks(int n1, int n2, int tx)
 {
     if (g_ac_ych > 0) return g_ac_ych;
     const int ntz = n1 % 4 == 0 ? (n1 - 9 + A_TZ - 1) / A_TZ : (n1 - 2 * AR + A_TZ - 1) / A_TZ;
     const int ntx = (n2 - 2 * AR + tx - 1) / tx;
-    const int nsm = device_sm_count() * (tx == 8 ? 2 : 1);
+    const bool ring = n1 % 4 == 0 && g_ac_ring;
+    const int nsm = device_sm_count() * (tx == 8 && !ring ? 2 : 1);
     int best = 1;
     double best_eff = 0;
     for (int c = 1; c <= 8; c++) {
         const int g = ntz * ntx * c;
         const double waves = (double)g / nsm;
-        const double eff = waves / std::ceil(waves) * (1.0 - 0.01 * c);  // chunks re-read 10 slices
+        // each chunk loads the 10 slices around its y range once more
+        const double ylen = (double)(n3_hint() - 2 * AR) / c;
+        const double eff = waves / std::ceil(waves) * (ring ? ylen / (ylen + 10.0) : 1.0 - 0.01 * c);
         if (eff > best_eff) { best_eff = eff; best = c; }
     }
     return best;
@@ -464,11 +672,13 @@ int pick_ychunks(int n1, int n2, int tx)
 
 // Forward modelling from rest (W/gpu_funcs_3d.cu:133-315 with the sponge of
 // damp_kernel): returns the raw traces d[it][iy][ix] and the last two
-// stored levels.
+// levels as the reference leaves them -- level nt-2 damped (by the last
+// step's in-place damping), level nt-1 raw.
 int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, float dir, int zr, float *d_dev,
                float **last0, float **last1)
 {
-    m.tx = g_ac_tx;
+    m.tx = g_ac_ring && m.n1 % 4 == 0 ? T3_TX : g_ac_tx;
+    g_ac_n3 = m.n3;
     m.ych = pick_ychunks(m.n1, m.n2, m.tx);
     TRY(m.buf.alloc(2 * m.vol));
     float *A = m.buf.p, *B = m.buf.p + m.vol;
@@ -476,7 +686,7 @@ int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, floa
     for (int it = 0; it < m.nt; it++) {
         // A = level it-2 (older), B = level it-1; the new level goes over A
         TRY(m.step(A, B, A, damped, src_o, dir * wavelet[it], zr, d_dev ? d_dev + (size_t)it * m.n2 * m.n3 : nullptr,
-                   nullptr, nullptr, nullptr));
+                   nullptr, nullptr, nullptr, damped && it == m.nt - 1));
         std::swap(A, B);
     }
     *last0 = A;  // level nt-2
@@ -485,6 +695,13 @@ int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, floa
 }
 
 }  // namespace
+
+extern "C" int acoustic3d_set_kernel(int ring)
+{
+    RTM_CHECK_ARG(ring == 0 || ring == 1, "ring must be 0 or 1");
+    g_ac_ring = ring;
+    return RTM_OK;
+}
 
 extern "C" int acoustic3d_set(int tile_x, int ychunks)
 {
@@ -530,7 +747,7 @@ extern "C" int acoustic3d_fwd_c_(int n1, int n2, int n3, int nt, float d1, float
     if (p_last0) RTM_CUDA(cudaMemcpy(p_last0, l0, m.vol * sizeof(float), k));
     if (p_last1) RTM_CUDA(cudaMemcpy(p_last1, l1, m.vol * sizeof(float), k));
     RTM_CUDA(cudaDeviceSynchronize());
-    return RTM_OK;
+    return m.check_waits();
 }
 
 // 3D RTM (W/gpu_funcs_3d.cu:509-712): source propagated forward undamped,
@@ -592,5 +809,5 @@ extern "C" int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float
     cudaEventDestroy(e1);
     RTM_CUDA(cudaMemcpy(img, ib.p, m.vol * sizeof(float), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
     RTM_CUDA(cudaDeviceSynchronize());
-    return RTM_OK;
+    return m.check_waits();
 }

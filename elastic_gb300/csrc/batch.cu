@@ -35,6 +35,57 @@
 
 using namespace eg;
 
+namespace eg {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn_)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn_ encode_fn_impl()
+{
+    static EncodeTiledFn_ fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn_>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+
+bool tensor_maps_available() { return encode_fn_impl() != nullptr; }
+
+// 3D tensor map (ldz rows x cols columns x planes, plane stride plane_elems)
+// with a box of box_rows rows x box_cols columns x 1 plane
+int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
+             long long plane_elems, int box_rows, int box_cols)
+{
+    EncodeTiledFn_ fn = encode_fn_impl();
+    RTM_CHECK_ARG(fn, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t es = half ? 2 : 4;
+    const cuuint64_t dims[3] = {(cuuint64_t)ldz, (cuuint64_t)cols, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldz * es, (cuuint64_t)plane_elems * es};
+    const cuuint32_t box[3] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1};
+    const cuuint32_t el[3] = {1, 1, 1};
+    const CUresult r = fn(m, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                          const_cast<void *>(base), dims, strides, box, el, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        rtm_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return RTM_ERR_CUDA;
+    }
+    return RTM_OK;
+}
+
+}  // namespace eg
+
 static char g_pending_at[128] = "";
 static void note_pending(const char *where)
 {
@@ -98,50 +149,6 @@ __global__ void k_fold(long long n4, float4 *sum, float4 *cmp, float4 *part)
         cmp[i] = cv;
         part[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-}
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
-// against the driver library)
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_fn()
-{
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-        else
-            cudaGetLastError();
-    }
-    return fn;
-}
-
-// 3D tensor map (ldz rows x cols columns x planes, plane stride plane_elems)
-// with a box of box_rows rows x box_cols columns x 1 plane
-int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
-             long long plane_elems, int box_rows, int box_cols)
-{
-    EncodeTiledFn fn = encode_fn();
-    RTM_CHECK_ARG(fn, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t es = half ? 2 : 4;
-    const cuuint64_t dims[3] = {(cuuint64_t)ldz, (cuuint64_t)cols, (cuuint64_t)planes};
-    const cuuint64_t strides[2] = {(cuuint64_t)ldz * es, (cuuint64_t)plane_elems * es};
-    const cuuint32_t box[3] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1};
-    const cuuint32_t el[3] = {1, 1, 1};
-    const CUresult r = fn(m, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                          const_cast<void *>(base), dims, strides, box, el, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        rtm_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
-        return RTM_ERR_CUDA;
-    }
-    return RTM_OK;
 }
 
 // levels accumulated in FP32 partial planes between two folds
@@ -271,6 +278,10 @@ struct rtm_batch {
     DevBuf<int4> mruns;
     DevBuf<int> mlo;
     DevBuf<int> err;       // set by a step kernel whose tile load never completed
+    // test hook: the forward pass's first marching launch waits on `stall`,
+    // a zeroed device flag that nothing sets (rtm_batch_set_test_stall)
+    bool test_stall = false;
+    DevBuf<int> stall;
     DevBuf<int> dx0;
     ShotTable tab;    // forward pass work items (also used by the per-shot kernels)
     ShotTable tab_a;  // adjoint pass work items
@@ -651,6 +662,7 @@ int batch_group(rtm_batch *b, int s0, int ns, const float *traces, int traces_de
         if (use_march) {
             MarchArgs m = marg;
             for (int f = 0; f < 5; f++) m.own_plane[f] = (L & 1) * 5 + f;
+            if (b->test_stall && L == 2) m.stall = b->stall.p;
             TRY(launch_march(a, m, mctas, st));
         } else {
             TRY(launch_step<float>(a, false, false, b->tab.tx, 0, st, b->tab.tz, stf, thf));
@@ -1006,7 +1018,7 @@ extern "C" int rtm_batch_set(rtm_batch *b, int use_graph, int tile_x)
 extern "C" int rtm_batch_set_tma(rtm_batch *b, int on)
 {
     RTM_CHECK_ARG(b, "null argument");
-    if (on) RTM_CHECK_ARG(encode_fn() != nullptr, "tensor maps are not available from the driver");
+    if (on) RTM_CHECK_ARG(tensor_maps_available(), "tensor maps are not available from the driver");
     b->use_tma = on != 0;
     return RTM_OK;
 }
@@ -1015,6 +1027,20 @@ extern "C" int rtm_batch_set_march(rtm_batch *b, int mode)
 {
     RTM_CHECK_ARG(b && mode >= -1 && mode <= 3, "mode must be -1 .. 3");
     b->march = mode;
+    return RTM_OK;
+}
+
+extern "C" int rtm_batch_set_test_stall(rtm_batch *b, int on)
+{
+    RTM_CHECK_ARG(b, "null argument");
+    if (on) {
+        TRY(ensure_device());
+        if (!b->stall.p) {
+            TRY(b->stall.alloc(1));
+            RTM_CUDA(cudaMemset(b->stall.p, 0, sizeof(int)));
+        }
+    }
+    b->test_stall = on != 0;
     return RTM_OK;
 }
 

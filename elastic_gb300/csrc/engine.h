@@ -1,5 +1,7 @@
 // Host-side building blocks shared by the 2D elastic entry points.
 #pragma once
+#include <cuda.h>
+
 #include <vector>
 
 #include "common.cuh"
@@ -22,6 +24,14 @@ int kernel_version();
 
 int ensure_device();
 int device_sm_count();
+
+// Tensor maps for bulk tensor copies, encoded through the runtime's driver
+// entry point (no link against the driver library).  make_map: a 3D map of
+// ldz rows x cols columns x planes (plane stride plane_elems elements), FP32
+// or FP16, box of box_rows x box_cols x 1, zero fill outside the tensor.
+bool tensor_maps_available();
+int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
+             long long plane_elems, int box_rows, int box_cols);
 
 // Owning device allocation that grows on demand.
 template <typename T>

@@ -42,6 +42,10 @@ struct MarchArgs {
     const int4 *runs;   // (shot, first row of the strip, first chunk, end chunk)
     const int *run_lo;  // CTA b walks runs [run_lo[b], run_lo[b + 1])
     int own_plane[5];   // plane (in tm_own) of field f at the level being written
+    // test hook (null in normal use): a device flag that nothing sets; the
+    // producer waits on it before issuing any copy, so the wait runs out,
+    // the kernel reports it through the error flag and no copy is in flight
+    const int *stall;
     CUtensorMap tm_nb;  // level planes, box {144 rows, 8 columns, 1}
     CUtensorMap tm_own; // level planes, box {128 rows, 8 columns, 1}
     CUtensorMap tm_coef;  // coefficient planes, box {128 rows, 8 columns, 1}
@@ -147,6 +151,15 @@ __global__ void __launch_bounds__(M_FWD_THREADS, 1) k_fwd_march(const __grid_con
         // first (full[n & 1], own/coefficient slot n & 1); it is issued once
         // chunk n - 2 is done (chunk n - 1 for a run's first group)
         if (lane != 0) return;
+        if (m.stall) {
+            const long long t0 = clock64();
+            while (*reinterpret_cast<const volatile int *>(m.stall) == 0) {
+                if (clock64() - t0 > 2000000000LL) {
+                    if (a.err) atomicExch(a.err, 1);
+                    return;  // nothing issued: the consumers' waits run out too
+                }
+            }
+        }
         constexpr unsigned NB_BYTES = V2_LZ * MC * 4, OWN_BYTES = V2_TZ * MC * 4;
         {
             // group 0's own fields (written two levels back) and coefficients

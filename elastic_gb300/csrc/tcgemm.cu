@@ -1,0 +1,118 @@
+// Checks of the tcgen05 building blocks (umma.cuh) used by the learned
+// preconditioner's tensor-core GEMMs: the descriptor encoders, exported for a
+// CPU test against the PTX ISA field layout, and a one-instruction probe --
+// one 128 x N x 16 BF16 MMA with FP32 accumulation in tensor memory -- that
+// a GPU test compares with a host matrix product.
+#include <cuda_bf16.h>
+
+#include <cstring>
+
+#include "../../include/elastic_rtm.h"
+#include "common.cuh"
+#include "elastic2d_v2.cuh"
+#include "engine.h"
+#include "umma.cuh"
+
+using namespace eg;
+
+namespace {
+
+// The probe's operands are stored K-major without swizzle, core matrices
+// adjacent along K 128 bytes apart and along M (N) 256 bytes apart.  Every
+// descriptor offset the probe accepts (16 .. 256 bytes) keeps every read
+// inside the operand arrays, whatever the hardware makes of the fields.
+constexpr int PROBE_K = 16;
+
+__global__ void __launch_bounds__(128) k_umma_probe(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D, int N,
+                                                     uint32_t lbo, uint32_t sbo, int *status)
+{
+    __shared__ __align__(1024) __nv_bfloat16 sA[2 * 128 * PROBE_K];  // twice the operand: 8 KB
+    __shared__ __align__(1024) __nv_bfloat16 sB[2 * 256 * PROBE_K];  // 16 KB
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
+    for (int i = tid; i < 2 * 128 * PROBE_K; i += 128) sA[i] = __float2bfloat16(0.f);
+    for (int i = tid; i < 2 * 256 * PROBE_K; i += 128) sB[i] = __float2bfloat16(0.f);
+    __syncthreads();
+    auto place = [](int r, int k) { return (r >> 3) * 128 + (k >> 3) * 64 + (r & 7) * 8 + (k & 7); };  // in bf16
+    for (int i = tid; i < 128 * PROBE_K; i += 128) sA[place(i / PROBE_K, i % PROBE_K)] = A[i];
+    for (int i = tid; i < N * PROBE_K; i += 128) sB[place(i / PROBE_K, i % PROBE_K)] = B[i];
+    if (warp == 0) tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        mbar_init(&bar);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t d = tbase;
+    if (tid == 0) {
+        const uint64_t ad = umma_sdesc(smem_u32(sA), lbo, sbo, 0), bd = umma_sdesc(smem_u32(sB), lbo, sbo, 0);
+        umma_f16(d, ad, bd, umma_idesc_f16(128, N, true, true), false);
+        umma_commit(&bar);
+    }
+    bool ok = mbar_wait(&bar, 0);
+    if (!ok) ok = mbar_wait(&bar, 0);  // the MMA may still be running: give it a second limit
+    tc_fence_after();
+    if (ok) {
+        for (int c = 0; c < N; c += 16) {
+            float v[16];
+            tmem_ld16(d + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) D[(32 * warp + lane) * N + c + j] = v[j];
+        }
+    } else if (tid == 0) {
+        *status = 1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tmem_dealloc(d, ncols);
+        tmem_relinquish();
+    }
+}
+
+}  // namespace
+
+extern "C" int rtm_debug_umma_desc(int M, int N, int bf16, int f32, unsigned addr, unsigned lbo, unsigned sbo,
+                                   unsigned swizzle, unsigned long long *out)
+{
+    RTM_CHECK_ARG(out, "null argument");
+    out[0] = umma_idesc_f16(M, N, bf16 != 0, f32 != 0);
+    out[1] = umma_sdesc(addr, lbo, sbo, swizzle);
+    return RTM_OK;
+}
+
+extern "C" int rtm_debug_umma_probe(int N, unsigned lbo, unsigned sbo, const unsigned short *A, const unsigned short *B,
+                                    float *D)
+{
+    RTM_CHECK_ARG(N >= 16 && N <= 256 && N % 16 == 0, "N must be a multiple of 16 in 16 .. 256");
+    RTM_CHECK_ARG(lbo >= 16 && lbo <= 256 && sbo >= 16 && sbo <= 256 && lbo % 16 == 0 && sbo % 16 == 0,
+                  "descriptor offsets must be multiples of 16 in 16 .. 256");
+    RTM_CHECK_ARG(A && B && D, "null argument");
+    TRY(ensure_device());
+    DevBuf<__nv_bfloat16> a, b;
+    DevBuf<float> d;
+    DevBuf<int> st;
+    TRY(a.alloc(128 * PROBE_K));
+    TRY(b.alloc((size_t)N * PROBE_K));
+    TRY(d.alloc((size_t)128 * N));
+    TRY(st.alloc(1));
+    RTM_CUDA(cudaMemcpy(a.p, A, 128 * PROBE_K * 2, cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(b.p, B, (size_t)N * PROBE_K * 2, cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemset(d.p, 0, (size_t)128 * N * 4));
+    RTM_CUDA(cudaMemset(st.p, 0, 4));
+    k_umma_probe<<<1, 128>>>(a.p, b.p, d.p, N, lbo, sbo, st.p);
+    RTM_CUDA(cudaGetLastError());
+    RTM_CUDA(cudaDeviceSynchronize());
+    int s = 0;
+    RTM_CUDA(cudaMemcpy(&s, st.p, 4, cudaMemcpyDeviceToHost));
+    RTM_CUDA(cudaMemcpy(D, d.p, (size_t)128 * N * 4, cudaMemcpyDeviceToHost));
+    if (s) {
+        rtm_set_error("the probe's MMA did not complete within its time limit");
+        return RTM_ERR_TIMEOUT;
+    }
+    return RTM_OK;
+}

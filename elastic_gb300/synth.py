@@ -88,19 +88,21 @@ def single_shot_models(nz=200, nx=400, seed=0, blob=0.05, smooth_cells=5.0):
     return m0, dm
 
 
-def dipping_reflectivity(nz, nx, seed=0, n_layers=6, n_points=20, amp=0.05, top=20):
+def dipping_reflectivity(nz, nx, seed=0, n_layers=6, n_points=20, amp=0.05, top=20, bottom=None):
     """Relative perturbation [nx, nz]: `n_layers` dipping reflectors (one
     cell thick, slopes within +-15 degrees, amplitudes within +-amp) and
-    `n_points` point scatterers, all below row `top`."""
+    `n_points` point scatterers, all between rows `top` and `bottom`
+    (default: 5 rows above the bottom of the grid)."""
     rng = np.random.default_rng(seed)
+    bottom = nz - 5 if bottom is None else min(bottom, nz - 5)
     r = np.zeros((nx, nz))
     x = np.arange(nx)
     for _ in range(n_layers):
-        z0 = rng.uniform(top, nz - 10)
+        z0 = rng.uniform(top, bottom)
         slope = np.tan(np.radians(rng.uniform(-15.0, 15.0)))
         z = np.round(z0 + slope * (x - nx / 2)).astype(int)
-        ok = (z >= top) & (z < nz - 5)
+        ok = (z >= top) & (z < bottom)
         r[x[ok], z[ok]] += rng.uniform(-amp, amp)
     for _ in range(n_points):
-        r[rng.integers(5, nx - 5), rng.integers(top, nz - 5)] += rng.uniform(-amp, amp)
+        r[rng.integers(5, nx - 5), rng.integers(top, bottom)] += rng.uniform(-amp, amp)
     return r

@@ -247,8 +247,17 @@ int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float d2, float 
                       float damp_b, int zs, int xs, int ys, const float *wavelet, int zr, const float *data, int jt,
                       float *img, int on_device, double *ms);
 /* Kernel shape of the 3D propagator: tile width 8 or 16 columns and the
- * number of chunks the y march is split into (0 = chosen from the SM count). */
+ * number of chunks the y march is split into (0 = chosen from the SM count).
+ * The tile width applies to the cp.async-pipelined kernel; the slice-ring
+ * kernel uses 16 columns. */
 int acoustic3d_set(int tile_x, int ychunks);
+/* Step kernel where n1 % 4 == 0: 1 (default) the slice-ring kernel, whose
+ * p1 slices arrive by bulk tensor copies into a 13-slice shared-memory ring;
+ * 0 the cp.async-pipelined kernel with a register queue of y taps.  Both are
+ * bit-identical in exact arithmetic.  A ring kernel whose slice load does
+ * not land within about a second stops; the entry point then returns
+ * RTM_ERR_TIMEOUT (4). */
+int acoustic3d_set_kernel(int ring);
 
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
@@ -325,10 +334,33 @@ int rtm_batch_set_tma(rtm_batch *b, int on);
  * adjoint marching kernel runs, out[45] / out[47] their autotuner times (ms
  * per launch, -1 when not timed). */
 int rtm_batch_set_march(rtm_batch *b, int mode);
+/* Test hook for the timeout path (no counterpart in the reference): with
+ * on != 0 the forward pass's first marching launch of every following
+ * migration waits on a device flag that nothing sets.  The wait gives up
+ * after about a second, before the kernel has issued any copy, and
+ * rtm_batch_migrate returns RTM_ERR_TIMEOUT (4) for that group; with on = 0
+ * the engine migrates normally again.  Needs the marching forward kernel
+ * (rtm_batch_set_march with bit 1). */
+int rtm_batch_set_test_stall(rtm_batch *b, int on);
 void rtm_batch_destroy(rtm_batch *b);
 /* Page-locked host memory for fast host<->device traces and images. */
 void *rtm_host_alloc(size_t bytes);
 void rtm_host_free(void *p);
+
+/* Checks of the tensor-core building blocks (no counterpart in the
+ * reference).  rtm_debug_umma_desc: out[0] = the tcgen05 instruction
+ * descriptor (.kind::f16, M x N, BF16 or F16 operands, F32 or F16
+ * accumulator), out[1] = the shared-memory matrix descriptor of a matrix at
+ * shared address addr with byte offsets lbo (along K) and sbo (along M/N)
+ * and the given swizzle mode.  rtm_debug_umma_probe: one 128 x N x 16 BF16
+ * MMA (A 128x16 and B Nx16 row-major BF16 on the host, K contiguous) with the
+ * operands stored K-major without swizzle (core matrices 128 bytes apart
+ * along K, 256 along M/N) and the descriptors built with lbo/sbo; D (128 x N,
+ * FP32) comes back from tensor memory. */
+int rtm_debug_umma_desc(int M, int N, int bf16, int f32, unsigned addr, unsigned lbo, unsigned sbo, unsigned swizzle,
+                        unsigned long long *out);
+int rtm_debug_umma_probe(int N, unsigned lbo, unsigned sbo, const unsigned short *A, const unsigned short *B,
+                         float *D);
 
 /* ------------------------------------------ learned image preconditioner
  * (no counterpart in the reference).  A 4-level 3->3 channel U-Net

@@ -27,7 +27,8 @@
 
 /* 10th-order staggered coefficients, W/rtmlib-mod.f90:15 (single-precision
    division in Fortran; the float rounding of the double quotient is the same
-   for all five, checked in tests/test_oracle_host.py). */
+   for all five, checked in tests/test_oracle.py,
+   test_stagger_coefficients_single_precision). */
 static const R FN(c1) = (R)(35.0 / 294912.0);
 static const R FN(c2) = (R)(-405.0 / 229376.0);
 static const R FN(c3) = (R)(567.0 / 40960.0);
@@ -496,70 +497,91 @@ static R FN(mask_get)(int nz, int nx, const R *a, int iz, int ix, int lz, int hz
     return a[(size_t)iz + (size_t)nz * (size_t)ix];
 }
 
-void FN(ora_rtm_op3_c)(int nt, int nz, int nx, R *Vx0, R *Vz0, R *sxx0, R *szz0, R *sxz0, const R *m1_x,
-                       const R *m1_z, const R *aux_m2_c, const R *aux_m3_c, const R *aux_m2m3_c)
+/* One cell of the recursion.  checked = 1: every neighbour and coefficient
+   read goes through the reference's masks and the grid bounds (border
+   cells); checked = 0: the cell lies at least 10 cells inside the grid,
+   where every mask passes and every neighbour exists, so the reads are
+   direct.  Both evaluate the same products in the same order. */
+static inline __attribute__((always_inline)) void FN(gather_cell)(int nz, int nx, int iz, int ix, size_t n, int it,
+                                                                   R *Vx0, R *Vz0, R *sxx0,
+                                   R *szz0, R *sxz0, const R *m1_x, const R *m1_z, const R *aux_m2_c,
+                                   const R *aux_m3_c, const R *aux_m2m3_c, const R *c, const int checked)
 {
-    int it, iz, ix, k;
-    size_t n = PLANE;
-    const R c[5] = {FN(c1), FN(c2), FN(c3), FN(c4), FN(c5)};
+    int k;
     /* masks, 0-based inclusive ranges (W/rtmlib-modC.c:83-93) */
     const int zlo4 = 4, zhi = nz - 6, xlo4 = 4, xhi = nx - 6;
-#define AM2M3(z, x) FN(mask_get)(nz, nx, aux_m2m3_c, z, x, zlo4, zhi, xlo4, xhi)
-#define AM2(z, x) FN(mask_get)(nz, nx, aux_m2_c, z, x, zlo4, zhi, xlo4, xhi)
-#define AM3(z, x) FN(mask_get)(nz, nx, aux_m3_c, z, x, 5, zhi, 5, xhi)
-#define M1X(z, x) FN(mask_get)(nz, nx, m1_x, z, x, zlo4, zhi, 5, xhi)
-#define M1Z(z, x) FN(mask_get)(nz, nx, m1_z, z, x, 5, zhi, xlo4, xhi)
-#define FLD(f, z, x, t) (((z) < 0 || (z) >= nz || (x) < 0 || (x) >= nx) ? (R)0 : (f)[(size_t)(z) + (size_t)nz * (size_t)(x) + n * (size_t)(t)])
-    for (it = nt - 3; it >= 0; it--) {
-#pragma omp parallel for private(iz, k) schedule(static)
-        for (ix = 0; ix < nx; ix++)
-            for (iz = 0; iz < nz; iz++) {
-                size_t o = (size_t)iz + (size_t)nz * (size_t)ix + n * (size_t)it;
-                size_t o2 = o + 2 * n;
-                R v;
-                /* Vx: x-M5(aux_m2m3, sxx), x-M5(aux_m2, szz), z-P5(aux_m3, sxz) */
-                v = Vx0[o] + Vx0[o2];
-                for (k = 0; k < 5; k++) v = v + (AM2M3(iz, ix - 5 + k) * c[k]) * FLD(sxx0, iz, ix - 5 + k, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM2M3(iz, ix + 4 - k) * c[k]) * FLD(sxx0, iz, ix + 4 - k, it + 1);
-                for (k = 0; k < 5; k++) v = v + (AM2(iz, ix - 5 + k) * c[k]) * FLD(szz0, iz, ix - 5 + k, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM2(iz, ix + 4 - k) * c[k]) * FLD(szz0, iz, ix + 4 - k, it + 1);
-                for (k = 0; k < 5; k++) v = v + (AM3(iz - 4 + k, ix) * c[k]) * FLD(sxz0, iz - 4 + k, ix, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM3(iz + 5 - k, ix) * c[k]) * FLD(sxz0, iz + 5 - k, ix, it + 1);
-                Vx0[o] = v;
-                /* Vz: z-M5(aux_m2, sxx), z-M5(aux_m2m3, szz), x-P5(aux_m3, sxz) */
-                v = Vz0[o] + Vz0[o2];
-                for (k = 0; k < 5; k++) v = v + (AM2(iz - 5 + k, ix) * c[k]) * FLD(sxx0, iz - 5 + k, ix, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM2(iz + 4 - k, ix) * c[k]) * FLD(sxx0, iz + 4 - k, ix, it + 1);
-                for (k = 0; k < 5; k++) v = v + (AM2M3(iz - 5 + k, ix) * c[k]) * FLD(szz0, iz - 5 + k, ix, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM2M3(iz + 4 - k, ix) * c[k]) * FLD(szz0, iz + 4 - k, ix, it + 1);
-                for (k = 0; k < 5; k++) v = v + (AM3(iz, ix - 4 + k) * c[k]) * FLD(sxz0, iz, ix - 4 + k, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (AM3(iz, ix + 5 - k) * c[k]) * FLD(sxz0, iz, ix + 5 - k, it + 1);
-                Vz0[o] = v;
-                /* sxx: x-P5(m1_x, Vx) */
-                v = sxx0[o] + sxx0[o2];
-                for (k = 0; k < 5; k++) v = v + (M1X(iz, ix - 4 + k) * c[k]) * FLD(Vx0, iz, ix - 4 + k, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (M1X(iz, ix + 5 - k) * c[k]) * FLD(Vx0, iz, ix + 5 - k, it + 1);
-                sxx0[o] = v;
-                /* szz: z-P5(m1_z, Vz) */
-                v = szz0[o] + szz0[o2];
-                for (k = 0; k < 5; k++) v = v + (M1Z(iz - 4 + k, ix) * c[k]) * FLD(Vz0, iz - 4 + k, ix, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (M1Z(iz + 5 - k, ix) * c[k]) * FLD(Vz0, iz + 5 - k, ix, it + 1);
-                szz0[o] = v;
-                /* sxz: z-M5(m1_x, Vx), x-M5(m1_z, Vz) */
-                v = sxz0[o] + sxz0[o2];
-                for (k = 0; k < 5; k++) v = v + (M1X(iz - 5 + k, ix) * c[k]) * FLD(Vx0, iz - 5 + k, ix, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (M1X(iz + 4 - k, ix) * c[k]) * FLD(Vx0, iz + 4 - k, ix, it + 1);
-                for (k = 0; k < 5; k++) v = v + (M1Z(iz, ix - 5 + k) * c[k]) * FLD(Vz0, iz, ix - 5 + k, it + 1);
-                for (k = 4; k >= 0; k--) v = v - (M1Z(iz, ix + 4 - k) * c[k]) * FLD(Vz0, iz, ix + 4 - k, it + 1);
-                sxz0[o] = v;
-            }
-    }
+    size_t o = (size_t)iz + (size_t)nz * (size_t)ix + n * (size_t)it;
+    size_t o2 = o + 2 * n;
+    R v;
+#define CF(a, z, x, lz, hz, lx, hx) (checked ? FN(mask_get)(nz, nx, a, z, x, lz, hz, lx, hx) : (a)[(size_t)(z) + (size_t)nz * (size_t)(x)])
+#define AM2M3(z, x) CF(aux_m2m3_c, z, x, zlo4, zhi, xlo4, xhi)
+#define AM2(z, x) CF(aux_m2_c, z, x, zlo4, zhi, xlo4, xhi)
+#define AM3(z, x) CF(aux_m3_c, z, x, 5, zhi, 5, xhi)
+#define M1X(z, x) CF(m1_x, z, x, zlo4, zhi, 5, xhi)
+#define M1Z(z, x) CF(m1_z, z, x, 5, zhi, xlo4, xhi)
+#define FLD(f, z, x, t) ((checked && ((z) < 0 || (z) >= nz || (x) < 0 || (x) >= nx)) ? (R)0 : (f)[(size_t)(z) + (size_t)nz * (size_t)(x) + n * (size_t)(t)])
+    /* Vx: x-M5(aux_m2m3, sxx), x-M5(aux_m2, szz), z-P5(aux_m3, sxz) */
+    v = Vx0[o] + Vx0[o2];
+    for (k = 0; k < 5; k++) v = v + (AM2M3(iz, ix - 5 + k) * c[k]) * FLD(sxx0, iz, ix - 5 + k, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM2M3(iz, ix + 4 - k) * c[k]) * FLD(sxx0, iz, ix + 4 - k, it + 1);
+    for (k = 0; k < 5; k++) v = v + (AM2(iz, ix - 5 + k) * c[k]) * FLD(szz0, iz, ix - 5 + k, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM2(iz, ix + 4 - k) * c[k]) * FLD(szz0, iz, ix + 4 - k, it + 1);
+    for (k = 0; k < 5; k++) v = v + (AM3(iz - 4 + k, ix) * c[k]) * FLD(sxz0, iz - 4 + k, ix, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM3(iz + 5 - k, ix) * c[k]) * FLD(sxz0, iz + 5 - k, ix, it + 1);
+    Vx0[o] = v;
+    /* Vz: z-M5(aux_m2, sxx), z-M5(aux_m2m3, szz), x-P5(aux_m3, sxz) */
+    v = Vz0[o] + Vz0[o2];
+    for (k = 0; k < 5; k++) v = v + (AM2(iz - 5 + k, ix) * c[k]) * FLD(sxx0, iz - 5 + k, ix, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM2(iz + 4 - k, ix) * c[k]) * FLD(sxx0, iz + 4 - k, ix, it + 1);
+    for (k = 0; k < 5; k++) v = v + (AM2M3(iz - 5 + k, ix) * c[k]) * FLD(szz0, iz - 5 + k, ix, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM2M3(iz + 4 - k, ix) * c[k]) * FLD(szz0, iz + 4 - k, ix, it + 1);
+    for (k = 0; k < 5; k++) v = v + (AM3(iz, ix - 4 + k) * c[k]) * FLD(sxz0, iz, ix - 4 + k, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (AM3(iz, ix + 5 - k) * c[k]) * FLD(sxz0, iz, ix + 5 - k, it + 1);
+    Vz0[o] = v;
+    /* sxx: x-P5(m1_x, Vx) */
+    v = sxx0[o] + sxx0[o2];
+    for (k = 0; k < 5; k++) v = v + (M1X(iz, ix - 4 + k) * c[k]) * FLD(Vx0, iz, ix - 4 + k, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (M1X(iz, ix + 5 - k) * c[k]) * FLD(Vx0, iz, ix + 5 - k, it + 1);
+    sxx0[o] = v;
+    /* szz: z-P5(m1_z, Vz) */
+    v = szz0[o] + szz0[o2];
+    for (k = 0; k < 5; k++) v = v + (M1Z(iz - 4 + k, ix) * c[k]) * FLD(Vz0, iz - 4 + k, ix, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (M1Z(iz + 5 - k, ix) * c[k]) * FLD(Vz0, iz + 5 - k, ix, it + 1);
+    szz0[o] = v;
+    /* sxz: z-M5(m1_x, Vx), x-M5(m1_z, Vz) */
+    v = sxz0[o] + sxz0[o2];
+    for (k = 0; k < 5; k++) v = v + (M1X(iz - 5 + k, ix) * c[k]) * FLD(Vx0, iz - 5 + k, ix, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (M1X(iz + 4 - k, ix) * c[k]) * FLD(Vx0, iz + 4 - k, ix, it + 1);
+    for (k = 0; k < 5; k++) v = v + (M1Z(iz, ix - 5 + k) * c[k]) * FLD(Vz0, iz, ix - 5 + k, it + 1);
+    for (k = 4; k >= 0; k--) v = v - (M1Z(iz, ix + 4 - k) * c[k]) * FLD(Vz0, iz, ix + 4 - k, it + 1);
+    sxz0[o] = v;
+#undef CF
 #undef AM2M3
 #undef AM2
 #undef AM3
 #undef M1X
 #undef M1Z
 #undef FLD
+}
+
+void FN(ora_rtm_op3_c)(int nt, int nz, int nx, R *Vx0, R *Vz0, R *sxx0, R *szz0, R *sxz0, const R *m1_x,
+                       const R *m1_z, const R *aux_m2_c, const R *aux_m3_c, const R *aux_m2m3_c)
+{
+    int it, iz, ix;
+    size_t n = PLANE;
+    const R c[5] = {FN(c1), FN(c2), FN(c3), FN(c4), FN(c5)};
+    for (it = nt - 3; it >= 0; it--) {
+#pragma omp parallel for private(iz) schedule(static)
+        for (ix = 0; ix < nx; ix++)
+            for (iz = 0; iz < nz; iz++) {
+                if (iz >= 10 && iz <= nz - 11 && ix >= 10 && ix <= nx - 11)
+                    FN(gather_cell)(nz, nx, iz, ix, n, it, Vx0, Vz0, sxx0, szz0, sxz0, m1_x, m1_z, aux_m2_c, aux_m3_c,
+                                    aux_m2m3_c, c, 0);
+                else
+                    FN(gather_cell)(nz, nx, iz, ix, n, it, Vx0, Vz0, sxx0, szz0, sxz0, m1_x, m1_z, aux_m2_c, aux_m3_c,
+                                    aux_m2m3_c, c, 1);
+            }
+    }
 }
 
 /* --------------------------------------------------------------- a10 ---- */

@@ -321,6 +321,24 @@ def ref90_rtm(adj, rho, lam, mu, dm, D, dx, dt, nt, zsrc, xsrc, zrec, fp, abc, f
     return out
 
 
+def ref90_image(adj, lame, m, Vx0, Vz0, dx, dt, dm=None, H=None):
+    """The reference's image_init (+ image_init2 for lame=False) and
+    image_op2 (W/image-mod-rtm.f90:26-225), float32.  m = (m1, m2, m3)
+    planes [nx,nz] (rho, lambda, mu or rho, vp, vs); Vx0, Vz0 source
+    histories [nt,nx,nz].  adj=True: H (5 histories) -> images (dm1, dm2,
+    dm3); adj=False: dm -> 5 histories of Born secondary sources."""
+    r = ref90()
+    nt, nx, nz = Vx0.shape
+    m = [np.array(x, np.float32, order="C") for x in m]
+    V = [np.array(x, np.float32, order="C") for x in (Vx0, Vz0)]
+    dm = [np.zeros((nx, nz), np.float32) for _ in range(3)] if dm is None else [np.array(x, np.float32) for x in dm]
+    H = [np.zeros((nt, nx, nz), np.float32) for _ in range(5)] if H is None else [np.array(x, np.float32) for x in H]
+    F = ctypes.c_float
+    r.ref90_image(int(adj), int(lame), nz, nx, nt, F(dx), F(dt), _p(V[0]), _p(V[1]), *[_p(x) for x in m],
+                  *[_p(x) for x in dm], *[_p(x) for x in H])
+    return dm if adj else H
+
+
 # ------------------------------------------------------------------ 3D acoustic
 def acoustic_coeffs(d1, d2, d3):
     c = np.zeros(16, np.float32)

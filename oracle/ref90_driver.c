@@ -21,6 +21,11 @@
 
 int F_rtm_mod_adj_rtm_op(int *a_adj, rarr a_dm1_in, rarr a_dm2_in, rarr a_dm3_in, rarr a_vx_in, rarr a_vz_in,
                          rarr a_sigmaxx_in, rarr a_sigmazz_in, rarr a_sigmaxz_in);
+void F_image_mod_rtm_image_init(int *a_nx_in, float *a_dx_in, int *a_nz_in, float *a_dz_in, int *a_nt_in,
+                                float *a_dt_in, rarr a_vx0_in, rarr a_vz0_in, int *a_lame_in);
+void F_image_mod_rtm_image_init2(rarr a_m1_in, rarr a_m2_in, rarr a_m3_in);
+void F_image_mod_rtm_image_op2(int *a_adj, int *a_add, float *a_dm1_p, float *a_dm2_p, float *a_dm3_p, float *a_vx_p,
+                               float *a_vz_p, float *a_sigmaxx_p, float *a_sigmazz_p, float *a_sigmaxz_p);
 
 static float *hook_dst[5];
 
@@ -76,4 +81,23 @@ long ref90_get(const char *name, float *dst, long n)
     if (dst && size)
         memcpy(dst, a->p, sizeof(float) * (size_t)(size < n ? size : n));
     return size;
+}
+
+/* The reference's imaging operator alone (W/image-mod-rtm.f90): image_init on
+ * the source histories Vx0, Vz0 (nz,nx,nt), image_init2 with (m1,m2,m3) when
+ * lame = 0 (velocity parameterisation: rho, vp, vs), then image_op2(adj,
+ * add=.false.): adj = 1 images the five histories h1..h5 into dm1..dm3,
+ * adj = 0 writes the Born secondary sources of dm1..dm3 into h1..h5. */
+int ref90_image(int adj, int lame, int nz, int nx, int nt, float dx, float dt, float *Vx0, float *Vz0, float *m1,
+                float *m2, float *m3, float *dm1, float *dm2, float *dm3, float *h1, float *h2, float *h3, float *h4,
+                float *h5)
+{
+    rarr VX = {Vx0, {nz, nx, nt}}, VZ = {Vz0, {nz, nx, nt}};
+    rarr M1 = {m1, {nz, nx, 1}}, M2 = {m2, {nz, nx, 1}}, M3 = {m3, {nz, nx, 1}};
+    int add = 0;
+    F_image_mod_rtm_image_init(&nx, &dx, &nz, &dx, &nt, &dt, VX, VZ, &lame);
+    if (!lame)
+        F_image_mod_rtm_image_init2(M1, M2, M3);
+    F_image_mod_rtm_image_op2(&adj, &add, dm1, dm2, dm3, h1, h2, h3, h4, h5);
+    return 0;
 }

@@ -25,6 +25,14 @@ def setup(n1=40, n2=36, n3=34, nt=30, seed=0):
     return vel.astype(np.float32), w
 
 
+@pytest.fixture(autouse=True, params=["ring", "pipelined"])
+def kernel(request):
+    """Every test runs with both step kernels (they differ where n1 % 4 == 0)."""
+    A.set_kernel(request.param == "ring")
+    yield request.param
+    A.set_kernel(True)
+
+
 @pytest.fixture(params=["exact", "fast"])
 def mode(request, monkeypatch):
     monkeypatch.setenv("ELASTIC_RTM_EXACT3D", "1" if request.param == "exact" else "0")
@@ -79,3 +87,25 @@ def test_rtm_reverse_restart(mode):
         # (observed 2.5e-5 relative L2 at 40 steps), so the fast-mode bound
         # for this output is 1e-4.  Exact mode above is bit-identical.
         assert rel_l2(img, ref) < 1e-4
+
+
+@pytest.mark.parametrize("ychunks", [0, 3])
+def test_forward_several_z_tiles_and_y_chunks(mode, ychunks):
+    """A grid of three 128-row tiles (the last partial), several column tiles
+    and y chunks: every tile and chunk boundary of the kernels is crossed."""
+    A.set_shape(16, ychunks)
+    try:
+        vel, w = setup(n1=280, n2=52, n3=46, nt=14, seed=4)
+        coef = O.acoustic_coeffs(10.0, 10.0, 10.0)
+        tab = O.acoustic_damp_table(8, 0.04)
+        d_ref, p0, p1 = O.acoustic_forward(vel, coef, 8, tab, (135, 25, 22), w, 12)
+        d, l0, l1, _ = A.forward(vel, (10.0, 10.0, 10.0), 8, 0.04, (136, 26, 23), w, 13)
+    finally:
+        A.set_shape(16, 0)
+    assert np.abs(p1).max() > 0
+    if mode == "exact":
+        np.testing.assert_array_equal(d, d_ref)
+        np.testing.assert_array_equal(l0, p0)
+        np.testing.assert_array_equal(l1, p1)
+    else:
+        assert rel_l2(l1, p1) < 1e-5

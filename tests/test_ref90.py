@@ -130,3 +130,41 @@ def test_reference_fixtures_are_current():
         r = O.ref90_rtm(True, p["rho"], p["lam"], p["mu"], [np.zeros((nx, nz), F)] * 3, list(p["born"]),
                         dx, dt, nt, zsrc, xsrc, zrec, fp, abc)
         np.testing.assert_array_equal(np.stack(r["dm"]), p["image"])
+
+
+def _velocity_helpers():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("velocity_gpu_test", os.path.join(HERE, "test_gpu_velocity.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.parametrize("adj", [True, False])
+def test_velocity_imaging_restatement_equals_reference(adj):
+    """The velocity-parameterisation imaging condition and Born sources
+    (lame=.false., W/image-mod-rtm.f90:182-225) that tests/test_gpu_velocity.py
+    holds the GPU to, against the reference's own image_init, image_init2 and
+    image_op2 executed on the same float32 histories: equal to float32
+    rounding (the restatement sums in float64)."""
+    tv = _velocity_helpers()
+    rho, vp, vs = tv.models()
+    coefs, filt, _ = tv.histories(rho, vp, vs)
+    src = O.source_op2(tv.NT, tv.DT, tv.FP, tv.NS, dtype=np.float64)
+    H = O.forward(coefs, tv.NT, tv.DT, tv.ZSRC, tv.XSRC, src, tv.ABC, filt)
+    f32 = lambda a: np.asarray(a, F)
+    f64 = lambda a: np.asarray(a, F).astype(np.float64)
+    m = [f32(rho), f32(vp), f32(vs)]
+    S = [x.astype(np.float64) for x in O.image_init(f32(H[0]), f32(H[1]), F(tv.DX), F(tv.DT))]
+    rng = np.random.default_rng(2)
+    if adj:
+        A = [f32(rng.standard_normal(H[0].shape)) for _ in range(5)]
+        got = O.ref90_image(True, False, m, f32(H[0]), f32(H[1]), tv.DX, tv.DT, H=A)
+        want = tv.vel_images_reference(f64(rho), f64(vp), f64(vs), [a.astype(np.float64) for a in A], S)
+    else:
+        dm = [f32(rng.standard_normal(rho.shape)) for _ in range(3)]
+        got = O.ref90_image(False, False, m, f32(H[0]), f32(H[1]), tv.DX, tv.DT, dm=dm)
+        want = tv.vel_sources_reference(f64(rho), f64(vp), f64(vs), [d.astype(np.float64) for d in dm], S)
+    for a, b in zip(got, want):
+        assert np.linalg.norm(b) > 0
+        assert np.linalg.norm(a - b) <= 2e-6 * np.linalg.norm(b)

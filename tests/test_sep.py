@@ -72,3 +72,45 @@ def test_bad_headers(tmp_path):
     (tmp_path / "c.H").write_text('\t\tn1=2 in="b.bin" data_format="xdr_int"\n')
     with pytest.raises(ValueError):
         sep.read(str(tmp_path / "c.H"))
+
+
+GOLD_SEP = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sep")
+
+
+@pytest.mark.parametrize("name,axes", [
+    ("lambda-layer.H", [(300, 0.0, 4.0), (300, 0.0, 4.0)]),
+    ("dlambda-layer.H", [(300, 0.0, 4.0), (300, 0.0, 4.0)]),
+    ("seis-Vx-layer.H", [(3535, 0.0, 0.000565685), (300, 0.0, 4.0)]),
+    ("filter.H", [(45, 0.0, 1.0)]),
+])
+def test_reference_headers_parse(name, axes):
+    """The reference's own history headers (2d_rtm_restart/Dat, copied by
+    tests/golden/sep/copy_headers.py): axes, binary name and format."""
+    h = sep.read_header(os.path.join(GOLD_SEP, name))
+    assert sep.axes(h) == axes
+    assert h["data_format"] == "xdr_float"
+    assert h["in"].startswith("/data/") and h["in"].endswith(("@", "@ewzD0r"))
+
+
+def test_reference_headers_agree_with_the_reference_code():
+    """filter.H has abc+5 = 45 samples for abc = 40 (W/abc-mod.f90:42-56) and
+    the gathers' time step is rtm.f90's dt = 0.4*dx/(sqrt(2)*2000) for the
+    model's dx = 4 m, in single precision (W/rtm.f90:60)."""
+    f = sep.axes(sep.read_header(os.path.join(GOLD_SEP, "filter.H")))[0][0]
+    assert f == 40 + 5
+    ax = sep.axes(sep.read_header(os.path.join(GOLD_SEP, "seis-Vx-layer.H")))
+    dt = np.float32(0.4) * np.float32(4.0) / (np.sqrt(np.float32(2.0)) * np.float32(2000.0))
+    assert abs(ax[0][2] - float(dt)) < 5e-10
+    assert ax[1][2] == sep.axes(sep.read_header(os.path.join(GOLD_SEP, "lambda-layer.H")))[1][2]
+
+
+def test_reference_header_reads_a_local_binary(tmp_path):
+    """A reference header whose binary is re-pointed by an appended in= (the
+    later entry wins, as SEPlib reads it) reads xdr_float data in Fortran
+    axis order."""
+    text = open(os.path.join(GOLD_SEP, "filter.H")).read()
+    vals = (np.arange(45, dtype=np.float32) / 45).astype(">f4")
+    vals.tofile(tmp_path / "filter.H@")
+    (tmp_path / "filter.H").write_text(text + '\n\t\tin="filter.H@"\n')
+    a, _ = sep.read(str(tmp_path / "filter.H"))
+    np.testing.assert_array_equal(a, vals.astype(np.float32))
