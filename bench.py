@@ -580,6 +580,10 @@ CFG4 = dict(n1=512, n2=1024, n3=1024, d=10.0, dt=1e-3, nt=3000, vmin=1500.0, vma
 CFL_LIMIT_3D = 0.4419  # 2 / sqrt(3 * 6.8267): leapfrog limit of the 10th-order 3D Laplacian
 
 
+K3D_NAMES = {"slab": "k_acoustic3d_s", "slab-unpaired": "k_acoustic3d_s", "ring": "k_acoustic3d_t",
+             "pipelined": "k_acoustic3d_p"}
+
+
 def acoustic3d_block(args, steps, warmup, nt=None, n3=None):
     """3D acoustic 10th-order forward modelling,
     1024 x 1024 x 512 cells, dx=10 m, dt=1 ms, 20 Hz Ricker point source,
@@ -617,6 +621,7 @@ def acoustic3d_block(args, steps, warmup, nt=None, n3=None):
     wav = R.source_op2(window, c["dt"], c["fp"], 50)
     src = (11, n2 // 2, n3 // 2)
     A.set_shape(args.tile3d, 0)
+    A.set_kernel(args.kernel3d)
     for _ in range(warmup):
         A.forward(vel2, (c["d"],) * 3, c["damp_a"], c["damp_b"], src, wav[:8], c["zr"], on_device=True)
     torch.cuda.synchronize()
@@ -643,12 +648,15 @@ def acoustic3d_block(args, steps, warmup, nt=None, n3=None):
             "config": {"workload": f"3D acoustic 10th-order forward modelling, {n1}x{n2}x{n3}, "
                                    f"one step = {window} time steps, receivers on plane z={c['zr']}",
                        "vmax_realised": round(float(vmax), 1), "cfl": round(float(vmax) * c["dt"] / c["d"], 4),
-                       "cfl_limit": CFL_LIMIT_3D, "tile_x": args.tile3d, "inputs_vs_l2": "inputs larger than L2"},
+                       "cfl_limit": CFL_LIMIT_3D, "kernel": args.kernel3d,
+                       "tile_x": args.tile3d if args.kernel3d == "pipelined" else 16,
+                       "inputs_vs_l2": "inputs larger than L2"},
             "e2e": {"value": round(cells * window / e2e_s / 1e9, 2), "unit": "Gcell/s",
                     "h2d_bytes_per_step": 4 * n1 * n2 * n3, "d2h_bytes_per_step": 4 * window * n2 * n3 + 8 * n1 * n2 * n3},
             "gpu_launches": window * steps,
             "roofline": {"bound": "hbm", "achieved": round(rate * 16, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(rate * 16 / peak, 4), "peak_kind": kind, "kernel": "k_acoustic3d_p (16 B/cell)",
+                         "frac": round(rate * 16 / peak, 4), "peak_kind": kind,
+                         "kernel": K3D_NAMES[args.kernel3d] + " (16 B/cell)",
                          "traffic": None},
             "clocks": clocks}
     return line
@@ -687,6 +695,8 @@ def precond_block(args, steps, warmup, pairs=None, train_steps=None, ntest=None,
     against 10-iteration plain LSRTM at their Born data residuals."""
     import torch
     from elastic_gb300 import precond as PC
+    from elastic_gb300 import unet as UN
+    UN.set_gemm(args.gemm == "tc")
     c = dict(CFG3)
     if pairs:
         c["pairs"] = pairs
@@ -781,7 +791,9 @@ def precond_block(args, steps, warmup, pairs=None, train_steps=None, ntest=None,
             "gpu_launches": None,
             "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(tflops / peak, 4), "peak_kind": kind + " bf16 (cuBLAS burst)",
-                         "kernel": "k_gemm (mma.sync m16n8k16 BF16) over the whole training step", "traffic": None},
+                         "kernel": ("k_gemm_tc (tcgen05, forward and backward-data) + k_gemm (mma.sync, "
+                                    "backward-weights)" if args.gemm == "tc" else "k_gemm (mma.sync m16n8k16 BF16)")
+                                   + " over the whole training step", "traffic": None},
             "clocks": clocks}
     return line
 
@@ -887,12 +899,15 @@ def main():
     ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
+    ap.add_argument("--kernel3d", default="pipelined", choices=list(K3D_NAMES), help="3D step kernel")
+    ap.add_argument("--gemm", default="tc", choices=["tc", "mma"],
+                    help="U-Net GEMMs of the forward and backward-data passes: tcgen05 or mma.sync")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workload blocks")
     ap.add_argument("--no-ref-gpu", action="store_true", help="reference arm: skip the reference CUDA comparator")
-    ap.add_argument("--sec-pairs", type=int, default=512, help="training pairs of the secondary precond block")
-    ap.add_argument("--sec-train-steps", type=int, default=1500, help="Adam steps of the secondary precond block")
+    ap.add_argument("--sec-pairs", type=int, default=1024, help="training pairs of the secondary precond block")
+    ap.add_argument("--sec-train-steps", type=int, default=2000, help="Adam steps of the secondary precond block")
     ap.add_argument("--nt", type=int, default=None, help="override nt (profiling captures only)")
     ap.add_argument("--shots", type=int, default=None, help="override the shot count (profiling captures only)")
     args = ap.parse_args()

@@ -58,6 +58,7 @@ SIGNATURES = {
     "unet_layer_info": (_c_int, [_P, _c_int, _P]),
     "unet_get_params": (_c_int, [_P, _P]),
     "unet_set_params": (_c_int, [_P, _P]),
+    "unet_set_gemm": (_c_int, [_c_int]),
     "unet_forward": (_c_int, [_P, _P, _c_int, _P, _c_int]),
     "unet_loss_grad": (_c_int, [_P, _P, _P, _c_int, _c_int, _P, _P]),
     "unet_train_step": (_c_int, [_P, _P, _P, _c_int, _c_int, _c_float, _c_float, _c_float, _c_float, _P]),

@@ -15,10 +15,16 @@ def set_shape(tile_x=16, ychunks=0):
     check(load().acoustic3d_set(tile_x, ychunks))
 
 
-def set_kernel(ring=True):
-    """Step kernel for n1 % 4 == 0: the slice-ring kernel fed by bulk tensor
-    copies (default) or the cp.async-pipelined kernel with a register queue."""
-    check(load().acoustic3d_set_kernel(1 if ring else 0))
+KERNELS = {"slab": 0, "ring": 1, "pipelined": 2, "slab-unpaired": 3}
+
+
+def set_kernel(kind="slab"):
+    """Step kernel for n1 % 4 == 0: "slab" (default: bulk-tensor-copied x/z
+    slab, unrolled register queue, paired FP32 arithmetic), "slab-unpaired"
+    (the same with scalar instructions, identical results), "ring" (every
+    tap from a ring of copied slices) or "pipelined" (cp.async halo, shifted
+    register queue)."""
+    check(load().acoustic3d_set_kernel(KERNELS[kind]))
 
 
 def forward(vel2, d, damp_a, damp_b, src, wavelet, zr, record=True, on_device=False):

@@ -94,6 +94,64 @@ __device__ __forceinline__ float fs(float x, float y) { return EXACT ? __fsub_rn
 
 __device__ __forceinline__ float e4(const float4 &v, int j) { return j == 0 ? v.x : j == 1 ? v.y : j == 2 ? v.z : v.w; }
 
+// The complete update of a thread's 4 cells (rows z..z+3 of column x at
+// slice y, offset o of row z): the sponge factor, the source, the receiver
+// row, the imaging condition and the rim (rows outside the interior stay
+// zero).  acc: the Laplacian sums, p: p1 at the cells.  Threads whose cells
+// touch none of these take the straight-line update in the kernels instead
+// (same arithmetic with a factor of one); this branch is rarely taken.
+template <bool EXACT>
+__device__ __forceinline__ float4 cells_full(const Ac3DArgs &a, int z, int x, int y, long long o, float4 acc4,
+                                          float4 p4, float4 p0c, float4 velc)
+{
+    const float acc[4] = {acc4.x, acc4.y, acc4.z, acc4.w}, p[4] = {p4.x, p4.y, p4.z, p4.w};
+    float out[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int zz = z + j;
+        const bool inside = zz >= AR && zz < a.n1 - AR;
+        const float f = damp_of<EXACT>(a, zz, x, y);
+        const float p0v = e4(p0c, j);
+        const float p0d = f == 1.f ? p0v : fm<EXACT>(f, p0v);
+        float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), acc[j]), p[j]), p[j]), p0d);
+        const long long oj = o + j;
+        if (oj == a.src_o) v = fa<EXACT>(v, a.src_val);
+        if (inside && zz == a.zr) {
+            const long long ri = (long long)y * a.n2 + x;
+            if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
+            if (a.rec_out) a.rec_out[ri] = v;
+        }
+        if (inside && a.img) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
+        out[j] = inside ? ((f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v)) : 0.f;
+    }
+    return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+// True when none of a thread's 4 cells (rows z..z+3, column x) is on the
+// rim, the source or the receiver row, and no image is formed: then, on a
+// slice outside the sponge, the plain update applies.
+__device__ __forceinline__ bool cells_plain(const Ac3DArgs &a, int z, int x)
+{
+    if (a.img || z < AR || z + 3 >= a.n1 - AR) return false;
+    if ((a.rec_in || a.rec_out) && a.zr >= z && a.zr < z + 4) return false;
+    if (a.src_o >= 0) {
+        const long long s3 = (long long)a.n1 * a.n2;
+        const long long r = a.src_o % s3;
+        if (r / a.n1 == x && r % a.n1 >= z && r % a.n1 < z + 4) return false;
+    }
+    return true;
+}
+
+// Sponge distance of the thread's 4 rows and column (the slice's own
+// distance is added per slice).
+__device__ __forceinline__ int cells_edge(int z, int x, int n1, int n2)
+{
+    int e = edge_dist(x, n2);
+#pragma unroll
+    for (int j = 0; j < 4; j++) e = min(e, edge_dist(z + j, n1));
+    return e;
+}
+
 template <bool EXACT, int TX>
 __global__ void __launch_bounds__(TX * 32) k_acoustic3d(const __grid_constant__ Ac3DArgs a)
 {
@@ -243,6 +301,8 @@ __global__ void __launch_bounds__(TX * 32, TX == 8 ? 2 : 1) k_acoustic3d_p(const
     const bool grp = colok && z < n1;  // this thread's float4 exists
     const long long s2 = n1, s3 = (long long)n1 * n2;
     const long long ocol = (long long)x * s2 + z;
+    const bool plain = cells_plain(a, z, x);
+    const int ezx = cells_edge(z, x, n1, n2);
     auto L4 = [&](const float *p, long long o) -> float4 {
         return grp ? __ldg(reinterpret_cast<const float4 *>(p + o)) : make_float4(0.f, 0.f, 0.f, 0.f);
     };
@@ -318,26 +378,17 @@ __global__ void __launch_bounds__(TX * 32, TX == 8 ? 2 : 1) k_acoustic3d_p(const
                     accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[3 + 3 * (k - 1)], yp));
                 }
             }
-            float out[4];
+            float out[4], pv[4];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int zz = z + j;
-                const float p = e4(q[5], j);
-                const float acc = accv[j];
-                const bool inside = zz >= AR && zz < n1 - AR;
-                const float f = damp_of<EXACT>(a, zz, x, y);
-                const float p0v = e4(p0c, j);
-                const float p0d = f == 1.f ? p0v : fm<EXACT>(f, p0v);
-                float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), acc), p), p), p0d);
-                const long long oj = o + j;
-                if (oj == a.src_o) v = fa<EXACT>(v, a.src_val);
-                if (inside && zz == a.zr) {
-                    const long long ri = (long long)y * n2 + x;
-                    if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
-                    if (a.rec_out) a.rec_out[ri] = v;
-                }
-                if (inside && a.img) a.img[oj] = fa<EXACT>(a.img[oj], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[oj]));
-                out[j] = inside ? ((f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v)) : 0.f;
+            for (int j = 0; j < 4; j++) pv[j] = e4(q[5], j);
+            if (__builtin_expect(plain && (!a.damp || min(ezx, edge_dist(y, n3)) >= a.damp_a), 1)) {
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    out[j] = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), accv[j]), pv[j]), pv[j]), e4(p0c, j));
+            } else {
+                const float4 r = cells_full<EXACT>(a, z, x, y, o, make_float4(accv[0], accv[1], accv[2], accv[3]),
+                                                   q[5], p0c, velc);
+                out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
             }
             *reinterpret_cast<float4 *>(a.p2 + o) = make_float4(out[0], out[1], out[2], out[3]);
         }
@@ -379,7 +430,6 @@ constexpr size_t T3_SMEM = (size_t)T3_NR * T3_SLICE * sizeof(float) + 128 + T3_N
 
 struct Ac3DTArgs {
     Ac3DArgs a;
-    int src_z, src_x, src_y;  // source cell (0-based), src_y = -1: none
     CUtensorMap tm;           // p1: n1 x n2 x n3, box {A_LZ, T3_LX, 1}
 };
 
@@ -405,14 +455,12 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
     const bool grp = x < n2 - AR && z < n1;  // this thread's float4 exists
     const long long s3 = (long long)n1 * n2;
     const long long ocol = (long long)x * n1 + z;
-    // per-thread constants: sponge distance of the 4 rows and the column,
-    // source and receiver rows within the 4 cells (-1: none)
-    int ezx = edge_dist(x, n2);
-#pragma unroll
-    for (int j = 0; j < 4; j++) ezx = min(ezx, edge_dist(z + j, n1));
-    const int sj = (A.src_y >= 0 && A.src_x == x && A.src_z >= z && A.src_z < z + 4) ? A.src_z - z : -1;
-    const int rj = (a.zr >= AR && a.zr < n1 - AR && a.zr >= z && a.zr < z + 4 && (a.rec_in || a.rec_out)) ? a.zr - z : -1;
+    // per-thread constants: the plain update applies (no rim, source or
+    // receiver cell), sponge distance of the 4 rows and the column
+    const bool plain = cells_plain(a, z, x);
+    const int ezx = cells_edge(z, x, n1, n2);
     auto slot = [&](int s) { return (s - (ya - AR)) % T3_NR; };
+    auto wrap = [](int t) { return t >= T3_NR ? t - T3_NR : t; };  // t in [0, 2 T3_NR)
     auto issue = [&](int s) {
         const int k = slot(s);
         mbar_expect_tx(&full[k], (unsigned)(T3_SLICE * sizeof(float)));
@@ -432,7 +480,8 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
     float4 p0c = L4(a.p0, ocol + (long long)ya * s3), velc = L4(a.vel, ocol + (long long)ya * s3);
     const float *coef = a.coef;
     const int cofs = (warp + AR) * A_LZ + (4 * lane + A_ZH);  // this thread's float4 within a slice
-    for (int y = ya; y < yb; y++) {
+    int sy = AR;  // ring slot of slice y
+    for (int y = ya; y < yb; y++, sy = wrap(sy + 1)) {
         // slices y-5 .. y+5 resident: wait for y+5 (and, first, for y-5 .. y+4)
         bool ok = true;
         for (int s = (y == ya ? ya - AR : y + AR); s <= y + AR; s++) {
@@ -452,7 +501,7 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
             veln = L4(a.vel, ocol + (long long)(y + 1) * s3);
         }
         if (grp) {
-            const float *cz = ring + slot(y) * T3_SLICE + cofs;
+            const float *cz = ring + sy * T3_SLICE + cofs;
             float w[20];
 #pragma unroll
             for (int i = 0; i < 20; i += 4) {
@@ -466,8 +515,8 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
             for (int k = 1; k <= AR; k++) {
                 const float4 xm = *reinterpret_cast<const float4 *>(cz - k * A_LZ);
                 const float4 xp = *reinterpret_cast<const float4 *>(cz + k * A_LZ);
-                const float4 ym = *reinterpret_cast<const float4 *>(ring + slot(y - k) * T3_SLICE + cofs);
-                const float4 yq = *reinterpret_cast<const float4 *>(ring + slot(y + k) * T3_SLICE + cofs);
+                const float4 ym = *reinterpret_cast<const float4 *>(ring + wrap(sy + T3_NR - k) * T3_SLICE + cofs);
+                const float4 yq = *reinterpret_cast<const float4 *>(ring + wrap(sy + k) * T3_SLICE + cofs);
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const float zp = fa<EXACT>(w[8 + j + k], w[8 + j - k]);
@@ -478,26 +527,17 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
                     accv[j] = fa<EXACT>(accv[j], fm<EXACT>(coef[3 + 3 * (k - 1)], yp));
                 }
             }
-            const bool nodamp = !a.damp || min(ezx, edge_dist(y, n3)) >= a.damp_a;
             const long long o = ocol + (long long)y * s3;
             float out[4];
+            if (__builtin_expect(plain && (!a.damp || min(ezx, edge_dist(y, n3)) >= a.damp_a), 1)) {
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int zz = z + j;
-                const float p = w[8 + j];
-                const bool inside = zz >= AR && zz < n1 - AR;
-                const float f = nodamp ? 1.f : damp_of<EXACT>(a, zz, x, y);
-                const float p0v = e4(p0c, j);
-                const float p0d = f == 1.f ? p0v : fm<EXACT>(f, p0v);
-                float v = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), accv[j]), p), p), p0d);
-                if (j == sj && y == A.src_y) v = fa<EXACT>(v, a.src_val);
-                if (j == rj) {
-                    const long long ri = (long long)y * n2 + x;
-                    if (a.rec_in) v = fa<EXACT>(v, a.rec_in[ri]);
-                    if (a.rec_out) a.rec_out[ri] = v;
-                }
-                if (IMG && inside) a.img[o + j] = fa<EXACT>(a.img[o + j], fm<EXACT>(fm<EXACT>(1e-6f, v), a.simg[o + j]));
-                out[j] = inside ? ((f == 1.f || a.raw_out) ? v : fm<EXACT>(f, v)) : 0.f;
+                for (int j = 0; j < 4; j++)
+                    out[j] = fs<EXACT>(fa<EXACT>(fa<EXACT>(fm<EXACT>(e4(velc, j), accv[j]), w[8 + j]), w[8 + j]),
+                                       e4(p0c, j));
+            } else {
+                const float4 r = cells_full<EXACT>(a, z, x, y, o, make_float4(accv[0], accv[1], accv[2], accv[3]),
+                                                   make_float4(w[8], w[9], w[10], w[11]), p0c, velc);
+                out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
             }
             *reinterpret_cast<float4 *>(a.p2 + o) = make_float4(out[0], out[1], out[2], out[3]);
         }
@@ -506,44 +546,308 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
     }
 }
 
-int g_ac_ring = 1;  // 1: ring kernel where n1 % 4 == 0; 0: cp.async pipelined kernel
+// Slab kernel (default for n1 % 4 == 0).  The same tiles and march as
+// k_acoustic3d_p, arranged so that every thread runs the same straight-line
+// code on every slice:
+// - the x and z taps come from a slab of slice y (the tile's 144 rows by
+//   26 columns) that one thread loads by a bulk tensor copy two slices ahead
+//   into one of three slots, completing on an mbarrier (bounded wait);
+// - the y taps come from a register queue of S3_Q float4 (slices y-5 .. y+5
+//   and the load of y+6 in flight); the march is unrolled by S3_Q, so each
+//   slot has a fixed register and nothing is shifted;
+// - the sponge factor is a per-slice branch that is uniform across the CTA
+//   (the tile's least edge distance against the slice's): inside the
+//   sponge every cell looks its factor up, a factor of one leaving a value
+//   unchanged; the rim rows are zeroed by a select in the CTAs that hold
+//   any; only the threads holding the source or the receiver row branch
+//   off, for a few instructions;
+// - the arithmetic runs on pairs of cells (cells 0-1 and 2-3 of a thread),
+//   with the paired single-precision instructions when PK is set; every
+//   operation is rounded separately as in the scalar form (fused
+//   multiply-adds in fast mode), so PK changes no bit of the result.
+constexpr int S3_NS = 3;                 // slab slots
+constexpr int S3_Q = 12;                 // register queue depth = unroll of the march
+constexpr size_t S3_SMEM = (size_t)S3_NS * T3_SLICE * sizeof(float) + 128 + S3_NS * 8;
 
-template <bool EXACT>
-int launch_ac_ring(const Ac3DArgs &a0, int ychunks, cudaStream_t st)
+template <bool PK>
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    if (PK) return __fadd2_rn(a, b);
+    return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+template <bool PK>
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    if (PK) return __fmul2_rn(a, b);
+    return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+template <bool PK>
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
+{
+    if (PK) return __ffma2_rn(a, b, c);
+    return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
+}
+// acc + c x: two roundings in exact mode, one (fused) in fast mode
+template <bool EXACT, bool PK>
+__device__ __forceinline__ float2 mac2(float2 acc, float2 c, float2 x)
+{
+    return EXACT ? add2<PK>(acc, mul2<PK>(c, x)) : fma2<PK>(c, x, acc);
+}
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 bc2(float c) { return make_float2(c, c); }
+
+template <bool EXACT, bool IMG, bool PK>
+__global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_constant__ Ac3DTArgs A)
+{
+    const Ac3DArgs &a = A.a;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *slab = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(slab + S3_NS * T3_SLICE);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n1 = a.n1, n2 = a.n2, n3 = a.n3;
+    const int ntz = (n1 - 9 + A_TZ - 1) / A_TZ;  // rows 4 .. n1-6 (interior plus row 4)
+    int b = blockIdx.x;
+    const int yc = b % a.ychunks;
+    b /= a.ychunks;
+    const int tzi = b % ntz, txi = b / ntz;
+    const int z0 = 4 + tzi * A_TZ, x0 = AR + txi * T3_TX;
+    const int ylen = (n3 - 2 * AR + a.ychunks - 1) / a.ychunks;
+    const int ya = AR + yc * ylen, yb = min(n3 - AR, ya + ylen);
+    if (ya >= yb) return;
+    const int z = z0 + 4 * lane, x = x0 + warp;
+    const bool grp = x < n2 - AR && z < n1;  // this thread's float4 exists
+    const long long s3 = (long long)n1 * n2;
+    // tile constants (uniform): least sponge distance over the tile's
+    // interior cells (edge_dist is smallest at a range's ends), rim rows
+    const int zlo = max(z0, AR), zhi = min(z0 + A_TZ - 1, n1 - AR - 1), xhi = min(x0 + T3_TX - 1, n2 - AR - 1);
+    const int tile_e = min(min(edge_dist(zlo, n1), edge_dist(zhi, n1)), min(edge_dist(x0, n2), edge_dist(xhi, n2)));
+    const bool tile_rim = z0 < AR || z0 + A_TZ > n1 - AR;
+    const bool damped = a.damp != nullptr;
+    // per-thread special cells: the receiver row's component rj and the
+    // source's component sj (at slice ys), -1 where none
+    int rj = -1, sj = -1, ys = -1;
+    if (grp && (a.rec_in || a.rec_out) && a.zr >= z && a.zr < z + 4 && a.zr >= AR && a.zr < n1 - AR) rj = a.zr - z;
+    if (grp && a.src_o >= 0) {
+        const long long r = a.src_o % s3;
+        const int sx = (int)(r / n1), sz = (int)(r % n1);
+        if (sx == x && sz >= z && sz < z + 4) {
+            sj = sz - z;
+            ys = (int)(a.src_o / s3);
+        }
+    }
+    auto issue = [&](int s, int k) {
+        mbar_expect_tx(&full[k], (unsigned)(T3_SLICE * sizeof(float)));
+        tma_load_3d(slab + k * T3_SLICE, &A.tm, z0 - A_ZH, x0 - AR, s, &full[k]);
+    };
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < S3_NS; k++) mbar_init(&full[k]);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        issue(ya, 0);
+        if (ya + 1 < yb) issue(ya + 1, 1);
+    }
+    const float *pp1 = a.p1 + (long long)x * n1 + z;  // this thread's column in each array
+    const float *pp0 = a.p0 + (long long)x * n1 + z, *pvel = a.vel + (long long)x * n1 + z;
+    float *pp2 = a.p2 + (long long)x * n1 + z;
+    auto L4 = [&](const float *p, int y) -> float4 {
+        return grp ? __ldg(reinterpret_cast<const float4 *>(p + (long long)y * s3)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    // queue slot of slice s: (s - ya + 5) % S3_Q
+    float4 q[S3_Q];
+#pragma unroll
+    for (int k = 0; k < 2 * AR + 1; k++) q[k] = L4(pp1, ya - AR + k);
+    q[S3_Q - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 p0s[2], vels[2];
+    p0s[0] = L4(pp0, ya);
+    vels[0] = L4(pvel, ya);
+    p0s[1] = vels[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float *coef = a.coef;
+    const int cofs = (warp + AR) * A_LZ + (4 * lane + A_ZH);  // this thread's float4 within a slab
+    for (int yblk = ya; yblk < yb; yblk += S3_Q) {
+#pragma unroll
+        for (int u = 0; u < S3_Q; u++) {
+            const int y = yblk + u;
+            if (y >= yb) break;
+            const int ss = u % S3_NS;
+            const bool ok = mbar_wait(&full[ss], (unsigned)((u / S3_NS) & 1));
+            if (__syncthreads_or(!ok)) {
+                // record, let the copies in flight land (bounded) and stop
+                if (threadIdx.x == 0) {
+                    if (a.err) atomicExch(a.err, 1);
+                    for (int s = y; s <= min(y + 1, yb - 1); s++) {
+                        const int v = s - yblk;
+                        mbar_wait(&full[v % S3_NS], (unsigned)((v / S3_NS) & 1));
+                    }
+                }
+                __syncthreads();
+                return;
+            }
+            // every thread is past slice y-1: its slot takes slice y+2
+            if (threadIdx.x == 0 && y + 2 < yb) issue(y + 2, (u + 2) % S3_NS);
+            if (y + 6 <= yb - 1 + AR) q[(u + 11) % S3_Q] = L4(pp1, y + 6);
+            float4 imgc = make_float4(0.f, 0.f, 0.f, 0.f), simgc = imgc;
+            if (IMG && grp) {
+                imgc = *reinterpret_cast<const float4 *>(a.img + (long long)x * n1 + z + (long long)y * s3);
+                simgc = __ldg(reinterpret_cast<const float4 *>(a.simg + (long long)x * n1 + z + (long long)y * s3));
+            }
+            if (y + 1 < yb) {
+                p0s[(u + 1) & 1] = L4(pp0, y + 1);
+                vels[(u + 1) & 1] = L4(pvel, y + 1);
+            }
+            if (!grp) continue;
+            const float *cz = slab + ss * T3_SLICE + cofs;
+            float w[20];  // rows z-8 .. z+11 of column x
+#pragma unroll
+            for (int i = 0; i < 20; i += 4) {
+                const float4 t = *reinterpret_cast<const float4 *>(cz - 8 + i);
+                w[i] = t.x; w[i + 1] = t.y; w[i + 2] = t.z; w[i + 3] = t.w;
+            }
+            const float4 pc = q[(u + AR) % S3_Q];
+            float2 acc[2] = {mul2<PK>(bc2(coef[0]), lo2(pc)), mul2<PK>(bc2(coef[0]), hi2(pc))};
+#pragma unroll
+            for (int k = 1; k <= AR; k++) {
+                const float4 xm = *reinterpret_cast<const float4 *>(cz - k * A_LZ);
+                const float4 xp = *reinterpret_cast<const float4 *>(cz + k * A_LZ);
+                const float4 ym = q[(u + AR - k) % S3_Q], yp = q[(u + AR + k) % S3_Q];
+                const float2 cz2 = bc2(coef[1 + 3 * (k - 1)]), cx2 = bc2(coef[2 + 3 * (k - 1)]),
+                             cy2 = bc2(coef[3 + 3 * (k - 1)]);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int j = 2 * h;
+                    // z pairs are register pairs only for even k
+                    const float2 zs = (k & 1) ? make_float2(__fadd_rn(w[8 + j + k], w[8 + j - k]),
+                                                            __fadd_rn(w[9 + j + k], w[9 + j - k]))
+                                              : add2<PK>(make_float2(w[8 + j + k], w[9 + j + k]),
+                                                         make_float2(w[8 + j - k], w[9 + j - k]));
+                    acc[h] = mac2<EXACT, PK>(acc[h], cz2, zs);
+                    acc[h] = mac2<EXACT, PK>(acc[h], cx2, add2<PK>(h ? hi2(xp) : lo2(xp), h ? hi2(xm) : lo2(xm)));
+                    acc[h] = mac2<EXACT, PK>(acc[h], cy2, add2<PK>(h ? hi2(yp) : lo2(yp), h ? hi2(ym) : lo2(ym)));
+                }
+            }
+            const float4 p0c = p0s[u & 1], velc = vels[u & 1];
+            // sponge factors of the 4 cells (uniform branch)
+            const bool sp = damped && min(tile_e, edge_dist(y, n3)) < a.damp_a;
+            float2 fac[2] = {bc2(1.f), bc2(1.f)};
+            if (sp) {
+                const int m = min(edge_dist(x, n2), edge_dist(y, n3));
+                float f[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int e = min(edge_dist(z + j, n1), m);
+                    f[j] = 1.f;
+                    if (e >= 0 && e < a.damp_a) f[j] = fminf(__ldg(a.damp + e), 1.f);
+                }
+                fac[0] = make_float2(f[0], f[1]);
+                fac[1] = make_float2(f[2], f[3]);
+            }
+            float2 v[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float2 p = h ? hi2(pc) : lo2(pc);
+                const float2 p0d = sp ? mul2<PK>(fac[h], h ? hi2(p0c) : lo2(p0c)) : (h ? hi2(p0c) : lo2(p0c));
+                const float2 vel = h ? hi2(velc) : lo2(velc);
+                float2 t = EXACT ? add2<PK>(mul2<PK>(vel, acc[h]), p) : fma2<PK>(vel, acc[h], p);
+                t = add2<PK>(t, p);
+                v[h] = fma2<PK>(p0d, bc2(-1.f), t);  // t - p0d, one rounding
+            }
+            if (rj >= 0 || (sj >= 0 && y == ys)) {
+                float vv[4] = {v[0].x, v[0].y, v[1].x, v[1].y};
+                const long long ri = (long long)y * n2 + x;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (j == sj && y == ys) vv[j] = __fadd_rn(vv[j], a.src_val);
+                    if (j == rj) {
+                        if (a.rec_in) vv[j] = __fadd_rn(vv[j], a.rec_in[ri]);
+                        if (a.rec_out) a.rec_out[ri] = vv[j];
+                    }
+                }
+                v[0] = make_float2(vv[0], vv[1]);
+                v[1] = make_float2(vv[2], vv[3]);
+            }
+            const long long o = (long long)y * s3;
+            if (IMG) {
+                float2 im[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const float2 t = mul2<PK>(bc2(1e-6f), v[h]);
+                    const float2 ic = h ? hi2(imgc) : lo2(imgc), sc = h ? hi2(simgc) : lo2(simgc);
+                    im[h] = EXACT ? add2<PK>(ic, mul2<PK>(t, sc)) : fma2<PK>(t, sc, ic);
+                }
+                float r[4] = {im[0].x, im[0].y, im[1].x, im[1].y};
+                if (tile_rim) {
+                    const float c[4] = {imgc.x, imgc.y, imgc.z, imgc.w};
+#pragma unroll
+                    for (int j = 0; j < 4; j++)
+                        if (z + j < AR || z + j >= n1 - AR) r[j] = c[j];
+                }
+                *reinterpret_cast<float4 *>(a.img + (long long)x * n1 + z + o) = make_float4(r[0], r[1], r[2], r[3]);
+            }
+            float2 out[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) out[h] = (sp && !a.raw_out) ? mul2<PK>(fac[h], v[h]) : v[h];
+            float r[4] = {out[0].x, out[0].y, out[1].x, out[1].y};
+            if (tile_rim) {
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (z + j < AR || z + j >= n1 - AR) r[j] = 0.f;
+            }
+            *reinterpret_cast<float4 *>(pp2 + o) = make_float4(r[0], r[1], r[2], r[3]);
+        }
+    }
+}
+
+// Step kernel where n1 % 4 == 0 and tensor maps are available:
+// 0 slab (default), 1 ring, 2 cp.async pipelined, 3 slab without the paired
+// instructions (same results as 0)
+int g_ac_kind = 2;
+
+// Launch of a kernel that takes Ac3DTArgs (p1's tensor map, box of the
+// tile's 144 rows by 26 columns) with dynamic shared memory smem.
+template <typename K>
+int launch_tma3d(K kern, int variant, size_t smem, const Ac3DArgs &a0, int ychunks, cudaStream_t st)
 {
     Ac3DTArgs t;
     memset(&t, 0, sizeof t);
     t.a = a0;
     t.a.ychunks = ychunks;
-    t.src_z = t.src_x = t.src_y = -1;
-    if (a0.src_o >= 0) {
-        const long long s3 = (long long)a0.n1 * a0.n2;
-        t.src_y = (int)(a0.src_o / s3);
-        t.src_x = (int)((a0.src_o % s3) / a0.n1);
-        t.src_z = (int)(a0.src_o % a0.n1);
-    }
     TRY(make_map(&t.tm, a0.p1, false, a0.n1, a0.n2, a0.n3, (long long)a0.n1 * a0.n2, A_LZ, T3_LX));
-    auto kern = a0.img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>;
-    static bool attr[RTM_MAX_DEVICES][2] = {};
+    static bool attr[RTM_MAX_DEVICES][16] = {};
     {
         const int dev = rtm_current_device();
         std::lock_guard<std::mutex> lk(rtm_device_state_lock());
-        if (!attr[dev][a0.img != nullptr]) {
-            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T3_SMEM));
-            attr[dev][a0.img != nullptr] = true;
+        if (!attr[dev][variant]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr[dev][variant] = true;
         }
     }
     const int ntz = (a0.n1 - 9 + A_TZ - 1) / A_TZ;
     const int ntx = (a0.n2 - 2 * AR + T3_TX - 1) / T3_TX;
-    kern<<<ntz * ntx * ychunks, T3_TX * 32, T3_SMEM, st>>>(t);
+    kern<<<ntz * ntx * ychunks, T3_TX * 32, smem, st>>>(t);
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }
 
 template <bool EXACT>
+int launch_ac_tma(const Ac3DArgs &a0, int ychunks, cudaStream_t st)
+{
+    const bool img = a0.img != nullptr;
+    const int v = (EXACT ? 8 : 0) + (img ? 4 : 0);
+    switch (g_ac_kind) {
+    case 1: return launch_tma3d(img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>, v, T3_SMEM, a0, ychunks, st);
+    case 3: return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, false> : k_acoustic3d_s<EXACT, false, false>, v + 2,
+                                S3_SMEM, a0, ychunks, st);
+    default: return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, true> : k_acoustic3d_s<EXACT, false, true>, v + 3,
+                                 S3_SMEM, a0, ychunks, st);
+    }
+}
+
+template <bool EXACT>
 int launch_ac(const Ac3DArgs &a0, int tx, int ychunks, cudaStream_t st)
 {
-    if (a0.n1 % 4 == 0 && g_ac_ring && tensor_maps_available()) return launch_ac_ring<EXACT>(a0, ychunks, st);
+    if (a0.n1 % 4 == 0 && g_ac_kind != 2 && tensor_maps_available()) return launch_ac_tma<EXACT>(a0, ychunks, st);
     Ac3DArgs a = a0;
     a.ychunks = ychunks;
     const int ntx = (a.n2 - 2 * AR + tx - 1) / tx;
@@ -655,16 +959,19 @@ int pick_ychunks(int n1, int n2, int tx)
     if (g_ac_ych > 0) return g_ac_ych;
     const int ntz = n1 % 4 == 0 ? (n1 - 9 + A_TZ - 1) / A_TZ : (n1 - 2 * AR + A_TZ - 1) / A_TZ;
     const int ntx = (n2 - 2 * AR + tx - 1) / tx;
-    const bool ring = n1 % 4 == 0 && g_ac_ring;
-    const int nsm = device_sm_count() * (tx == 8 && !ring ? 2 : 1);
+    const bool tma = n1 % 4 == 0 && g_ac_kind != 2;
+    const int nsm = device_sm_count() * (tx == 8 && !tma ? 2 : 1);
     int best = 1;
     double best_eff = 0;
     for (int c = 1; c <= 8; c++) {
         const int g = ntz * ntx * c;
         const double waves = (double)g / nsm;
-        // each chunk loads the 10 slices around its y range once more
+        // each chunk reads the 10 slices of p1 around its y range once more
+        // (the ring kernel all four arrays' worth of time, the slab kernel
+        // one array of four)
         const double ylen = (double)(n3_hint() - 2 * AR) / c;
-        const double eff = waves / std::ceil(waves) * (ring ? ylen / (ylen + 10.0) : 1.0 - 0.01 * c);
+        const double extra = g_ac_kind == 1 ? 10.0 : 2.5;
+        const double eff = waves / std::ceil(waves) * (tma ? ylen / (ylen + extra) : 1.0 - 0.01 * c);
         if (eff > best_eff) { best_eff = eff; best = c; }
     }
     return best;
@@ -677,7 +984,7 @@ int pick_ychunks(int n1, int n2, int tx)
 int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, float dir, int zr, float *d_dev,
                float **last0, float **last1)
 {
-    m.tx = g_ac_ring && m.n1 % 4 == 0 ? T3_TX : g_ac_tx;
+    m.tx = g_ac_kind != 2 && m.n1 % 4 == 0 ? T3_TX : g_ac_tx;
     g_ac_n3 = m.n3;
     m.ych = pick_ychunks(m.n1, m.n2, m.tx);
     TRY(m.buf.alloc(2 * m.vol));
@@ -696,10 +1003,10 @@ int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, floa
 
 }  // namespace
 
-extern "C" int acoustic3d_set_kernel(int ring)
+extern "C" int acoustic3d_set_kernel(int kind)
 {
-    RTM_CHECK_ARG(ring == 0 || ring == 1, "ring must be 0 or 1");
-    g_ac_ring = ring;
+    RTM_CHECK_ARG(kind >= 0 && kind <= 3, "kind must be 0 (slab), 1 (ring), 2 (pipelined) or 3 (slab, unpaired)");
+    g_ac_kind = kind;
     return RTM_OK;
 }
 

@@ -2,8 +2,11 @@
 // U-Net (about 0.9M parameters) with BF16 weights and activations and FP32
 // accumulation, trained with Adam.  Every convolution pass -- forward,
 // backward-data and backward-weights -- is one tensor-core GEMM of this file
-// (mma.sync m16n8k16 BF16, FP32 accumulators, cp.async 3-stage pipeline)
-// on im2col operands in NHWC layout.
+// on im2col operands in NHWC layout: the forward and backward-data passes on
+// the fifth-generation tensor cores (tcgen05 MMAs, accumulators in tensor
+// memory, k_gemm_tc), the backward-weights pass (both operands transposed,
+// split over K with FP32 atomics) with mma.sync m16n8k16 (k_gemm, cp.async
+// 3-stage pipeline), which also serves every pass when unet_set_gemm(0).
 //
 // Network (channels c = 32, 64, 96, 128; 3x3 convolutions with leaky ReLU,
 // slope LEAK for negative inputs, which keeps units from dying without any
@@ -28,12 +31,28 @@
 
 #include "../../include/elastic_rtm.h"
 #include "common.cuh"
+#include "elastic2d_v2.cuh"
 #include "engine.h"
+#include "umma.cuh"
 
 namespace {
 
 using bf16 = __nv_bfloat16;
 using eg::DevBuf;
+using eg::fence_async_smem;
+using eg::mbar_init;
+using eg::mbar_wait;
+using eg::smem_u32;
+using eg::tc_fence_after;
+using eg::tc_fence_before;
+using eg::tmem_alloc;
+using eg::tmem_dealloc;
+using eg::tmem_ld16;
+using eg::tmem_relinquish;
+using eg::umma_commit;
+using eg::umma_f16;
+using eg::umma_idesc_f16;
+using eg::umma_sdesc;
 
 // ----------------------------------------------------------------- GEMM
 // C[M,N] = A[M,K] * B[N,K]^T with BF16 operands and FP32 accumulation.
@@ -60,6 +79,7 @@ struct GemmArgs {
     int conv;
     const bf16 *X;
     int ldx, xoff, C, H, W;
+    int *err;  // tensor-core GEMM: set when a bounded wait ran out (nullable)
 };
 
 constexpr int GBM = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
@@ -264,6 +284,227 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(const GemmArgs g)
             }
 }
 
+// ------------------------------------------------- tensor-core (tcgen05)
+// C[M,N] = A[M,K] * B[N,K]^T for K-major A (plain or implicit 3x3 im2col) and
+// B, one 128 x BN output tile per CTA (BN >= N, a multiple of 16), FP32
+// accumulation in tensor memory.  Per 64-wide K tile the 128 threads stage A
+// (128 x 64) and B (BN x 64) with cp.async into the canonical K-major layout
+// without swizzle -- 8-row x 16-byte core matrices, 128 bytes apart along K
+// and 1024 along M/N -- zero-filling rows past M or N and columns past K;
+// one thread issues four 128 x BN x 16 MMAs (tcgen05.mma .kind::f16, BF16
+// operands) and commits them to the stage's mbarrier.  Loads run S-2 tiles
+// ahead and refill the stage of the tile two back, so the tensor core always
+// has the next tiles queued while a stage is being refilled.  Each thread
+// loads the same 16-byte K column (8 K values) of the same 8 rows of every
+// tile: the rows' pixel coordinates are worked out once.  After the last
+// tile the four warps read the accumulator rows from tensor memory (warp w:
+// rows 32 w .. 32 w + 31) and apply the epilogue: bias, leaky ReLU, BF16 or
+// FP32 store.  Every wait is bounded; one that runs out sets g.err and the
+// tile's output is not written.
+constexpr int TC_BM = 128, TC_BK = 64, TC_THREADS = 128;
+constexpr int TC_ROWS = TC_THREADS / (TC_BK / 8);  // rows a thread pass covers (16)
+
+template <int BN>
+struct TcCfg {
+    static constexpr int A_BYTES = TC_BM * TC_BK * 2;
+    static constexpr int B_BYTES = BN * TC_BK * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int STAGES = (200 * 1024 / STAGE) < 6 ? (200 * 1024 / STAGE) : 6;
+    static constexpr uint32_t NCOLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 + 8 * (STAGES + 2);
+    static_assert(STAGES >= 4, "stages");
+};
+
+template <int BN, int EPI>
+__global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(const __grid_constant__ GemmArgs g)
+{
+    using T = TcCfg<BN>;
+    constexpr int S = T::STAGES, D = S - 2;  // load-ahead distance
+    constexpr int AR_ = TC_BM / TC_ROWS, BR_ = BN / TC_ROWS;  // row passes of A and B (8, BN/16)
+    extern __shared__ __align__(16) unsigned char tc_raw[];
+    unsigned char *base = tc_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(tc_raw) & 1023u)) & 1023u);
+    unsigned long long *freeb = reinterpret_cast<unsigned long long *>(base + S * T::STAGE);
+    unsigned long long *done = freeb + S;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_BM;
+    const int ktiles = (g.K + TC_BK - 1) / TC_BK;
+    if (warp == 0) {
+        tmem_alloc(tslot, T::NCOLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < S; i++) mbar_init(&freeb[i]);
+        mbar_init(done);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    // this thread's K column (8 values at q*8) and rows r0 + 16 i
+    const int q = tid & 7, r0 = tid >> 3;
+    // shared-memory byte offset of (row r, K column q) in a tile
+    auto dst_of = [&](int r) { return ((r >> 3) << 10) | (q << 7) | ((r & 7) << 4); };
+    // pixel coordinates of the A rows (implicit im2col)
+    int pix[AR_], py[AR_], px[AR_];
+#pragma unroll
+    for (int i = 0; i < AR_; i++) {
+        const int m = m0 + r0 + TC_ROWS * i;
+        pix[i] = m < g.M ? m : -1;
+        if (g.conv && m < g.M) {
+            px[i] = m % g.W;
+            py[i] = (m / g.W) % g.H;
+        } else {
+            px[i] = py[i] = 0;
+        }
+    }
+    auto load = [&](int kt, int stage) {
+        unsigned char *sa = base + stage * T::STAGE, *sb = sa + T::A_BYTES;
+        const int kk = kt * TC_BK + q * 8;
+        const bool kok = kk < g.K;
+        if (g.conv) {
+            const int tap = kk / g.C, c = kk - tap * g.C;
+            const int ky = tap / 3, kx = tap - 3 * ky;
+            const bool tok = kok && tap < 9;
+            const long long dpix = (long long)(ky - 1) * g.W + (kx - 1);
+#pragma unroll
+            for (int i = 0; i < AR_; i++) {
+                const int yy = py[i] + ky - 1, xx = px[i] + kx - 1;
+                const bool ok = tok && pix[i] >= 0 && yy >= 0 && yy < g.H && xx >= 0 && xx < g.W;
+                const bf16 *src = ok ? g.X + ((long long)pix[i] + dpix) * g.ldx + g.xoff + c : g.X;
+                cpa16(sa + dst_of(r0 + TC_ROWS * i), src, ok);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < AR_; i++) {
+                const bool ok = kok && pix[i] >= 0;
+                cpa16(sa + dst_of(r0 + TC_ROWS * i), g.A + (ok ? (long long)pix[i] * g.lda + kk : 0), ok);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < BR_; i++) {
+            const int r = r0 + TC_ROWS * i;
+            const bool ok = kok && r < g.N;
+            cpa16(sb + dst_of(r), g.B + (ok ? (long long)r * g.ldb + kk : 0), ok);
+        }
+    };
+    constexpr uint32_t IDESC = umma_idesc_f16(TC_BM, BN, true, true);
+#pragma unroll
+    for (int t = 0; t < D; t++) {
+        if (t < ktiles) load(t, t);
+        asm volatile("cp.async.commit_group;\n" ::);
+    }
+    bool fail = false;
+    for (int kt = 0; kt < ktiles; kt++) {
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(D - 1));
+        fence_async_smem();
+        __syncthreads();
+        const int stage = kt % S;
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(base + stage * T::STAGE), b_addr = a_addr + T::A_BYTES;
+#pragma unroll
+            for (int k = 0; k < TC_BK / 16; k++)
+                umma_f16(tmem, umma_sdesc(a_addr + 256 * k, 128, 1024, 0), umma_sdesc(b_addr + 256 * k, 128, 1024, 0),
+                         IDESC, kt > 0 || k > 0);
+            umma_commit(&freeb[stage]);
+        }
+        const int nt = kt + D;
+        if (nt < ktiles && !fail) {
+            // tile nt goes into the stage of tile nt - S = kt - 2, once that
+            // tile's MMAs (committed two iterations ago) are done
+            if (nt >= S && !mbar_wait(&freeb[(nt - S) % S], (unsigned)(((nt - S) / S) & 1))) fail = true;
+            if (!fail) load(nt, nt % S);
+        }
+        asm volatile("cp.async.commit_group;\n" ::);
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    if (tid == 0) umma_commit(done);
+    bool ok = mbar_wait(done, 0);
+    if (!ok) ok = mbar_wait(done, 0);  // the MMAs may still be running: a second limit
+    tc_fence_after();
+    if (__syncthreads_or(fail || !ok)) {
+        if (tid == 0 && g.err) atomicExch(g.err, 1);
+    } else {
+        const int m = m0 + 32 * warp + lane;
+#pragma unroll
+        for (int c = 0; c < BN; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+            if (m >= g.M) continue;
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int n = c + j;
+                if (n < g.N && g.bias) v[j] += g.bias[n];
+                if (EPI == EPI_BF16 && g.relu) v[j] = v[j] > 0.f ? v[j] : LEAK * v[j];
+            }
+            if (EPI == EPI_F32) {
+                float *dst = g.Cf + (long long)m * g.ldc + c;
+                if (c + 16 <= g.N && (g.ldc & 3) == 0) {
+#pragma unroll
+                    for (int j = 0; j < 16; j += 4)
+                        *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (c + j < g.N) dst[j] = v[j];
+                }
+            } else {
+                bf16 *dst = g.Cb + (long long)m * g.ldc + g.coff + c;
+                if (c + 16 <= g.N && ((g.ldc | g.coff) & 7) == 0) {
+                    uint4 w[2];
+                    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(w);
+#pragma unroll
+                    for (int j = 0; j < 8; j++) h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                    reinterpret_cast<uint4 *>(dst)[0] = w[0];
+                    reinterpret_cast<uint4 *>(dst)[1] = w[1];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        if (c + j < g.N) dst[j] = __float2bfloat16_rn(v[j]);
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, T::NCOLS);
+}
+
+template <int BN, int EPI>
+int gemm_tc_launch(const GemmArgs &g, cudaStream_t st)
+{
+    using T = TcCfg<BN>;
+    auto kern = k_gemm_tc<BN, EPI>;
+    static bool attr[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::SMEM));
+            attr[dev] = true;
+        }
+    }
+    kern<<<(g.M + TC_BM - 1) / TC_BM, TC_THREADS, T::SMEM, st>>>(g);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+template <int EPI>
+int gemm_tc(const GemmArgs &g, cudaStream_t st)
+{
+    if (g.N <= 16) return gemm_tc_launch<16, EPI>(g, st);
+    if (g.N <= 32) return gemm_tc_launch<32, EPI>(g, st);
+    if (g.N <= 64) return gemm_tc_launch<64, EPI>(g, st);
+    if (g.N <= 96) return gemm_tc_launch<96, EPI>(g, st);
+    if (g.N <= 128) return gemm_tc_launch<128, EPI>(g, st);
+    return gemm_tc_launch<256, EPI>(g, st);
+}
+
+int g_gemm_tc = 1;  // 1: tensor-core GEMMs for the non-transposed passes; 0: mma.sync only
+
 template <bool A_T, bool B_T, int BN, int WM, int EPI>
 int gemm_launch(const GemmArgs &g, int splits, cudaStream_t st)
 {
@@ -306,6 +547,10 @@ int gemm(const GemmArgs &g, bool a_t, bool b_t, int epi, int splits, cudaStream_
     RTM_CHECK_ARG(epi != EPI_BF16 || ((g.ldc | g.coff) & 1) == 0, "BF16 GEMM output needs even ldc and offset");
     RTM_CHECK_ARG(!g.conv || (g.C % 32 == 0 && (g.ldx | g.xoff) % 8 == 0 && g.X && g.H > 0 && g.W > 0),
                   "implicit im2col needs C %% 32 == 0 and 16-byte aligned channel runs");
+    const bool tc = g_gemm_tc && !a_t && !b_t && splits == 1 && g.kchunk >= g.K && g.N <= 256 &&
+                    (g.conv || (g.lda % 8 == 0 && g.A)) && g.ldb % 8 == 0;
+    if (tc && epi == EPI_BF16) return gemm_tc<EPI_BF16>(g, st);
+    if (tc && epi == EPI_F32) return gemm_tc<EPI_F32>(g, st);
     if (epi == EPI_BF16 && !a_t && !b_t) return gemm_bn<false, false, EPI_BF16>(g, splits, st);
     if (epi == EPI_F32 && !a_t && !b_t) return gemm_bn<false, false, EPI_F32>(g, splits, st);
     if (epi == EPI_F32_ATOMIC_T && a_t && b_t) return gemm_bn<true, true, EPI_F32_ATOMIC_T>(g, splits, st);
@@ -603,6 +848,7 @@ struct unet {
     DevBuf<bf16> col, gout;
     DevBuf<float> out, tgt;
     DevBuf<double> part;
+    DevBuf<int> err;  // set by a tensor-core GEMM whose bounded wait ran out
     cudaStream_t st = nullptr;
     int n_last = 0;
 
@@ -677,6 +923,8 @@ int setup(unet *u)
     TRY(u->out.alloc((size_t)P0 * 8));
     TRY(u->tgt.alloc((size_t)P0 * u->cout));
     TRY(u->part.alloc(4096));
+    TRY(u->err.alloc(1));
+    RTM_CUDA(cudaMemset(u->err.p, 0, sizeof(int)));
     return RTM_OK;
 }
 
@@ -744,6 +992,7 @@ int conv_fwd(unet *u, int i, int n)
     const long long P = (long long)n * l.H * l.W;
     GemmArgs g;
     memset(&g, 0, sizeof g);
+    g.err = u->err.p;
     if (l.ks == 3 && in.c % 32 == 0) {
         set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
     } else if (l.ks == 3) {
@@ -855,6 +1104,7 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     const In in = layer_input(u, i);
     GemmArgs g;
     memset(&g, 0, sizeof g);
+    g.err = u->err.p;
     if (l.ks == 3 && in.c % 32 == 0) {
         set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
     } else if (l.ks == 3) {
@@ -886,6 +1136,7 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     // input gradient: dX[P][cin] = im2col(gy)[P][ktp] * Wt[cin][ktp]^T
     const GIn gin = layer_ginput(u, i);
     memset(&g, 0, sizeof g);
+    g.err = u->err.p;
     if (l.ks == 3) {
         set_implicit(g, gy, ldg, 0, l.coutp, l.H, l.W);
     } else {
@@ -1053,6 +1304,28 @@ extern "C" int unet_set_params(unet *u, const float *w)
     return RTM_OK;
 }
 
+namespace {
+// status 4 when a tensor-core GEMM's bounded wait ran out during the call
+int check_gemm_waits(unet *u)
+{
+    int e = 0;
+    RTM_CUDA(cudaMemcpy(&e, u->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        RTM_CUDA(cudaMemset(u->err.p, 0, sizeof(int)));
+        rtm_set_error("a tensor-core GEMM's wait did not complete within its time limit");
+        return RTM_ERR_TIMEOUT;
+    }
+    return RTM_OK;
+}
+}  // namespace
+
+extern "C" int unet_set_gemm(int tensor_core)
+{
+    RTM_CHECK_ARG(tensor_core == 0 || tensor_core == 1, "tensor_core must be 0 or 1");
+    g_gemm_tc = tensor_core;
+    return RTM_OK;
+}
+
 extern "C" int unet_forward(unet *u, const float *x, int n, float *y, int on_device)
 {
     RTM_CHECK_ARG(u && x && y, "null argument");
@@ -1067,7 +1340,7 @@ extern "C" int unet_forward(unet *u, const float *x, int n, float *y, int on_dev
     if (!on_device)
         RTM_CUDA(cudaMemcpyAsync(y, u->tgt.p, P * u->cout * sizeof(float), cudaMemcpyDeviceToHost, u->st));
     RTM_CUDA(cudaStreamSynchronize(u->st));
-    return RTM_OK;
+    return check_gemm_waits(u);
 }
 
 extern "C" int unet_loss_grad(unet *u, const float *x, const float *t, int n, int on_device, double *loss, float *grad)
@@ -1080,7 +1353,7 @@ extern "C" int unet_loss_grad(unet *u, const float *x, const float *t, int n, in
     TRY(backward(u, n));
     if (grad) RTM_CUDA(cudaMemcpyAsync(grad, u->gw.p, u->nparam * sizeof(float), cudaMemcpyDeviceToHost, u->st));
     RTM_CUDA(cudaStreamSynchronize(u->st));
-    return RTM_OK;
+    return check_gemm_waits(u);
 }
 
 extern "C" int unet_train_step(unet *u, const float *x, const float *t, int n, int on_device, float lr, float beta1,
@@ -1102,5 +1375,5 @@ extern "C" int unet_train_step(unet *u, const float *x, const float *t, int n, i
     RTM_CUDA(cudaGetLastError());
     TRY(refresh_weights(u));
     RTM_CUDA(cudaStreamSynchronize(u->st));
-    return RTM_OK;
+    return check_gemm_waits(u);
 }

@@ -7,6 +7,12 @@ import numpy as np
 from ._lib import check, load, ptr
 
 
+def set_gemm(tensor_core=True):
+    """GEMM kernel of the forward and backward-data passes: tcgen05 tensor-core
+    MMAs with tensor-memory accumulators (default) or mma.sync."""
+    check(load().unet_set_gemm(1 if tensor_core else 0))
+
+
 class UNet:
     """unet_create/unet_* of the C-ABI.  Images are float32 NHWC
     (n, H, W, 3); parameters one flat float32 vector."""

@@ -251,13 +251,18 @@ int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float d2, float 
  * The tile width applies to the cp.async-pipelined kernel; the slice-ring
  * kernel uses 16 columns. */
 int acoustic3d_set(int tile_x, int ychunks);
-/* Step kernel where n1 % 4 == 0: 1 (default) the slice-ring kernel, whose
- * p1 slices arrive by bulk tensor copies into a 13-slice shared-memory ring;
- * 0 the cp.async-pipelined kernel with a register queue of y taps.  Both are
- * bit-identical in exact arithmetic.  A ring kernel whose slice load does
+/* Step kernel where n1 % 4 == 0 (other n1 run a scalar kernel):
+ *   0 (default) slab kernel: each slice's x/z slab arrives by a bulk tensor
+ *     copy two slices ahead, the y taps from a register queue, paired FP32
+ *     instructions;
+ *   1 slice-ring kernel: every tap from a 13-slice shared-memory ring filled
+ *     by bulk tensor copies;
+ *   2 cp.async-pipelined kernel with a shifted register queue;
+ *   3 the slab kernel with scalar instructions.
+ * All are bit-identical in exact arithmetic.  A kernel whose slice load does
  * not land within about a second stops; the entry point then returns
  * RTM_ERR_TIMEOUT (4). */
-int acoustic3d_set_kernel(int ring);
+int acoustic3d_set_kernel(int kind);
 
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
@@ -389,6 +394,12 @@ int unet_loss_grad(unet *u, const float *x, const float *t, int n, int on_device
 /* one Adam step (bias-corrected) on the batch; loss before the update */
 int unet_train_step(unet *u, const float *x, const float *t, int n, int on_device, float lr, float beta1, float beta2,
                     float eps, double *loss);
+/* GEMM path of the forward and backward-data passes: 1 (default) the
+ * tcgen05 tensor-core kernel (MMAs with tensor-memory accumulators), 0 the
+ * mma.sync kernel.  The backward-weights pass always runs mma.sync.  A
+ * tensor-core GEMM whose bounded wait runs out makes the call return
+ * RTM_ERR_TIMEOUT (4). */
+int unet_set_gemm(int tensor_core);
 
 #ifdef __cplusplus
 }

@@ -25,12 +25,12 @@ def setup(n1=40, n2=36, n3=34, nt=30, seed=0):
     return vel.astype(np.float32), w
 
 
-@pytest.fixture(autouse=True, params=["ring", "pipelined"])
+@pytest.fixture(autouse=True, params=["slab", "slab-unpaired", "ring", "pipelined"])
 def kernel(request):
-    """Every test runs with both step kernels (they differ where n1 % 4 == 0)."""
-    A.set_kernel(request.param == "ring")
+    """Every test runs with every step kernel (they differ where n1 % 4 == 0)."""
+    A.set_kernel(request.param)
     yield request.param
-    A.set_kernel(True)
+    A.set_kernel("slab")
 
 
 @pytest.fixture(params=["exact", "fast"])

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import unet_oracle as U
-from elastic_gb300.unet import UNet
+from elastic_gb300.unet import UNet, set_gemm
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +34,32 @@ def setup(H=32, W=32, n=2, seed=3):
     x = U.bf16_round(rng.standard_normal((n, H, W, 3))).astype(np.float32)
     t = rng.standard_normal((n, H, W, 3)).astype(np.float32)
     return net, table, p, x, t
+
+
+@pytest.fixture(autouse=True, params=["tcgen05", "mma_sync"])
+def gemm_path(request):
+    """Every test runs with both GEMM kernels of the forward and
+    backward-data passes."""
+    set_gemm(request.param == "tcgen05")
+    yield request.param
+    set_gemm(True)
+
+
+def test_tcgen05_and_mma_sync_paths_agree():
+    """The two GEMM kernels accumulate the same BF16 products in FP32 in
+    different orders: network outputs and gradients agree closely (the BF16
+    rounding of activations can flip on either side of a tie)."""
+    net, table, p, x, t = setup(H=64, W=64, n=2, seed=5)
+    set_gemm(True)
+    y_tc = net.forward(x)
+    _, g_tc = net.loss_grad(x, t)
+    set_gemm(False)
+    y_ms = net.forward(x)
+    _, g_ms = net.loss_grad(x, t)
+    e_y, e_g = rel(y_tc, y_ms), rel(g_tc, g_ms)
+    print("tcgen05 vs mma.sync: output rel. L2 %.2e, gradient %.2e" % (e_y, e_g))
+    assert np.abs(y_tc).max() > 0
+    assert e_y < 5e-3 and e_g < 2e-2
 
 
 def test_unet_forward_matches_oracle():
