@@ -71,13 +71,16 @@ def dist_env():
     return rank, world, local
 
 
-def measured_peaks():
+def measured_peaks(key="hbm_gbs"):
+    """Roofline denominator: the measured copy bandwidth (GB/s) or
+    BF16 GEMM rate (TFLOP/s), else the recorded fallback."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        if key in d:
+            return float(d[key]), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}[key], "fallback"
 
 
 def profile_traffic():
@@ -696,7 +699,7 @@ def precond_block(args, steps, warmup, pairs=None, train_steps=None, ntest=None,
     import torch
     from elastic_gb300 import precond as PC
     from elastic_gb300 import unet as UN
-    UN.set_gemm(args.gemm == "tc")
+    UN.set_gemm({"tma": "tcgen05_tma", "tc": "tcgen05", "mma": "mma_sync"}[args.gemm])
     c = dict(CFG3)
     if pairs:
         c["pairs"] = pairs
@@ -791,15 +794,58 @@ def precond_block(args, steps, warmup, pairs=None, train_steps=None, ntest=None,
             "gpu_launches": None,
             "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "unit": "TFLOP/s",
                          "frac": round(tflops / peak, 4), "peak_kind": kind + " bf16 (cuBLAS burst)",
-                         "kernel": ("k_gemm_tc (tcgen05, forward and backward-data) + k_gemm (mma.sync, "
-                                    "backward-weights)" if args.gemm == "tc" else "k_gemm (mma.sync m16n8k16 BF16)")
+                         "kernel": {"tma": "k_conv_tc (tcgen05, bulk-copied convolution taps) + k_gemm_tc + k_gemm "
+                                           "(mma.sync, backward-weights)",
+                                    "tc": "k_gemm_tc (tcgen05, forward and backward-data) + k_gemm (mma.sync, "
+                                          "backward-weights)",
+                                    "mma": "k_gemm (mma.sync m16n8k16 BF16)"}[args.gemm]
                                    + " over the whole training step", "traffic": None},
             "clocks": clocks}
     return line
 
 
 def run_precond(args):
-    print(json.dumps(precond_block(args, args.steps, args.warmup, pairs=args.pairs, nt=args.nt)), flush=True)
+    print(json.dumps(precond_block(args, args.steps, args.warmup, pairs=args.pairs, train_steps=args.train_steps,
+                                   nt=args.nt)), flush=True)
+
+
+def run_unet(args):
+    """U-Net training step alone (the network of the precond workload: 256 x
+    256 patches, batch 32, Adam) on seeded synthetic input/target patches
+    resident in HBM: the kernel-level rate and roofline of the learned
+    preconditioner's training, without pair generation."""
+    import torch
+    from elastic_gb300 import unet as UN
+    UN.set_gemm({"tma": "tcgen05_tma", "tc": "tcgen05", "mma": "mma_sync"}[args.gemm])
+    c = dict(CFG3)
+    net = UN.UNet(c["nx"], c["nz"], c["batch"], seed=0)
+    g = torch.Generator(device="cuda").manual_seed(c["seed"])
+    nb = 8  # distinct batches cycled through (64 MB of inputs, larger than L2 with the activations)
+    x = torch.randn((nb, c["batch"], c["nx"], c["nz"], 3), device="cuda", generator=g)
+    y = 0.1 * torch.randn((nb, c["batch"], c["nx"], c["nz"], 3), device="cuda", generator=g)
+    for i in range(args.warmup):
+        net.train_step(x[i % nb], y[i % nb], lr=c["lr"])
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        for i in range(args.steps):
+            net.train_step(x[i % nb], y[i % nb], lr=c["lr"])
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    flops = unet_train_flops(net.layer_table(), c["batch"])
+    peak, kind = measured_peaks("bf16_tflops")
+    tf = flops / (ms * 1e-3) / 1e12
+    print(json.dumps({"metric": "training images/s (learned preconditioner U-Net)", "value": round(c["batch"] / ms * 1e3, 2),
+                      "unit": "images/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                      "dtype": "bf16", "data": "synthetic",
+                      "config": {"workload": f"U-Net training step, {c['nx']}x{c['nz']} patches, batch {c['batch']}, "
+                                             f"Adam; seeded random inputs and targets", "gemm": args.gemm},
+                      "roofline": {"bound": "tensor", "achieved": round(tf, 2), "peak": peak, "unit": "TFLOP/s",
+                                   "frac": round(tf / peak, 4), "peak_kind": kind, "traffic": None},
+                      "clocks": clk.summary()}), flush=True)
 
 
 # --------------------------------------------------------------- config 5 sample
@@ -894,14 +940,16 @@ def main():
     ap.add_argument("--group", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--tune-steps", type=int, default=20)
-    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond"])
+    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond", "unet"])
     ap.add_argument("--pairs", type=int, default=None, help="training pairs of the precond workload")
+    ap.add_argument("--train-steps", type=int, default=None, help="Adam steps of the precond workload")
     ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
     ap.add_argument("--kernel3d", default="pipelined", choices=list(K3D_NAMES), help="3D step kernel")
-    ap.add_argument("--gemm", default="tc", choices=["tc", "mma"],
-                    help="U-Net GEMMs of the forward and backward-data passes: tcgen05 or mma.sync")
+    ap.add_argument("--gemm", default="tma", choices=["tma", "tc", "mma"],
+                    help="U-Net GEMMs of the forward and backward-data passes: tcgen05 with bulk-copied "
+                         "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workload blocks")
@@ -921,6 +969,8 @@ def main():
         run_reference(args)
     elif args.workload == "acoustic3d":
         run_acoustic3d(args)
+    elif args.workload == "unet":
+        run_unet(args)
     elif args.workload == "precond":
         run_precond(args)
     elif args.workload == "rtm2d":

@@ -86,6 +86,7 @@ SIGNATURES = {
     "rtm_debug_umma_desc": (_c_int, [_c_int, _c_int, _c_int, _c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                      ctypes.c_uint, _P]),
     "rtm_debug_umma_probe": (_c_int, [_c_int, ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),
+    "rtm_debug_umma_probe_sw": (_c_int, [_c_int, _c_int, _P, _P, _P]),
 }
 
 _lib = None

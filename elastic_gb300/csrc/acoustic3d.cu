@@ -562,9 +562,11 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
 //   any; only the threads holding the source or the receiver row branch
 //   off, for a few instructions;
 // - the arithmetic runs on pairs of cells (cells 0-1 and 2-3 of a thread),
-//   with the paired single-precision instructions when PK is set; every
-//   operation is rounded separately as in the scalar form (fused
-//   multiply-adds in fast mode), so PK changes no bit of the result.
+//   with the paired single-precision instructions when PK is set, in the
+//   scalar form's order and roundings (fused multiply-adds in fast mode).
+//   Measured: the paired instructions round some subnormal results
+//   differently from the scalar ones, which the wavefield's leading edge
+//   reaches, so exact arithmetic always runs the scalar form (PK = false).
 constexpr int S3_NS = 3;                 // slab slots
 constexpr int S3_Q = 12;                 // register queue depth = unroll of the march
 constexpr size_t S3_SMEM = (size_t)S3_NS * T3_SLICE * sizeof(float) + 128 + S3_NS * 8;
@@ -839,8 +841,9 @@ int launch_ac_tma(const Ac3DArgs &a0, int ychunks, cudaStream_t st)
     case 1: return launch_tma3d(img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>, v, T3_SMEM, a0, ychunks, st);
     case 3: return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, false> : k_acoustic3d_s<EXACT, false, false>, v + 2,
                                 S3_SMEM, a0, ychunks, st);
-    default: return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, true> : k_acoustic3d_s<EXACT, false, true>, v + 3,
-                                 S3_SMEM, a0, ychunks, st);
+    default:  // paired instructions in fast arithmetic only
+        return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, !EXACT> : k_acoustic3d_s<EXACT, false, !EXACT>, v + 3,
+                            S3_SMEM, a0, ychunks, st);
     }
 }
 

@@ -84,6 +84,34 @@ int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long col
     return RTM_OK;
 }
 
+int make_map_nd(CUtensorMap *m, const void *base, bool bf16, int rank, const long long *dims, const long long *strides_b,
+                const int *box, int swizzle)
+{
+    EncodeTiledFn_ fn = encode_fn_impl();
+    RTM_CHECK_ARG(fn, "cuTensorMapEncodeTiled is not available from the driver");
+    RTM_CHECK_ARG(rank >= 1 && rank <= 5, "tensor map rank %d", rank);
+    cuuint64_t d[5], st[4];
+    cuuint32_t bx[5], el[5];
+    for (int i = 0; i < rank; i++) {
+        d[i] = (cuuint64_t)dims[i];
+        bx[i] = (cuuint32_t)box[i];
+        el[i] = 1;
+        if (i + 1 < rank) st[i] = (cuuint64_t)strides_b[i];
+    }
+    const CUtensorMapSwizzle sw = swizzle == 128 ? CU_TENSOR_MAP_SWIZZLE_128B
+                                  : swizzle == 64 ? CU_TENSOR_MAP_SWIZZLE_64B
+                                  : swizzle == 32 ? CU_TENSOR_MAP_SWIZZLE_32B
+                                                  : CU_TENSOR_MAP_SWIZZLE_NONE;
+    const CUresult r = fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank,
+                          const_cast<void *>(base), d, st, bx, el, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        rtm_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return RTM_ERR_CUDA;
+    }
+    return RTM_OK;
+}
+
 }  // namespace eg
 
 static char g_pending_at[128] = "";

@@ -32,6 +32,12 @@ int device_sm_count();
 bool tensor_maps_available();
 int make_map(CUtensorMap *m, const void *base, bool half, int ldz, long long cols, long long planes,
              long long plane_elems, int box_rows, int box_cols);
+// Tensor map of rank 1..5 over BF16 (bf16) or FP32 elements: dims[i]
+// elements along dimension i (0 innermost, unit stride), strides_b[i] bytes
+// between elements of dimension i + 1, a box of box[i] elements, swizzle of
+// 0, 32, 64 or 128 bytes, zero fill outside the tensor.
+int make_map_nd(CUtensorMap *m, const void *base, bool bf16, int rank, const long long *dims, const long long *strides_b,
+                const int *box, int swizzle);
 
 // Owning device allocation that grows on demand.
 template <typename T>

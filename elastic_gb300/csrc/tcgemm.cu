@@ -74,7 +74,109 @@ __global__ void __launch_bounds__(128) k_umma_probe(const __nv_bfloat16 *A, cons
     }
 }
 
+// Swizzled K-major operands, as bulk tensor copies with a 128-byte (64-byte)
+// swizzle leave them: rows of 128 (64) bytes, 8-row atoms of 1024 (512)
+// bytes, the 16-byte chunk c of row r stored at chunk c ^ (r % 8) (c ^ (r % 8
+// / 2)).  The probe places A (128 x K) and B (N x K) that way, K = 64 (32),
+// and accumulates K / 16 MMAs whose descriptors advance by 32 bytes along K
+// inside the atom -- the form the convolution kernels issue.  Both arrays
+// are whole atoms on a 1024-byte boundary, so every address a descriptor
+// can form lies inside them.
+__device__ __forceinline__ uint32_t swz_off(int r, int k, int row_bytes)
+{
+    const int rr = r & 7, byte = 2 * k, chunk = byte >> 4;
+    const int phys = row_bytes == 128 ? (chunk ^ rr) : (chunk ^ (rr >> 1));
+    return (uint32_t)((r >> 3) * 8 * row_bytes + rr * row_bytes + phys * 16 + (byte & 15));
+}
+
+__global__ void __launch_bounds__(128) k_umma_probe_sw(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D, int N,
+                                                        int K, int *status)
+{
+    extern __shared__ __align__(16) unsigned char pr_raw[];
+    unsigned char *base = pr_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(pr_raw) & 1023u)) & 1023u);
+    unsigned char *sA = base, *sB = base + 128 * 128;  // A: up to 16 KB
+    unsigned long long *bar = reinterpret_cast<unsigned long long *>(sB + 256 * 128);
+    uint32_t *tbase = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rb = 2 * K;  // row bytes: 128 (K = 64) or 64 (K = 32)
+    const uint32_t ncols = N <= 32 ? 32u : N <= 64 ? 64u : N <= 128 ? 128u : 256u;
+    for (int i = tid; i < 128 * K; i += 128)
+        *reinterpret_cast<__nv_bfloat16 *>(sA + swz_off(i / K, i % K, rb)) = A[i];
+    for (int i = tid; i < N * K; i += 128)
+        *reinterpret_cast<__nv_bfloat16 *>(sB + swz_off(i / K, i % K, rb)) = B[i];
+    if (warp == 0) tmem_alloc(tbase, ncols);
+    if (tid == 0) {
+        mbar_init(bar);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t d = *tbase;
+    if (tid == 0) {
+        const uint32_t sw = rb == 128 ? 2u : 4u, sbo = 8u * rb;
+        for (int k = 0; k < K / 16; k++) {
+            const uint64_t ad = umma_sdesc(smem_u32(sA) + 32 * k, 16, sbo, sw);
+            const uint64_t bd = umma_sdesc(smem_u32(sB) + 32 * k, 16, sbo, sw);
+            umma_f16(d, ad, bd, umma_idesc_f16(128, N, true, true), k > 0);
+        }
+        umma_commit(bar);
+    }
+    bool ok = mbar_wait(bar, 0);
+    if (!ok) ok = mbar_wait(bar, 0);
+    tc_fence_after();
+    if (ok) {
+        for (int c = 0; c < N; c += 16) {
+            float v[16];
+            tmem_ld16(d + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+            for (int j = 0; j < 16; j++) D[(32 * warp + lane) * N + c + j] = v[j];
+        }
+    } else if (tid == 0) {
+        *status = 1;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tmem_dealloc(d, ncols);
+        tmem_relinquish();
+    }
+}
+constexpr size_t PROBE_SW_SMEM = 1024 + 128 * 128 + 256 * 128 + 16;
+
 }  // namespace
+
+extern "C" int rtm_debug_umma_probe_sw(int N, int K, const unsigned short *A, const unsigned short *B, float *D)
+{
+    RTM_CHECK_ARG(N >= 16 && N <= 256 && N % 16 == 0, "N must be a multiple of 16 in 16 .. 256");
+    RTM_CHECK_ARG(K == 32 || K == 64, "K must be 32 (64-byte swizzle) or 64 (128-byte swizzle)");
+    RTM_CHECK_ARG(A && B && D, "null argument");
+    TRY(ensure_device());
+    DevBuf<__nv_bfloat16> a, b;
+    DevBuf<float> d;
+    DevBuf<int> st;
+    TRY(a.alloc((size_t)128 * K));
+    TRY(b.alloc((size_t)N * K));
+    TRY(d.alloc((size_t)128 * N));
+    TRY(st.alloc(1));
+    RTM_CUDA(cudaMemcpy(a.p, A, (size_t)128 * K * 2, cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemcpy(b.p, B, (size_t)N * K * 2, cudaMemcpyHostToDevice));
+    RTM_CUDA(cudaMemset(d.p, 0, (size_t)128 * N * 4));
+    RTM_CUDA(cudaMemset(st.p, 0, 4));
+    RTM_CUDA(cudaFuncSetAttribute(k_umma_probe_sw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PROBE_SW_SMEM));
+    k_umma_probe_sw<<<1, 128, PROBE_SW_SMEM>>>(a.p, b.p, d.p, N, K, st.p);
+    RTM_CUDA(cudaGetLastError());
+    RTM_CUDA(cudaDeviceSynchronize());
+    int s = 0;
+    RTM_CUDA(cudaMemcpy(&s, st.p, 4, cudaMemcpyDeviceToHost));
+    RTM_CUDA(cudaMemcpy(D, d.p, (size_t)128 * N * 4, cudaMemcpyDeviceToHost));
+    if (s) {
+        rtm_set_error("the probe's MMA did not complete within its time limit");
+        return RTM_ERR_TIMEOUT;
+    }
+    return RTM_OK;
+}
 
 extern "C" int rtm_debug_umma_desc(int M, int N, int bf16, int f32, unsigned addr, unsigned lbo, unsigned sbo,
                                    unsigned swizzle, unsigned long long *out)

@@ -40,9 +40,14 @@ namespace {
 using bf16 = __nv_bfloat16;
 using eg::DevBuf;
 using eg::fence_async_smem;
+using eg::make_map_nd;
+using eg::mbar_expect_tx;
 using eg::mbar_init;
 using eg::mbar_wait;
 using eg::smem_u32;
+using eg::tensor_maps_available;
+using eg::tma_load_2d;
+using eg::tma_load_4d;
 using eg::tc_fence_after;
 using eg::tc_fence_before;
 using eg::tmem_alloc;
@@ -315,6 +320,53 @@ struct TcCfg {
     static_assert(STAGES >= 4, "stages");
 };
 
+// Epilogue of a 128 x BN tensor-memory accumulator: warp w reads rows
+// 32 w .. 32 w + 31 (output pixels m0 + row), adds the bias, applies the
+// leaky ReLU (BF16 output) and stores BF16 or FP32.
+template <int BN, int EPI>
+__device__ __forceinline__ void tc_epilogue(const GemmArgs &g, uint32_t tmem, int m0, int warp, int lane)
+{
+    const int m = m0 + 32 * warp + lane;
+#pragma unroll
+    for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+        if (m >= g.M) continue;
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+            const int n = c + j;
+            if (n < g.N && g.bias) v[j] += g.bias[n];
+            if (EPI == EPI_BF16 && g.relu) v[j] = v[j] > 0.f ? v[j] : LEAK * v[j];
+        }
+        if (EPI == EPI_F32) {
+            float *dst = g.Cf + (long long)m * g.ldc + c;
+            if (c + 16 <= g.N && (g.ldc & 3) == 0) {
+#pragma unroll
+                for (int j = 0; j < 16; j += 4)
+                    *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c + j < g.N) dst[j] = v[j];
+            }
+        } else {
+            bf16 *dst = g.Cb + (long long)m * g.ldc + g.coff + c;
+            if (c + 16 <= g.N && ((g.ldc | g.coff) & 7) == 0) {
+                uint4 w[2];
+                __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(w);
+#pragma unroll
+                for (int j = 0; j < 8; j++) h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                reinterpret_cast<uint4 *>(dst)[0] = w[0];
+                reinterpret_cast<uint4 *>(dst)[1] = w[1];
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c + j < g.N) dst[j] = __float2bfloat16_rn(v[j]);
+            }
+        }
+    }
+}
+
 template <int BN, int EPI>
 __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(const __grid_constant__ GemmArgs g)
 {
@@ -428,45 +480,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(const __grid_constant__ 
     if (__syncthreads_or(fail || !ok)) {
         if (tid == 0 && g.err) atomicExch(g.err, 1);
     } else {
-        const int m = m0 + 32 * warp + lane;
-#pragma unroll
-        for (int c = 0; c < BN; c += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
-            if (m >= g.M) continue;
-#pragma unroll
-            for (int j = 0; j < 16; j++) {
-                const int n = c + j;
-                if (n < g.N && g.bias) v[j] += g.bias[n];
-                if (EPI == EPI_BF16 && g.relu) v[j] = v[j] > 0.f ? v[j] : LEAK * v[j];
-            }
-            if (EPI == EPI_F32) {
-                float *dst = g.Cf + (long long)m * g.ldc + c;
-                if (c + 16 <= g.N && (g.ldc & 3) == 0) {
-#pragma unroll
-                    for (int j = 0; j < 16; j += 4)
-                        *reinterpret_cast<float4 *>(dst + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; j++)
-                        if (c + j < g.N) dst[j] = v[j];
-                }
-            } else {
-                bf16 *dst = g.Cb + (long long)m * g.ldc + g.coff + c;
-                if (c + 16 <= g.N && ((g.ldc | g.coff) & 7) == 0) {
-                    uint4 w[2];
-                    __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(w);
-#pragma unroll
-                    for (int j = 0; j < 8; j++) h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                    reinterpret_cast<uint4 *>(dst)[0] = w[0];
-                    reinterpret_cast<uint4 *>(dst)[1] = w[1];
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 16; j++)
-                        if (c + j < g.N) dst[j] = __float2bfloat16_rn(v[j]);
-                }
-            }
-        }
+        tc_epilogue<BN, EPI>(g, tmem, m0, warp, lane);
     }
     tc_fence_before();
     __syncthreads();
@@ -503,7 +517,195 @@ int gemm_tc(const GemmArgs &g, cudaStream_t st)
     return gemm_tc_launch<256, EPI>(g, st);
 }
 
-int g_gemm_tc = 1;  // 1: tensor-core GEMMs for the non-transposed passes; 0: mma.sync only
+// ------------------------------------ 3x3 convolution by bulk tensor copies
+// The implicit-im2col GEMM of a 3x3 (pad 1) convolution of an NHWC tensor
+// X (C channels, C % 32 == 0) for image widths W with W % 128 == 0 or
+// 128 % W == 0: a 128-pixel output tile is a segment of one image row
+// (W >= 128) or 128 / W whole rows, so its A operand for tap (dy, dx) and
+// channel chunk c is ONE box of the activation tensor -- KC channels x the
+// tile's pixels shifted by (dy - 1, dx - 1) -- that a bulk tensor copy
+// fetches with the zero padding supplied by the copy's out-of-range fill.
+// The K loop runs over 9 taps x C / KC chunks (KC = 64 with a 128-byte
+// swizzle, 32 with a 64-byte swizzle); B (the weights, K-major [N][9 C]) is
+// a box of KC x BN.  One thread issues the copies into an S-stage ring (full
+// and empty mbarriers), one thread issues the MMAs (tcgen05.mma, accumulator
+// in tensor memory) and commits each stage back to its empty barrier; the
+// four warps then run the epilogue of k_gemm_tc.  Every wait is bounded and
+// a run-out sets g.err (the tile's output is then not written).
+struct ConvTcArgs {
+    GemmArgs g;
+    CUtensorMap tma;  // X + xoff: {C, W, H, images}, box {KC, min(W,128), 128/min(W,128), 1}
+    CUtensorMap tmb;  // B: {9 C, N}, box {KC, BN}
+    int nk;           // K steps: 9 * C / KC
+    int cchunks;      // C / KC
+};
+
+template <int BN, int KC>
+struct ConvCfg {
+    static constexpr int A_BYTES = TC_BM * KC * 2;
+    static constexpr int B_BYTES = BN * KC * 2;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int STAGES = (96 * 1024 / STAGE) < 4 ? 4 : (96 * 1024 / STAGE) > 8 ? 8 : (96 * 1024 / STAGE);
+    static constexpr uint32_t NCOLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 + 8 * (2 * STAGES + 1) + 16;
+};
+
+template <int BN, int EPI, int KC>
+__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ ConvTcArgs A)
+{
+    using T = ConvCfg<BN, KC>;
+    constexpr int S = T::STAGES;
+    const GemmArgs &g = A.g;
+    extern __shared__ __align__(16) unsigned char cv_raw[];
+    unsigned char *base = cv_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(cv_raw) & 1023u)) & 1023u);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(base + S * T::STAGE);
+    unsigned long long *empty = full + S, *done = empty + S;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    int *fail = reinterpret_cast<int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_BM;
+    // tile origin: image, first row, first column
+    const int HW = g.H * g.W;
+    const int img = m0 / HW, rem = m0 - img * HW, y0 = rem / g.W, x0 = rem - y0 * g.W;
+    if (warp == 0) {
+        tmem_alloc(tslot, T::NCOLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < S; i++) {
+            mbar_init(&full[i]);
+            mbar_init(&empty[i]);
+        }
+        mbar_init(done);
+        *fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int nk = A.nk;
+    if (tid == 0) {
+        // producer: K step i into stage i % S once the MMAs of step i - S
+        // have released it
+        for (int i = 0; i < nk; i++) {
+            const int st = i % S;
+            if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i - S) / S) & 1))) {
+                atomicExch(fail, 1);
+                break;
+            }
+            if (*reinterpret_cast<volatile int *>(fail)) break;
+            const int tap = i / A.cchunks, cc = i - tap * A.cchunks, dy = tap / 3, dx = tap - 3 * dy;
+            unsigned char *sa = base + st * T::STAGE;
+            mbar_expect_tx(&full[st], (unsigned)T::STAGE);
+            tma_load_4d(sa, &A.tma, cc * KC, x0 + dx - 1, y0 + dy - 1, img, &full[st]);
+            tma_load_2d(sa + T::A_BYTES, &A.tmb, tap * g.C + cc * KC, 0, &full[st]);
+        }
+    } else if (tid == 32) {
+        // MMA issue: KC / 16 MMAs per step, the descriptors advancing 32
+        // bytes along K inside the swizzle atom
+        constexpr uint32_t IDESC = umma_idesc_f16(TC_BM, BN, true, true);
+        constexpr uint32_t SW = KC == 64 ? 2u : 4u, SBO = 8u * KC * 2u;
+        for (int i = 0; i < nk; i++) {
+            const int st = i % S;
+            if (!mbar_wait(&full[st], (unsigned)((i / S) & 1))) {
+                atomicExch(fail, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(base + st * T::STAGE), b_addr = a_addr + T::A_BYTES;
+#pragma unroll
+            for (int k = 0; k < KC / 16; k++)
+                umma_f16(tmem, umma_sdesc(a_addr + 32 * k, 16, SBO, SW), umma_sdesc(b_addr + 32 * k, 16, SBO, SW), IDESC,
+                         i > 0 || k > 0);
+            umma_commit(&empty[st]);
+        }
+        umma_commit(done);  // also after a failure: tracks every MMA issued
+    }
+    bool ok = mbar_wait(done, 0);
+    if (!ok) ok = mbar_wait(done, 0);  // the MMAs may still be running: a second limit
+    tc_fence_after();
+    if (__syncthreads_or(!ok || *reinterpret_cast<volatile int *>(fail))) {
+        if (tid == 0) {
+            if (g.err) atomicExch(g.err, 1);
+            // let copies that were issued but never consumed land (bounded)
+            for (int i = 0; i < nk && i < S; i++) mbar_wait(&full[(nk - 1 - i) % S], (unsigned)(((nk - 1 - i) / S) & 1));
+        }
+    } else {
+        tc_epilogue<BN, EPI>(g, tmem, m0, warp, lane);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, T::NCOLS);
+}
+
+// Tensor maps and launch of k_conv_tc; RTM_ERR_ARG when the geometry does
+// not fit (the caller then uses k_gemm_tc).
+template <int BN, int EPI, int KC>
+int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
+{
+    using T = ConvCfg<BN, KC>;
+    ConvTcArgs a;
+    memset(&a, 0, sizeof a);
+    a.g = g;
+    a.cchunks = g.C / KC;
+    a.nk = 9 * a.cchunks;
+    const int bw = g.W < 128 ? g.W : 128, bh = 128 / bw;
+    const long long imgs = (long long)g.M / ((long long)g.H * g.W);
+    {
+        const long long dims[4] = {g.C, g.W, g.H, imgs};
+        const long long strides[3] = {2LL * g.ldx, 2LL * g.ldx * g.W, 2LL * g.ldx * g.W * g.H};
+        const int box[4] = {KC, bw, bh, 1};
+        TRY(make_map_nd(&a.tma, g.X + g.xoff, true, 4, dims, strides, box, 2 * KC));
+    }
+    {
+        const long long dims[2] = {9LL * g.C, g.N};
+        const long long strides[1] = {2LL * g.ldb};
+        const int box[2] = {KC, BN};
+        TRY(make_map_nd(&a.tmb, g.B, true, 2, dims, strides, box, 2 * KC));
+    }
+    auto kern = k_conv_tc<BN, EPI, KC>;
+    static bool attr[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::SMEM));
+            attr[dev] = true;
+        }
+    }
+    kern<<<g.M / TC_BM, TC_THREADS, T::SMEM, st>>>(a);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+template <int EPI, int KC>
+int conv_tc_kc(const GemmArgs &g, cudaStream_t st)
+{
+    if (g.N <= 32) return conv_tc_launch<32, EPI, KC>(g, st);
+    if (g.N <= 64) return conv_tc_launch<64, EPI, KC>(g, st);
+    if (g.N <= 96) return conv_tc_launch<96, EPI, KC>(g, st);
+    if (g.N <= 128) return conv_tc_launch<128, EPI, KC>(g, st);
+    return conv_tc_launch<256, EPI, KC>(g, st);
+}
+
+// True when k_conv_tc covers this GEMM.
+bool conv_tc_fits(const GemmArgs &g)
+{
+    if (!g.conv || g.C % 32 || g.N > 256 || g.K != 9 * g.C || g.M % TC_BM) return false;
+    if (!(g.W % 128 == 0 || 128 % g.W == 0) || ((long long)g.H * g.W) % TC_BM) return false;
+    if (((uintptr_t)(g.X + g.xoff) & 15) || ((uintptr_t)g.B & 15) || g.ldx % 8 || g.ldb % 8) return false;
+    return tensor_maps_available();
+}
+
+template <int EPI>
+int conv_tc(const GemmArgs &g, cudaStream_t st)
+{
+    return g.C % 64 == 0 ? conv_tc_kc<EPI, 64>(g, st) : conv_tc_kc<EPI, 32>(g, st);
+}
+
+int g_gemm_tc = 2;  // 2: 3x3 convolutions by bulk-copied tap boxes, other non-transposed GEMMs on k_gemm_tc;
+                    // 1: k_gemm_tc for every non-transposed pass; 0: mma.sync only
 
 template <bool A_T, bool B_T, int BN, int WM, int EPI>
 int gemm_launch(const GemmArgs &g, int splits, cudaStream_t st)
@@ -549,6 +751,10 @@ int gemm(const GemmArgs &g, bool a_t, bool b_t, int epi, int splits, cudaStream_
                   "implicit im2col needs C %% 32 == 0 and 16-byte aligned channel runs");
     const bool tc = g_gemm_tc && !a_t && !b_t && splits == 1 && g.kchunk >= g.K && g.N <= 256 &&
                     (g.conv || (g.lda % 8 == 0 && g.A)) && g.ldb % 8 == 0;
+    if (tc && g_gemm_tc == 2 && conv_tc_fits(g)) {
+        if (epi == EPI_BF16) return conv_tc<EPI_BF16>(g, st);
+        if (epi == EPI_F32) return conv_tc<EPI_F32>(g, st);
+    }
     if (tc && epi == EPI_BF16) return gemm_tc<EPI_BF16>(g, st);
     if (tc && epi == EPI_F32) return gemm_tc<EPI_F32>(g, st);
     if (epi == EPI_BF16 && !a_t && !b_t) return gemm_bn<false, false, EPI_BF16>(g, splits, st);
@@ -1321,7 +1527,7 @@ int check_gemm_waits(unet *u)
 
 extern "C" int unet_set_gemm(int tensor_core)
 {
-    RTM_CHECK_ARG(tensor_core == 0 || tensor_core == 1, "tensor_core must be 0 or 1");
+    RTM_CHECK_ARG(tensor_core >= 0 && tensor_core <= 2, "tensor_core must be 0, 1 or 2");
     g_gemm_tc = tensor_core;
     return RTM_OK;
 }

@@ -7,10 +7,15 @@ import numpy as np
 from ._lib import check, load, ptr
 
 
-def set_gemm(tensor_core=True):
-    """GEMM kernel of the forward and backward-data passes: tcgen05 tensor-core
-    MMAs with tensor-memory accumulators (default) or mma.sync."""
-    check(load().unet_set_gemm(1 if tensor_core else 0))
+GEMMS = {"mma_sync": 0, "tcgen05": 1, "tcgen05_tma": 2}
+
+
+def set_gemm(kind="tcgen05_tma"):
+    """GEMM kernel of the forward and backward-data passes: "tcgen05_tma"
+    (default: tcgen05 MMAs, 3x3 convolutions fed by bulk tensor copies of
+    shifted activation boxes), "tcgen05" (operands gathered by threads) or
+    "mma_sync"."""
+    check(load().unet_set_gemm(GEMMS[kind]))
 
 
 class UNet:

@@ -366,6 +366,11 @@ int rtm_debug_umma_desc(int M, int N, int bf16, int f32, unsigned addr, unsigned
                         unsigned long long *out);
 int rtm_debug_umma_probe(int N, unsigned lbo, unsigned sbo, const unsigned short *A, const unsigned short *B,
                          float *D);
+/* rtm_debug_umma_probe_sw: A (128 x K) and B (N x K), K = 64 or 32, placed
+ * in shared memory in the 128-byte (K = 64) or 64-byte (K = 32) swizzled
+ * K-major layout that bulk tensor copies produce, multiplied by K/16 MMAs
+ * whose descriptors advance 32 bytes along K: D = A B^T (128 x N, FP32). */
+int rtm_debug_umma_probe_sw(int N, int K, const unsigned short *A, const unsigned short *B, float *D);
 
 /* ------------------------------------------ learned image preconditioner
  * (no counterpart in the reference).  A 4-level 3->3 channel U-Net
@@ -394,11 +399,13 @@ int unet_loss_grad(unet *u, const float *x, const float *t, int n, int on_device
 /* one Adam step (bias-corrected) on the batch; loss before the update */
 int unet_train_step(unet *u, const float *x, const float *t, int n, int on_device, float lr, float beta1, float beta2,
                     float eps, double *loss);
-/* GEMM path of the forward and backward-data passes: 1 (default) the
- * tcgen05 tensor-core kernel (MMAs with tensor-memory accumulators), 0 the
- * mma.sync kernel.  The backward-weights pass always runs mma.sync.  A
- * tensor-core GEMM whose bounded wait runs out makes the call return
- * RTM_ERR_TIMEOUT (4). */
+/* GEMM path of the forward and backward-data passes: 2 (default) tcgen05
+ * MMAs with tensor-memory accumulators, the 3x3 convolutions fed by bulk
+ * tensor copies of shifted activation boxes (zero padding from the copies'
+ * out-of-range fill), other GEMMs by the thread-gathered kernel of 1; 1 the
+ * thread-gathered tcgen05 kernel for every such GEMM; 0 the mma.sync
+ * kernel.  The backward-weights pass always runs mma.sync.  A tensor-core
+ * GEMM whose bounded wait runs out makes the call return RTM_ERR_TIMEOUT (4). */
 int unet_set_gemm(int tensor_core);
 
 #ifdef __cplusplus

@@ -44,3 +44,22 @@ def test_umma_probe_matches_host_product(N):
     err_sw = np.linalg.norm(swapped - want) / np.linalg.norm(want)
     print("N=%d: rel. L2 with (LBO=128 along K, SBO=256 along M/N) %.2e, swapped %.2e" % (N, err, err_sw))
     assert err < 1e-6
+
+
+@pytest.mark.parametrize("K", [64, 32])
+@pytest.mark.parametrize("N", [32, 96, 256])
+def test_umma_swizzled_probe_matches_host_product(N, K):
+    """The swizzled K-major layouts of the convolution kernels (128-byte
+    swizzle for 64-channel chunks, 64-byte for 32-channel chunks) with the
+    descriptor advanced 32 bytes per 16-wide K step."""
+    rng = np.random.default_rng(N + K)
+    A = to_bf16_bits(rng.standard_normal((128, K)))
+    B = to_bf16_bits(rng.standard_normal((N, K)))
+    want = from_bf16_bits(A).astype(np.float64) @ from_bf16_bits(B).astype(np.float64).T
+    D = np.zeros((128, N), np.float32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    st = load().rtm_debug_umma_probe_sw(N, K, P(A), P(B), P(D))
+    assert st == 0, load().rtm_last_error()
+    err = np.linalg.norm(D - want) / np.linalg.norm(want)
+    print("N=%d K=%d swizzled: rel. L2 %.2e" % (N, K, err))
+    assert err < 1e-6

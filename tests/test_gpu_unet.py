@@ -36,30 +36,37 @@ def setup(H=32, W=32, n=2, seed=3):
     return net, table, p, x, t
 
 
-@pytest.fixture(autouse=True, params=["tcgen05", "mma_sync"])
+@pytest.fixture(autouse=True, params=["tcgen05_tma", "tcgen05", "mma_sync"])
 def gemm_path(request):
-    """Every test runs with both GEMM kernels of the forward and
+    """Every test runs with each GEMM kernel of the forward and
     backward-data passes."""
-    set_gemm(request.param == "tcgen05")
+    set_gemm(request.param)
     yield request.param
-    set_gemm(True)
+    set_gemm()
 
 
-def test_tcgen05_and_mma_sync_paths_agree():
-    """The two GEMM kernels accumulate the same BF16 products in FP32 in
+@pytest.mark.parametrize("hw", [(64, 64, 2), (256, 256, 1), (128, 256, 1)])
+def test_gemm_paths_agree(hw):
+    """The GEMM kernels accumulate the same BF16 products in FP32 in
     different orders: network outputs and gradients agree closely (the BF16
-    rounding of activations can flip on either side of a tie)."""
-    net, table, p, x, t = setup(H=64, W=64, n=2, seed=5)
-    set_gemm(True)
-    y_tc = net.forward(x)
-    _, g_tc = net.loss_grad(x, t)
-    set_gemm(False)
-    y_ms = net.forward(x)
-    _, g_ms = net.loss_grad(x, t)
-    e_y, e_g = rel(y_tc, y_ms), rel(g_tc, g_ms)
-    print("tcgen05 vs mma.sync: output rel. L2 %.2e, gradient %.2e" % (e_y, e_g))
-    assert np.abs(y_tc).max() > 0
-    assert e_y < 5e-3 and e_g < 2e-2
+    rounding of activations can flip on either side of a tie).  The sizes
+    take the bulk-copy convolution through its whole-row tiles (W <= 128)
+    and its row-segment tiles (W = 256)."""
+    H, W, n = hw
+    net, table, p, x, t = setup(H=H, W=W, n=n, seed=5)
+    out = {}
+    for kind in ("tcgen05_tma", "tcgen05", "mma_sync"):
+        set_gemm(kind)
+        y = net.forward(x)
+        _, g = net.loss_grad(x, t)
+        out[kind] = (y, g)
+    y_ms, g_ms = out["mma_sync"]
+    assert np.abs(y_ms).max() > 0
+    for kind in ("tcgen05_tma", "tcgen05"):
+        e_y, e_g = rel(out[kind][0], y_ms), rel(out[kind][1], g_ms)
+        print("%s vs mma.sync at %dx%d: output rel. L2 %.2e, gradient %.2e" % (kind, H, W, e_y, e_g))
+        assert e_y < 5e-3 and e_g < 2e-2
+    net.close()
 
 
 def test_unet_forward_matches_oracle():
