@@ -583,7 +583,7 @@ CFG4 = dict(n1=512, n2=1024, n3=1024, d=10.0, dt=1e-3, nt=3000, vmin=1500.0, vma
 CFL_LIMIT_3D = 0.4419  # 2 / sqrt(3 * 6.8267): leapfrog limit of the 10th-order 3D Laplacian
 
 
-K3D_NAMES = {"slab": "k_acoustic3d_s", "slab-unpaired": "k_acoustic3d_s", "ring": "k_acoustic3d_t",
+K3D_NAMES = {"slab": "k_acoustic3d_s", "slab-paired": "k_acoustic3d_s", "ring": "k_acoustic3d_t",
              "pipelined": "k_acoustic3d_p"}
 
 
@@ -946,7 +946,7 @@ def main():
     ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
     ap.add_argument("--n3", type=int, default=None, help="override n3 of the 3D workload (profiling only)")
     ap.add_argument("--tile3d", type=int, default=16)
-    ap.add_argument("--kernel3d", default="pipelined", choices=list(K3D_NAMES), help="3D step kernel")
+    ap.add_argument("--kernel3d", default="slab", choices=list(K3D_NAMES), help="3D step kernel")
     ap.add_argument("--gemm", default="tma", choices=["tma", "tc", "mma"],
                     help="U-Net GEMMs of the forward and backward-data passes: tcgen05 with bulk-copied "
                          "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")

@@ -15,15 +15,15 @@ def set_shape(tile_x=16, ychunks=0):
     check(load().acoustic3d_set(tile_x, ychunks))
 
 
-KERNELS = {"slab": 0, "ring": 1, "pipelined": 2, "slab-unpaired": 3}
+KERNELS = {"slab": 0, "ring": 1, "pipelined": 2, "slab-paired": 3}
 
 
 def set_kernel(kind="slab"):
-    """Step kernel for n1 % 4 == 0: "slab" (default: bulk-tensor-copied x/z
-    slab, unrolled register queue, paired FP32 arithmetic), "slab-unpaired"
-    (the same with scalar instructions, identical results), "ring" (every
-    tap from a ring of copied slices) or "pipelined" (cp.async halo, shifted
-    register queue)."""
+    """Step kernel for n1 % 4 == 0: "slab" (default: every operand by bulk
+    tensor copies issued slices ahead, y taps from an unrolled register
+    queue), "slab-paired" (the same with paired FP32 instructions in fast
+    arithmetic), "ring" (every tap from a ring of copied slices) or
+    "pipelined" (cp.async halo, shifted register queue)."""
     check(load().acoustic3d_set_kernel(KERNELS[kind]))
 
 

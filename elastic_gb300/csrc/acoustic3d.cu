@@ -546,30 +546,48 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_t(const __grid_con
     }
 }
 
-// Slab kernel (default for n1 % 4 == 0).  The same tiles and march as
-// k_acoustic3d_p, arranged so that every thread runs the same straight-line
-// code on every slice:
-// - the x and z taps come from a slab of slice y (the tile's 144 rows by
-//   26 columns) that one thread loads by a bulk tensor copy two slices ahead
-//   into one of three slots, completing on an mbarrier (bounded wait);
-// - the y taps come from a register queue of S3_Q float4 (slices y-5 .. y+5
-//   and the load of y+6 in flight); the march is unrolled by S3_Q, so each
-//   slot has a fixed register and nothing is shifted;
+// Slab kernel (kinds 0 and 3).  The same tiles and march as k_acoustic3d_p,
+// arranged so that every operand arrives by a bulk tensor copy issued
+// slices ahead of its use and every thread runs the same straight-line code
+// on every slice:
+// - slab ring: slice s of p1 over the tile's 144 rows by 26 columns (x and z
+//   halo) lands in slot s % S3_NS, issued when the march reaches slice
+//   s - 7; slice y's x and z taps come from its slab;
+// - the y taps come from a register queue of S3_Q float4 (slices y-5 .. y+5)
+//   refilled from the centre of slab y+5 (landed two slices after its
+//   issue); the march is unrolled by S3_Q so that each queue slot is a
+//   fixed register and nothing is shifted;
+// - p0 and v^2 dt^2 of the tile's cells (128 rows x 16 columns) land in a
+//   ring of S3_NP slots, issued three slices ahead;
 // - the sponge factor is a per-slice branch that is uniform across the CTA
-//   (the tile's least edge distance against the slice's): inside the
-//   sponge every cell looks its factor up, a factor of one leaving a value
-//   unchanged; the rim rows are zeroed by a select in the CTAs that hold
-//   any; only the threads holding the source or the receiver row branch
-//   off, for a few instructions;
-// - the arithmetic runs on pairs of cells (cells 0-1 and 2-3 of a thread),
-//   with the paired single-precision instructions when PK is set, in the
-//   scalar form's order and roundings (fused multiply-adds in fast mode).
-//   Measured: the paired instructions round some subnormal results
-//   differently from the scalar ones, which the wavefield's leading edge
-//   reaches, so exact arithmetic always runs the scalar form (PK = false).
-constexpr int S3_NS = 3;                 // slab slots
-constexpr int S3_Q = 12;                 // register queue depth = unroll of the march
-constexpr size_t S3_SMEM = (size_t)S3_NS * T3_SLICE * sizeof(float) + 128 + S3_NS * 8;
+//   (the tile's least edge distance against the slice's): inside the sponge
+//   every cell looks its factor up, a factor of one leaving a value
+//   unchanged; rim rows are zeroed by a select in the CTAs that hold any;
+//   only the threads holding the source or the receiver row branch off;
+// - with PK (kind 3, fast arithmetic only) the cells are updated in pairs
+//   (cells 0-1 and 2-3 of a thread) by the paired single-precision
+//   instructions, in the scalar form's order and roundings.  Measured: the
+//   paired instructions round some subnormal results differently from the
+//   scalar ones, which the wavefield's leading edge reaches, so exact
+//   arithmetic runs the scalar form; and the paired form is no faster (the
+//   kernel is bound by shared-memory latency, not by issue), so the
+//   default is the scalar form.
+// One CTA-wide barrier per slice; it also carries the bounded waits'
+// outcome: a CTA whose copy does not land within about a second records it
+// in the error flag, lets its copies in flight land and stops.
+constexpr int S3_NS = 8;                 // slab slots (power of two)
+constexpr int S3_LEAD = 7;               // slab s is issued at slice s - S3_LEAD
+constexpr int S3_NP = 4;                 // p0 / vel slots (power of two), issued S3_NP - 1 slices ahead
+constexpr int S3_Q = 11;                 // register queue depth = unroll of the march
+constexpr int S3_BOX = A_TZ * T3_TX;     // floats of a p0 or vel box
+constexpr size_t S3_SMEM = ((size_t)S3_NS * T3_SLICE + 2 * S3_NP * S3_BOX) * sizeof(float) + 128 + (S3_NS + S3_NP) * 8;
+
+struct Ac3DSArgs {
+    Ac3DArgs a;
+    CUtensorMap tm;   // p1: box {A_LZ, T3_LX, 1}
+    CUtensorMap tm0;  // p0: box {A_TZ, T3_TX, 1}
+    CUtensorMap tmv;  // vel: box {A_TZ, T3_TX, 1}
+};
 
 template <bool PK>
 __device__ __forceinline__ float2 add2(float2 a, float2 b)
@@ -600,12 +618,14 @@ __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); 
 __device__ __forceinline__ float2 bc2(float c) { return make_float2(c, c); }
 
 template <bool EXACT, bool IMG, bool PK>
-__global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_constant__ Ac3DTArgs A)
+__global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_constant__ Ac3DSArgs A)
 {
     const Ac3DArgs &a = A.a;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *slab = reinterpret_cast<float *>(smem_raw + ((128u - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127u)) & 127u));
-    unsigned long long *full = reinterpret_cast<unsigned long long *>(slab + S3_NS * T3_SLICE);
+    float *p0b = slab + S3_NS * T3_SLICE, *velb = p0b + S3_NP * S3_BOX;
+    unsigned long long *fulls = reinterpret_cast<unsigned long long *>(velb + S3_NP * S3_BOX);
+    unsigned long long *fullp = fulls + S3_NS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int n1 = a.n1, n2 = a.n2, n3 = a.n3;
     const int ntz = (n1 - 9 + A_TZ - 1) / A_TZ;  // rows 4 .. n1-6 (interior plus row 4)
@@ -638,69 +658,80 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_con
             ys = (int)(a.src_o / s3);
         }
     }
-    auto issue = [&](int s, int k) {
-        mbar_expect_tx(&full[k], (unsigned)(T3_SLICE * sizeof(float)));
-        tma_load_3d(slab + k * T3_SLICE, &A.tm, z0 - A_ZH, x0 - AR, s, &full[k]);
+    const int slab_last = yb - 1 + AR;  // the queue reads slabs up to here
+    auto issue_slab = [&](int s) {
+        const int k = (s - ya) & (S3_NS - 1);
+        mbar_expect_tx(&fulls[k], (unsigned)(T3_SLICE * sizeof(float)));
+        tma_load_3d(slab + k * T3_SLICE, &A.tm, z0 - A_ZH, x0 - AR, s, &fulls[k]);
     };
+    auto issue_box = [&](int s) {
+        const int k = (s - ya) & (S3_NP - 1);
+        mbar_expect_tx(&fullp[k], (unsigned)(2 * S3_BOX * sizeof(float)));
+        tma_load_3d(p0b + k * S3_BOX, &A.tm0, z0, x0, s, &fullp[k]);
+        tma_load_3d(velb + k * S3_BOX, &A.tmv, z0, x0, s, &fullp[k]);
+    };
+    auto slab_ok = [&](int s) { return mbar_wait(&fulls[(s - ya) & (S3_NS - 1)], (unsigned)(((s - ya) / S3_NS) & 1)); };
+    auto box_ok = [&](int s) { return mbar_wait(&fullp[(s - ya) & (S3_NP - 1)], (unsigned)(((s - ya) / S3_NP) & 1)); };
     if (threadIdx.x == 0) {
-        for (int k = 0; k < S3_NS; k++) mbar_init(&full[k]);
+        for (int k = 0; k < S3_NS; k++) mbar_init(&fulls[k]);
+        for (int k = 0; k < S3_NP; k++) mbar_init(&fullp[k]);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        issue(ya, 0);
-        if (ya + 1 < yb) issue(ya + 1, 1);
+        for (int s = ya; s <= min(ya + S3_LEAD - 1, slab_last); s++) issue_slab(s);
+        for (int s = ya; s <= min(ya + S3_NP - 2, yb - 1); s++) issue_box(s);
     }
-    const float *pp1 = a.p1 + (long long)x * n1 + z;  // this thread's column in each array
-    const float *pp0 = a.p0 + (long long)x * n1 + z, *pvel = a.vel + (long long)x * n1 + z;
     float *pp2 = a.p2 + (long long)x * n1 + z;
-    auto L4 = [&](const float *p, int y) -> float4 {
-        return grp ? __ldg(reinterpret_cast<const float4 *>(p + (long long)y * s3)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    };
-    // queue slot of slice s: (s - ya + 5) % S3_Q
+    // queue slot of slice s: (s - ya + 5) % S3_Q; slices ya-5 .. ya+4 from
+    // global memory, later ones from the slabs
     float4 q[S3_Q];
+    {
+        const float *pp1 = a.p1 + (long long)x * n1 + z;
 #pragma unroll
-    for (int k = 0; k < 2 * AR + 1; k++) q[k] = L4(pp1, ya - AR + k);
-    q[S3_Q - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 p0s[2], vels[2];
-    p0s[0] = L4(pp0, ya);
-    vels[0] = L4(pvel, ya);
-    p0s[1] = vels[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < 2 * AR; k++)
+            q[k] = grp ? __ldg(reinterpret_cast<const float4 *>(pp1 + (long long)(ya - AR + k) * s3))
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+        q[S3_Q - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     const float *coef = a.coef;
     const int cofs = (warp + AR) * A_LZ + (4 * lane + A_ZH);  // this thread's float4 within a slab
+    const int bofs = warp * A_TZ + 4 * lane;                  // ... within a p0 / vel box
     for (int yblk = ya; yblk < yb; yblk += S3_Q) {
 #pragma unroll
         for (int u = 0; u < S3_Q; u++) {
             const int y = yblk + u;
             if (y >= yb) break;
-            const int ss = u % S3_NS;
-            const bool ok = mbar_wait(&full[ss], (unsigned)((u / S3_NS) & 1));
+            // slab y (x/z taps; landed before unless in the first slices),
+            // slab y+5 (queue) and the p0/vel box of y
+            const bool ok = slab_ok(y) && slab_ok(y + AR) && box_ok(y);
             if (__syncthreads_or(!ok)) {
                 // record, let the copies in flight land (bounded) and stop
                 if (threadIdx.x == 0) {
                     if (a.err) atomicExch(a.err, 1);
-                    for (int s = y; s <= min(y + 1, yb - 1); s++) {
-                        const int v = s - yblk;
-                        mbar_wait(&full[v % S3_NS], (unsigned)((v / S3_NS) & 1));
-                    }
+                    for (int s = y; s <= min(y + S3_LEAD - 1, slab_last); s++) slab_ok(s);
+                    for (int s = y; s <= min(y + S3_NP - 2, yb - 1); s++) box_ok(s);
                 }
                 __syncthreads();
                 return;
             }
-            // every thread is past slice y-1: its slot takes slice y+2
-            if (threadIdx.x == 0 && y + 2 < yb) issue(y + 2, (u + 2) % S3_NS);
-            if (y + 6 <= yb - 1 + AR) q[(u + 11) % S3_Q] = L4(pp1, y + 6);
+            // every thread is past slice y-1: its slab slot takes slice y+7,
+            // its box slot slice y+3
+            if (threadIdx.x == 0) {
+                if (y + S3_LEAD <= slab_last) issue_slab(y + S3_LEAD);
+                if (y + S3_NP - 1 < yb) issue_box(y + S3_NP - 1);
+            }
+            q[(u + 2 * AR) % S3_Q] = *reinterpret_cast<const float4 *>(slab + ((y + AR - ya) & (S3_NS - 1)) * T3_SLICE + cofs);
+            const int pk = (y - ya) & (S3_NP - 1);
+            const float4 p0c = *reinterpret_cast<const float4 *>(p0b + pk * S3_BOX + bofs);
+            const float4 velc = *reinterpret_cast<const float4 *>(velb + pk * S3_BOX + bofs);
+            if (!grp) continue;
             float4 imgc = make_float4(0.f, 0.f, 0.f, 0.f), simgc = imgc;
-            if (IMG && grp) {
+            if (IMG) {
                 imgc = *reinterpret_cast<const float4 *>(a.img + (long long)x * n1 + z + (long long)y * s3);
                 simgc = __ldg(reinterpret_cast<const float4 *>(a.simg + (long long)x * n1 + z + (long long)y * s3));
             }
-            if (y + 1 < yb) {
-                p0s[(u + 1) & 1] = L4(pp0, y + 1);
-                vels[(u + 1) & 1] = L4(pvel, y + 1);
-            }
-            if (!grp) continue;
-            const float *cz = slab + ss * T3_SLICE + cofs;
+            const float *cz = slab + ((y - ya) & (S3_NS - 1)) * T3_SLICE + cofs;
             float w[20];  // rows z-8 .. z+11 of column x
 #pragma unroll
             for (int i = 0; i < 20; i += 4) {
@@ -729,7 +760,6 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_con
                     acc[h] = mac2<EXACT, PK>(acc[h], cy2, add2<PK>(h ? hi2(yp) : lo2(yp), h ? hi2(ym) : lo2(ym)));
                 }
             }
-            const float4 p0c = p0s[u & 1], velc = vels[u & 1];
             // sponge factors of the 4 cells (uniform branch)
             const bool sp = damped && min(tile_e, edge_dist(y, n3)) < a.damp_a;
             float2 fac[2] = {bc2(1.f), bc2(1.f)};
@@ -802,33 +832,29 @@ __global__ void __launch_bounds__(T3_TX * 32, 1) k_acoustic3d_s(const __grid_con
 }
 
 // Step kernel where n1 % 4 == 0 and tensor maps are available:
-// 0 slab (default), 1 ring, 2 cp.async pipelined, 3 slab without the paired
-// instructions (same results as 0)
-int g_ac_kind = 2;
+// 0 slab (default), 1 ring, 2 cp.async pipelined, 3 slab with paired
+// single-precision instructions in fast arithmetic
+int g_ac_kind = 0;
 
-// Launch of a kernel that takes Ac3DTArgs (p1's tensor map, box of the
-// tile's 144 rows by 26 columns) with dynamic shared memory smem.
-template <typename K>
-int launch_tma3d(K kern, int variant, size_t smem, const Ac3DArgs &a0, int ychunks, cudaStream_t st)
+// Tensor maps of a step: p1 with a box of the tile's 144 rows by 26 columns
+// (ring and slab kernels), p0 and vel with a box of its 128 rows by 16
+// columns (slab kernel).
+int step_map(CUtensorMap *m, const float *p, const Ac3DArgs &a, bool slab)
 {
-    Ac3DTArgs t;
-    memset(&t, 0, sizeof t);
-    t.a = a0;
-    t.a.ychunks = ychunks;
-    TRY(make_map(&t.tm, a0.p1, false, a0.n1, a0.n2, a0.n3, (long long)a0.n1 * a0.n2, A_LZ, T3_LX));
+    return make_map(m, p, false, a.n1, a.n2, a.n3, (long long)a.n1 * a.n2, slab ? A_LZ : A_TZ, slab ? T3_LX : T3_TX);
+}
+
+// Dynamic shared memory above 48 KB, set once per kernel and device.
+template <typename K>
+int smem_attr(K kern, int variant, size_t smem)
+{
     static bool attr[RTM_MAX_DEVICES][16] = {};
-    {
-        const int dev = rtm_current_device();
-        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
-        if (!attr[dev][variant]) {
-            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr[dev][variant] = true;
-        }
+    const int dev = rtm_current_device();
+    std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+    if (!attr[dev][variant]) {
+        RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr[dev][variant] = true;
     }
-    const int ntz = (a0.n1 - 9 + A_TZ - 1) / A_TZ;
-    const int ntx = (a0.n2 - 2 * AR + T3_TX - 1) / T3_TX;
-    kern<<<ntz * ntx * ychunks, T3_TX * 32, smem, st>>>(t);
-    RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }
 
@@ -837,14 +863,34 @@ int launch_ac_tma(const Ac3DArgs &a0, int ychunks, cudaStream_t st)
 {
     const bool img = a0.img != nullptr;
     const int v = (EXACT ? 8 : 0) + (img ? 4 : 0);
-    switch (g_ac_kind) {
-    case 1: return launch_tma3d(img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>, v, T3_SMEM, a0, ychunks, st);
-    case 3: return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, false> : k_acoustic3d_s<EXACT, false, false>, v + 2,
-                                S3_SMEM, a0, ychunks, st);
-    default:  // paired instructions in fast arithmetic only
-        return launch_tma3d(img ? k_acoustic3d_s<EXACT, true, !EXACT> : k_acoustic3d_s<EXACT, false, !EXACT>, v + 3,
-                            S3_SMEM, a0, ychunks, st);
+    const int ntz = (a0.n1 - 9 + A_TZ - 1) / A_TZ;
+    const int ntx = (a0.n2 - 2 * AR + T3_TX - 1) / T3_TX;
+    const int grid = ntz * ntx * ychunks;
+    if (g_ac_kind == 1) {
+        Ac3DTArgs t;
+        memset(&t, 0, sizeof t);
+        t.a = a0;
+        t.a.ychunks = ychunks;
+        TRY(step_map(&t.tm, a0.p1, a0, true));
+        auto kern = img ? k_acoustic3d_t<EXACT, true> : k_acoustic3d_t<EXACT, false>;
+        TRY(smem_attr(kern, v, T3_SMEM));
+        kern<<<grid, T3_TX * 32, T3_SMEM, st>>>(t);
+    } else {
+        Ac3DSArgs t;
+        memset(&t, 0, sizeof t);
+        t.a = a0;
+        t.a.ychunks = ychunks;
+        TRY(step_map(&t.tm, a0.p1, a0, true));
+        TRY(step_map(&t.tm0, a0.p0, a0, false));
+        TRY(step_map(&t.tmv, a0.vel, a0, false));
+        // paired instructions in fast arithmetic only (kind 3)
+        auto kern = g_ac_kind != 3 ? (img ? k_acoustic3d_s<EXACT, true, false> : k_acoustic3d_s<EXACT, false, false>)
+                                   : (img ? k_acoustic3d_s<EXACT, true, !EXACT> : k_acoustic3d_s<EXACT, false, !EXACT>);
+        TRY(smem_attr(kern, v + (g_ac_kind != 3 ? 2 : 3), S3_SMEM));
+        kern<<<grid, T3_TX * 32, S3_SMEM, st>>>(t);
     }
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
 }
 
 template <bool EXACT>
@@ -1008,7 +1054,7 @@ int ac_forward(Ac3D &m, bool damped, long long src_o, const float *wavelet, floa
 
 extern "C" int acoustic3d_set_kernel(int kind)
 {
-    RTM_CHECK_ARG(kind >= 0 && kind <= 3, "kind must be 0 (slab), 1 (ring), 2 (pipelined) or 3 (slab, unpaired)");
+    RTM_CHECK_ARG(kind >= 0 && kind <= 3, "kind must be 0 (slab), 1 (ring), 2 (pipelined) or 3 (slab, paired)");
     g_ac_kind = kind;
     return RTM_OK;
 }

@@ -95,14 +95,6 @@ __device__ __forceinline__ void wait_previous_level()
     asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
 }
 
-__device__ __forceinline__ void mbar_init_n(unsigned long long *bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"((unsigned)__cvta_generic_to_shared(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive(unsigned long long *bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"((unsigned)__cvta_generic_to_shared(bar)) : "memory");
-}
 
 // Rank of field f among the recorded components (its trace slot).
 __device__ __forceinline__ int rec_slot(int mask, int f) { return __popc(mask & ((1 << f) - 1)); }

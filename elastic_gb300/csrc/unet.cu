@@ -527,31 +527,41 @@ int gemm_tc(const GemmArgs &g, cudaStream_t st)
 // fetches with the zero padding supplied by the copy's out-of-range fill.
 // The K loop runs over 9 taps x C / KC chunks (KC = 64 with a 128-byte
 // swizzle, 32 with a 64-byte swizzle); B (the weights, K-major [N][9 C]) is
-// a box of KC x BN.  One thread issues the copies into an S-stage ring (full
-// and empty mbarriers), one thread issues the MMAs (tcgen05.mma, accumulator
-// in tensor memory) and commits each stage back to its empty barrier; the
-// four warps then run the epilogue of k_gemm_tc.  Every wait is bounded and
-// a run-out sets g.err (the tile's output is then not written).
+// a box of KC x BN.
+// Persistent: one CTA per SM walks tiles blockIdx.x, + gridDim.x, ...
+// Warp 4 (one thread) issues the copies of every tile's K steps into an
+// S-stage ring (full/empty mbarriers); warp 5 (one thread) issues the MMAs
+// (tcgen05.mma, FP32 accumulator in tensor memory), committing each stage
+// back to its empty barrier and each finished tile to tfull[buffer]; warps
+// 0-3 drain the accumulator buffer of the tile before (two buffers of BN
+// columns, released through tempty), so a tile's epilogue -- the epilogue
+// of k_gemm_tc -- runs under the next tile's MMAs and copies.  Every wait
+// is bounded; a run-out stops every role, sets g.err (outputs then
+// incomplete), and the copies in flight are let land before the CTA exits.
 struct ConvTcArgs {
     GemmArgs g;
     CUtensorMap tma;  // X + xoff: {C, W, H, images}, box {KC, min(W,128), 128/min(W,128), 1}
     CUtensorMap tmb;  // B: {9 C, N}, box {KC, BN}
     int nk;           // K steps: 9 * C / KC
     int cchunks;      // C / KC
+    int ntiles;       // M / 128
 };
+
+constexpr int CV_THREADS = 192;  // warps 0-3 epilogue, 4 copies, 5 MMAs
 
 template <int BN, int KC>
 struct ConvCfg {
     static constexpr int A_BYTES = TC_BM * KC * 2;
     static constexpr int B_BYTES = BN * KC * 2;
     static constexpr int STAGE = A_BYTES + B_BYTES;
-    static constexpr int STAGES = (96 * 1024 / STAGE) < 4 ? 4 : (96 * 1024 / STAGE) > 8 ? 8 : (96 * 1024 / STAGE);
-    static constexpr uint32_t NCOLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
-    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 + 8 * (2 * STAGES + 1) + 16;
+    static constexpr int STAGES = (192 * 1024 / STAGE) > 8 ? 8 : (192 * 1024 / STAGE);
+    static constexpr uint32_t NCOLS = 2 * BN <= 64 ? 64 : 2 * BN <= 128 ? 128 : 2 * BN <= 256 ? 256 : 512;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 + 8 * (2 * STAGES + 5) + 16;
+    static_assert(STAGES >= 4, "stages");
 };
 
 template <int BN, int EPI, int KC>
-__global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ ConvTcArgs A)
+__global__ void __launch_bounds__(CV_THREADS, 1) k_conv_tc(const __grid_constant__ ConvTcArgs A)
 {
     using T = ConvCfg<BN, KC>;
     constexpr int S = T::STAGES;
@@ -559,14 +569,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ 
     extern __shared__ __align__(16) unsigned char cv_raw[];
     unsigned char *base = cv_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(cv_raw) & 1023u)) & 1023u);
     unsigned long long *full = reinterpret_cast<unsigned long long *>(base + S * T::STAGE);
-    unsigned long long *empty = full + S, *done = empty + S;
+    unsigned long long *empty = full + S, *tfull = empty + S, *tempty = tfull + 2, *done = tempty + 2;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
     int *fail = reinterpret_cast<int *>(tslot + 1);
+    int *issued = fail + 1;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.x * TC_BM;
-    // tile origin: image, first row, first column
-    const int HW = g.H * g.W;
-    const int img = m0 / HW, rem = m0 - img * HW, y0 = rem / g.W, x0 = rem - y0 * g.W;
+    const int nk = A.nk, HW = g.H * g.W;
     if (warp == 0) {
         tmem_alloc(tslot, T::NCOLS);
         tmem_relinquish();
@@ -576,63 +584,113 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv_tc(const __grid_constant__ 
             mbar_init(&full[i]);
             mbar_init(&empty[i]);
         }
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&tfull[i]);
+            eg::mbar_init_n(&tempty[i], 4);
+        }
         mbar_init(done);
         *fail = 0;
+        *issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    const int nk = A.nk;
-    if (tid == 0) {
-        // producer: K step i into stage i % S once the MMAs of step i - S
-        // have released it
-        for (int i = 0; i < nk; i++) {
-            const int st = i % S;
-            if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i - S) / S) & 1))) {
-                atomicExch(fail, 1);
-                break;
+    auto failed = [&]() { return *reinterpret_cast<volatile int *>(fail) != 0; };
+    if (warp == 4) {
+        if (lane == 0) {
+            // copies: K step `it` (counted over all of this CTA's tiles) into
+            // stage it % S once the MMAs of step it - S have released it
+            int it = 0;
+            for (int t = blockIdx.x; t < A.ntiles && !failed(); t += gridDim.x) {
+                const int m0 = t * TC_BM, img = m0 / HW, rem = m0 - img * HW, y0 = rem / g.W, x0 = rem - y0 * g.W;
+                for (int i = 0; i < nk; i++, it++) {
+                    const int st = it % S;
+                    if (it >= S && !mbar_wait(&empty[st], (unsigned)(((it - S) / S) & 1))) {
+                        atomicExch(fail, 1);
+                        break;
+                    }
+                    const int tap = i / A.cchunks, cc = i - tap * A.cchunks, dy = tap / 3, dx = tap - 3 * dy;
+                    unsigned char *sa = base + st * T::STAGE;
+                    mbar_expect_tx(&full[st], (unsigned)T::STAGE);
+                    tma_load_4d(sa, &A.tma, cc * KC, x0 + dx - 1, y0 + dy - 1, img, &full[st]);
+                    tma_load_2d(sa + T::A_BYTES, &A.tmb, tap * g.C + cc * KC, 0, &full[st]);
+                    *reinterpret_cast<volatile int *>(issued) = it + 1;
+                }
             }
-            if (*reinterpret_cast<volatile int *>(fail)) break;
-            const int tap = i / A.cchunks, cc = i - tap * A.cchunks, dy = tap / 3, dx = tap - 3 * dy;
-            unsigned char *sa = base + st * T::STAGE;
-            mbar_expect_tx(&full[st], (unsigned)T::STAGE);
-            tma_load_4d(sa, &A.tma, cc * KC, x0 + dx - 1, y0 + dy - 1, img, &full[st]);
-            tma_load_2d(sa + T::A_BYTES, &A.tmb, tap * g.C + cc * KC, 0, &full[st]);
         }
-    } else if (tid == 32) {
-        // MMA issue: KC / 16 MMAs per step, the descriptors advancing 32
-        // bytes along K inside the swizzle atom
-        constexpr uint32_t IDESC = umma_idesc_f16(TC_BM, BN, true, true);
-        constexpr uint32_t SW = KC == 64 ? 2u : 4u, SBO = 8u * KC * 2u;
-        for (int i = 0; i < nk; i++) {
-            const int st = i % S;
-            if (!mbar_wait(&full[st], (unsigned)((i / S) & 1))) {
-                atomicExch(fail, 1);
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr uint32_t IDESC = umma_idesc_f16(TC_BM, BN, true, true);
+            constexpr uint32_t SW = KC == 64 ? 2u : 4u, SBO = 8u * KC * 2u;
+            int it = 0, j = 0;
+            for (int t = blockIdx.x; t < A.ntiles && !failed(); t += gridDim.x, j++) {
+                const int buf = j & 1;
+                // the epilogue has drained this buffer (tile j - 2)
+                if (j >= 2 && !mbar_wait(&tempty[buf], (unsigned)(((j - 2) >> 1) & 1))) {
+                    atomicExch(fail, 1);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(buf * BN);
+                bool ok = true;
+                for (int i = 0; i < nk; i++, it++) {
+                    const int st = it % S;
+                    if (!mbar_wait(&full[st], (unsigned)((it / S) & 1))) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_addr = smem_u32(base + st * T::STAGE), b_addr = a_addr + T::A_BYTES;
+#pragma unroll
+                    for (int k = 0; k < KC / 16; k++)
+                        umma_f16(acc, umma_sdesc(a_addr + 32 * k, 16, SBO, SW), umma_sdesc(b_addr + 32 * k, 16, SBO, SW),
+                                 IDESC, i > 0 || k > 0);
+                    umma_commit(&empty[st]);
+                }
+                if (!ok) {
+                    atomicExch(fail, 1);
+                    break;
+                }
+                umma_commit(&tfull[buf]);
+            }
+            umma_commit(done);  // tracks every MMA issued, also after a failure
+        }
+    } else {
+        // epilogue warps 0-3: tensor-memory lanes 32 warp .. + 31
+        int j = 0;
+        for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x, j++) {
+            const int buf = j & 1;
+            bool ok = mbar_wait(&tfull[buf], (unsigned)((j >> 1) & 1));
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) {
+                if (lane == 0) atomicExch(fail, 1);
                 break;
             }
             tc_fence_after();
-            const uint32_t a_addr = smem_u32(base + st * T::STAGE), b_addr = a_addr + T::A_BYTES;
-#pragma unroll
-            for (int k = 0; k < KC / 16; k++)
-                umma_f16(tmem, umma_sdesc(a_addr + 32 * k, 16, SBO, SW), umma_sdesc(b_addr + 32 * k, 16, SBO, SW), IDESC,
-                         i > 0 || k > 0);
-            umma_commit(&empty[st]);
+            tc_epilogue<BN, EPI>(g, tmem + (uint32_t)(buf * BN), t * TC_BM, warp, lane);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) eg::mbar_arrive(&tempty[buf]);
+            if (failed()) break;
         }
-        umma_commit(done);  // also after a failure: tracks every MMA issued
     }
-    bool ok = mbar_wait(done, 0);
-    if (!ok) ok = mbar_wait(done, 0);  // the MMAs may still be running: a second limit
+    // every MMA complete before the tensor memory is released
+    if (warp == 5 || tid == 0) {
+        bool ok = mbar_wait(done, 0);
+        if (!ok) ok = mbar_wait(done, 0);
+        if (!ok) atomicExch(fail, 1);
+    }
     tc_fence_after();
-    if (__syncthreads_or(!ok || *reinterpret_cast<volatile int *>(fail))) {
+    if (__syncthreads_or(failed())) {
         if (tid == 0) {
             if (g.err) atomicExch(g.err, 1);
-            // let copies that were issued but never consumed land (bounded)
-            for (int i = 0; i < nk && i < S; i++) mbar_wait(&full[(nk - 1 - i) % S], (unsigned)(((nk - 1 - i) / S) & 1));
+            // let issued copies land (bounded): the last S issued steps
+            const int n = *reinterpret_cast<volatile int *>(issued);
+            for (int i = n - 1; i >= 0 && i >= n - S; i--) mbar_wait(&full[i % S], (unsigned)((i / S) & 1));
         }
-    } else {
-        tc_epilogue<BN, EPI>(g, tmem, m0, warp, lane);
+        __syncthreads();
     }
     tc_fence_before();
     __syncthreads();
@@ -664,6 +722,7 @@ int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
         const int box[2] = {KC, BN};
         TRY(make_map_nd(&a.tmb, g.B, true, 2, dims, strides, box, 2 * KC));
     }
+    a.ntiles = g.M / TC_BM;
     auto kern = k_conv_tc<BN, EPI, KC>;
     static bool attr[RTM_MAX_DEVICES] = {};
     {
@@ -674,7 +733,8 @@ int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
             attr[dev] = true;
         }
     }
-    kern<<<g.M / TC_BM, TC_THREADS, T::SMEM, st>>>(a);
+    const int grid = std::min(a.ntiles, eg::device_sm_count());
+    kern<<<grid, CV_THREADS, T::SMEM, st>>>(a);
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }

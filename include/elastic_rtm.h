@@ -252,15 +252,15 @@ int acoustic3d_rtm_c_(int n1, int n2, int n3, int nt, float d1, float d2, float 
  * kernel uses 16 columns. */
 int acoustic3d_set(int tile_x, int ychunks);
 /* Step kernel where n1 % 4 == 0 (other n1 run a scalar kernel):
- *   0 (default) slab kernel: each slice's x/z slab arrives by a bulk tensor
- *     copy two slices ahead, the y taps from a register queue, paired FP32
- *     instructions;
+ *   0 (default) slab kernel: every operand arrives by bulk tensor copies
+ *     issued slices ahead (p1 slabs with their x/z halo, p0 and v^2 dt^2
+ *     boxes), the y taps from an unrolled register queue;
  *   1 slice-ring kernel: every tap from a 13-slice shared-memory ring filled
  *     by bulk tensor copies;
  *   2 cp.async-pipelined kernel with a shifted register queue;
- *   3 the slab kernel with scalar instructions.
- * All are bit-identical in exact arithmetic.  A kernel whose slice load does
- * not land within about a second stops; the entry point then returns
+ *   3 the slab kernel with paired FP32 instructions in fast arithmetic.
+ * All are bit-identical in exact arithmetic.  A kernel whose copy does not
+ * land within about a second stops; the entry point then returns
  * RTM_ERR_TIMEOUT (4). */
 int acoustic3d_set_kernel(int kind);
 

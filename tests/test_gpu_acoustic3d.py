@@ -25,7 +25,7 @@ def setup(n1=40, n2=36, n3=34, nt=30, seed=0):
     return vel.astype(np.float32), w
 
 
-@pytest.fixture(autouse=True, params=["slab", "slab-unpaired", "ring", "pipelined"])
+@pytest.fixture(autouse=True, params=["slab", "slab-paired", "ring", "pipelined"])
 def kernel(request):
     """Every test runs with every step kernel (they differ where n1 % 4 == 0)."""
     A.set_kernel(request.param)
