@@ -848,6 +848,58 @@ def run_unet(args):
                       "clocks": clk.summary()}), flush=True)
 
 
+def elastic3d_block(args, steps, warmup, n=None):
+    """One step of the reference's 3D elastic kernel test
+    (kernel_3d_test/rtmlib-modC.c:277-590: nine fields, six coefficient
+    planes, 10th-order staggered differences along z, x and y) on an n^3
+    interior (padded by 5 on every side), seeded random planes resident in
+    HBM; exact arithmetic (bit-identical to the reference's CPU step)."""
+    import torch
+    from elastic_gb300 import elastic3d as E
+    n = n or 384
+    g = torch.Generator(device="cuda").manual_seed(11)
+    shape = (n + 10, n + 10, n + 10)
+    mk = lambda: (torch.rand(shape, device="cuda", generator=g) * 2 - 1).contiguous()
+    inp, in1, out, m = [mk() for _ in range(9)], [mk() for _ in range(9)], [mk() for _ in range(9)], [mk() for _ in range(6)]
+    for _ in range(warmup):
+        E.step_dev(inp, in1, out, m, exact=True)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        for _ in range(steps):
+            E.step_dev(inp, in1, out, m, exact=True)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    cells = n ** 3
+    rate = cells / (ms * 1e-3) / 1e9
+    peak, kind = measured_peaks()
+    # e2e: the reference-shaped drop-in (host planes in, step, nine out)
+    h = [a.cpu().numpy() for a in inp + in1 + out + m]
+    te = time.perf_counter()
+    E.step(h[:9], h[9:18], h[18:27], h[27:], exact=True)
+    e2e_s = time.perf_counter() - te
+    del inp, in1, out, m
+    torch.cuda.empty_cache()
+    return {"metric": "Gcell-updates/s (3D elastic step)", "value": round(rate, 3), "unit": "Gcell/s", "n_gpus": 1,
+            "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"3D elastic kernel test step, {n}^3 interior (nine fields, six coefficients), "
+                                   "exact arithmetic", "inputs_vs_l2": "inputs larger than L2"},
+            "e2e": {"value": round(cells / e2e_s / 1e9, 3), "unit": "Gcell/s",
+                    "h2d_bytes_per_step": 33 * 4 * (n + 10) ** 3, "d2h_bytes_per_step": 9 * 4 * (n + 10) ** 3},
+            "gpu_launches": steps,
+            "roofline": {"bound": "hbm", "achieved": round(rate * 168, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(rate * 168 / peak, 4), "peak_kind": kind,
+                         "kernel": "k_k3_step (168 algorithmic B/cell: 33 planes read, 9 written)", "traffic": None},
+            "clocks": clk.summary()}
+
+
+def run_elastic3d(args):
+    print(json.dumps(elastic3d_block(args, args.steps, args.warmup, args.n3)), flush=True)
+
+
 # --------------------------------------------------------------- config 5 sample
 def c5_block(args, warmup=1, steps=1):
     """One 4-shot group of the 256-shot survey (6000 x 2000 cells, dx=5 m,
@@ -919,6 +971,7 @@ def run_default(args):
         if not args.no_secondary:
             sec = {}
             sec["acoustic3d"] = acoustic3d_block(args, steps=3, warmup=3)
+            sec["elastic3d"] = elastic3d_block(args, steps=10, warmup=3, n=384)
             sec["rtm2d_256shot_group"] = c5_block(args)
             sec["precond"] = precond_block(args, steps=100, warmup=5, pairs=args.sec_pairs,
                                            train_steps=args.sec_train_steps, ntest=2)
@@ -940,7 +993,7 @@ def main():
     ap.add_argument("--group", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--tune-steps", type=int, default=20)
-    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond", "unet"])
+    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond", "unet", "elastic3d"])
     ap.add_argument("--pairs", type=int, default=None, help="training pairs of the precond workload")
     ap.add_argument("--train-steps", type=int, default=None, help="Adam steps of the precond workload")
     ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
@@ -971,6 +1024,8 @@ def main():
         run_acoustic3d(args)
     elif args.workload == "unet":
         run_unet(args)
+    elif args.workload == "elastic3d":
+        run_elastic3d(args)
     elif args.workload == "precond":
         run_precond(args)
     elif args.workload == "rtm2d":

@@ -83,6 +83,11 @@ SIGNATURES = {
                                    _c_int, _P, _c_int, _P, _c_int, _P]),
     "acoustic3d_set": (_c_int, [_c_int, _c_int]),
     "acoustic3d_set_kernel": (_c_int, [_c_int]),
+    "rtm3d_gpu_init": (None, [_c_int] * 3),
+    "rtm3d_gpu_func": (None, [_c_int] * 3 + [_P] * 35),
+    "rtm3d_gpu_final": (None, []),
+    "rtm3d_set_exact": (_c_int, [_c_int]),
+    "rtm3d_step_dev": (_c_int, [_c_int] * 3 + [_P] * 4 + [_c_int]),
     "rtm_debug_umma_desc": (_c_int, [_c_int, _c_int, _c_int, _c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                      ctypes.c_uint, _P]),
     "rtm_debug_umma_probe": (_c_int, [_c_int, ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),

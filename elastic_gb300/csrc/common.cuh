@@ -18,6 +18,7 @@ enum RtmStatus {
 };
 
 void rtm_set_error(const char *fmt, ...);
+void rtm_set_status(int s, const char *where);
 
 // On failure the runtime's last-error slot is cleared as well, so that one
 // failed call is reported once and not again by the next check.

@@ -32,6 +32,13 @@ void rtm_set_error(const char *fmt, ...)
 }
 extern "C" const char *rtm_last_error(void) { return g_err; }
 extern "C" int rtm_last_status(void) { return g_last_status; }
+// status of a void drop-in entry point (read back by rtm_last_status); a
+// failure is also reported on stderr, the void entry points' only channel
+void rtm_set_status(int s, const char *where)
+{
+    g_last_status = s;
+    if (s) fprintf(stderr, "%s: %s\n", where, g_err);
+}
 extern "C" void rtm_set_exact(int exact) { g_exact = exact ? 1 : 0; }
 static int g_kernel_version = 0;
 extern "C" void rtm_set_kernel_version(int v) { g_kernel_version = (v == 1 || v == 2) ? v : 0; }

@@ -264,6 +264,36 @@ int acoustic3d_set(int tile_x, int ychunks);
  * RTM_ERR_TIMEOUT (4). */
 int acoustic3d_set_kernel(int kind);
 
+/* ----------------------------------- 3D elastic kernel test (kernel_3d_test)
+ * One step of the reference's 3D elastic kernel (kernel_3d_test/
+ * rtmlib-modC.c:277-590): nine fields Vy, Vx, Vz, syy, sxx, szz, sxy, sxz,
+ * syz and six coefficient planes m1_y, m1_x, m1_z, m2, m3, m2m3, each a
+ * padded (ny+10)(nx+10)(nz+10) float plane, z fastest, interior at +5;
+ * out = out + in1 + 10th-order staggered differences of coefficient x
+ * field taps of `in` along z, x and y.
+ * rtm3d_gpu_init / rtm3d_gpu_func / rtm3d_gpu_final have the signatures and
+ * meaning of the reference's rtm_gpu_init / rtm_gpu_func / rtm_gpu_final
+ * for this test (kernel_3d_test/gpu.h:68-79, rtmlib-modC-gpu.cu:65,218,698):
+ * host planes in, one step, the nine outputs copied back, gpu_kernel_time
+ * = {copy in, step, copy out} in seconds.  They carry an rtm3d_ prefix
+ * because the 2D drop-in already exports the reference's rtm_gpu_* names;
+ * the reference's test binds them by renaming on its compile line
+ * (INTEGRATION.md).  Status in rtm_last_status().  Exact arithmetic (the
+ * default, rtm3d_set_exact(1)) is bit-identical to the reference's CPU
+ * step; rtm3d_set_exact(0) lets the compiler fuse multiply-adds.
+ * rtm3d_step_dev: the same step on device planes (in[9], in1[9], out[9],
+ * m[6] arrays of device pointers), on the default stream. */
+void rtm3d_gpu_init(int ny, int nz, int nx);
+void rtm3d_gpu_func(int ny, int nz, int nx, float *vy0, float *vx0, float *vz0, float *syy0, float *sxx0, float *szz0,
+                    float *sxy0, float *sxz0, float *syz0, float *vy1, float *vx1, float *vz1, float *syy1, float *sxx1,
+                    float *szz1, float *sxy1, float *sxz1, float *syz1, float *vyo, float *vxo, float *vzo, float *syyo,
+                    float *sxxo, float *szzo, float *sxyo, float *sxzo, float *syzo, float *m1y, float *m1x, float *m1z,
+                    float *m2, float *m3, float *m2m3, float *debug, float *gpu_kernel_time);
+void rtm3d_gpu_final(void);
+int rtm3d_set_exact(int exact);
+int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *const *in1, float *const *out,
+                   const float *const *m, int exact);
+
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
  * shots of a survey, each on its own subgrid [x0, x0+nxs) of the full model

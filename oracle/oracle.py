@@ -392,3 +392,48 @@ def acoustic_rtm_stored(vel2, coef, damp_a, table, hist, zr, d, jt):
     lib().ora3d_rtm_stored(n1, n2, n3, nt, jt, _p(vel2), _p(coef), damp_a, _p(table), _p(np.ascontiguousarray(hist)),
                            zr, _p(np.ascontiguousarray(d)), _p(img))
     return img
+
+
+# ------------------------------------------------ 3D elastic kernel test (K3)
+K3_FIELDS = ("vy", "vx", "vz", "syy", "sxx", "szz", "sxy", "sxz", "syz")
+K3_COEFS = ("m1y", "m1x", "m1z", "m2", "m3", "m2m3")
+
+
+def _pp(arrs):
+    P = ctypes.c_void_p * len(arrs)
+    return P(*[a.ctypes.data_as(ctypes.c_void_p) for a in arrs])
+
+
+def k3_step(inp, in1, out, m):
+    """One step of the reference's 3D elastic kernel test
+    (kernel_3d_test/rtmlib-modC.c:277-590) in float32: inp, in1, out lists
+    of nine padded (ny+10, nx+10, nz+10) arrays (Vy, Vx, Vz, syy, sxx, szz,
+    sxy, sxz, syz), m six (m1y, m1x, m1z, m2, m3, m2m3).  out is updated in
+    place and returned."""
+    L = lib()
+    ny, nx, nz = (d - 10 for d in out[0].shape)
+    for a in list(inp) + list(in1) + list(out) + list(m):
+        assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"] and a.shape == out[0].shape
+    L.ora_k3_step(ctypes.c_int(ny), ctypes.c_int(nz), ctypes.c_int(nx), _pp(inp), _pp(in1), _pp(out), _pp(m))
+    return out
+
+
+def k3_table():
+    n = np.zeros(9, np.int32)
+    t = np.zeros(9 * 5 * 4, np.int32)
+    lib().ora_k3_table(_p(n), _p(t))
+    return n, t.reshape(9, 5, 4)
+
+
+K3_CHECK = os.path.join(HERE, "_ref", "k3_check_oracle")
+
+
+def k3_reference_check(binary=K3_CHECK, plant=False, timeout=600):
+    """Run the reference's own 3D elastic kernel test main (random 200^3
+    fields, the hand-off, its CPU step, func_check at 1e-13) with the
+    hand-off served by `binary`'s implementation; returns its stderr."""
+    env = dict(os.environ)
+    if plant:
+        env["K3_PLANT"] = "1"
+    r = subprocess.run([binary], capture_output=True, text=True, env=env, timeout=timeout)
+    return r.stderr
