@@ -92,6 +92,7 @@ SIGNATURES = {
                                      ctypes.c_uint, _P]),
     "rtm_debug_umma_probe": (_c_int, [_c_int, ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),
     "rtm_debug_umma_probe_sw": (_c_int, [_c_int, _c_int, _P, _P, _P]),
+    "rtm_debug_umma_probe2": (_c_int, [_c_int] * 5 + [ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),
 }
 
 _lib = None

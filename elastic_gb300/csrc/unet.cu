@@ -549,10 +549,19 @@ struct ConvTcArgs {
 
 constexpr int CV_THREADS = 192;  // warps 0-3 epilogue, 4 copies, 5 MMAs
 
-template <int BN, int KC>
+// SH (image rows of at least 128 pixels): a K step is a row of taps dy and a
+// channel chunk; its A operand is ONE box of 136 pixels (the tile's 128 and
+// its 1-pixel halo, rounded to whole 8-row atoms) and the three taps dx are
+// MMAs whose descriptors start dx rows into it (the swizzle follows the
+// absolute shared-memory address, so a row-shifted start needs no base
+// offset); B is the three taps' weight boxes.
+constexpr int CV_SH_ROWS = 136;
+
+template <int BN, int KC, bool SH>
 struct ConvCfg {
-    static constexpr int A_BYTES = TC_BM * KC * 2;
-    static constexpr int B_BYTES = BN * KC * 2;
+    static constexpr int A_BYTES = SH ? (CV_SH_ROWS * KC * 2 + 1023) / 1024 * 1024 : TC_BM * KC * 2;
+    static constexpr int B_TAP = BN * KC * 2;
+    static constexpr int B_BYTES = (SH ? 3 : 1) * B_TAP;
     static constexpr int STAGE = A_BYTES + B_BYTES;
     static constexpr int STAGES = (192 * 1024 / STAGE) > 8 ? 8 : (192 * 1024 / STAGE);
     static constexpr uint32_t NCOLS = 2 * BN <= 64 ? 64 : 2 * BN <= 128 ? 128 : 2 * BN <= 256 ? 256 : 512;
@@ -560,10 +569,10 @@ struct ConvCfg {
     static_assert(STAGES >= 4, "stages");
 };
 
-template <int BN, int EPI, int KC>
+template <int BN, int EPI, int KC, bool SH>
 __global__ void __launch_bounds__(CV_THREADS, 1) k_conv_tc(const __grid_constant__ ConvTcArgs A)
 {
-    using T = ConvCfg<BN, KC>;
+    using T = ConvCfg<BN, KC, SH>;
     constexpr int S = T::STAGES;
     const GemmArgs &g = A.g;
     extern __shared__ __align__(16) unsigned char cv_raw[];
@@ -611,11 +620,21 @@ __global__ void __launch_bounds__(CV_THREADS, 1) k_conv_tc(const __grid_constant
                         atomicExch(fail, 1);
                         break;
                     }
-                    const int tap = i / A.cchunks, cc = i - tap * A.cchunks, dy = tap / 3, dx = tap - 3 * dy;
                     unsigned char *sa = base + st * T::STAGE;
-                    mbar_expect_tx(&full[st], (unsigned)T::STAGE);
-                    tma_load_4d(sa, &A.tma, cc * KC, x0 + dx - 1, y0 + dy - 1, img, &full[st]);
-                    tma_load_2d(sa + T::A_BYTES, &A.tmb, tap * g.C + cc * KC, 0, &full[st]);
+                    if (SH) {
+                        // row of taps dy, channel chunk cc: one 136-pixel box, three weight boxes
+                        const int dy = i / A.cchunks, cc = i - dy * A.cchunks;
+                        mbar_expect_tx(&full[st], (unsigned)(CV_SH_ROWS * KC * 2 + 3 * T::B_TAP));
+                        tma_load_4d(sa, &A.tma, cc * KC, x0 - 1, y0 + dy - 1, img, &full[st]);
+                        for (int dx = 0; dx < 3; dx++)
+                            tma_load_2d(sa + T::A_BYTES + dx * T::B_TAP, &A.tmb, (3 * dy + dx) * g.C + cc * KC, 0,
+                                        &full[st]);
+                    } else {
+                        const int tap = i / A.cchunks, cc = i - tap * A.cchunks, dy = tap / 3, dx = tap - 3 * dy;
+                        mbar_expect_tx(&full[st], (unsigned)T::STAGE);
+                        tma_load_4d(sa, &A.tma, cc * KC, x0 + dx - 1, y0 + dy - 1, img, &full[st]);
+                        tma_load_2d(sa + T::A_BYTES, &A.tmb, tap * g.C + cc * KC, 0, &full[st]);
+                    }
                     *reinterpret_cast<volatile int *>(issued) = it + 1;
                 }
             }
@@ -644,9 +663,12 @@ __global__ void __launch_bounds__(CV_THREADS, 1) k_conv_tc(const __grid_constant
                     tc_fence_after();
                     const uint32_t a_addr = smem_u32(base + st * T::STAGE), b_addr = a_addr + T::A_BYTES;
 #pragma unroll
-                    for (int k = 0; k < KC / 16; k++)
-                        umma_f16(acc, umma_sdesc(a_addr + 32 * k, 16, SBO, SW), umma_sdesc(b_addr + 32 * k, 16, SBO, SW),
-                                 IDESC, i > 0 || k > 0);
+                    for (int dx = 0; dx < (SH ? 3 : 1); dx++)
+#pragma unroll
+                        for (int k = 0; k < KC / 16; k++)
+                            umma_f16(acc, umma_sdesc(a_addr + dx * (KC * 2) + 32 * k, 16, SBO, SW),
+                                     umma_sdesc(b_addr + dx * T::B_TAP + 32 * k, 16, SBO, SW), IDESC,
+                                     i > 0 || dx > 0 || k > 0);
                     umma_commit(&empty[st]);
                 }
                 if (!ok) {
@@ -699,16 +721,16 @@ __global__ void __launch_bounds__(CV_THREADS, 1) k_conv_tc(const __grid_constant
 
 // Tensor maps and launch of k_conv_tc; RTM_ERR_ARG when the geometry does
 // not fit (the caller then uses k_gemm_tc).
-template <int BN, int EPI, int KC>
+template <int BN, int EPI, int KC, bool SH>
 int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
 {
-    using T = ConvCfg<BN, KC>;
+    using T = ConvCfg<BN, KC, SH>;
     ConvTcArgs a;
     memset(&a, 0, sizeof a);
     a.g = g;
     a.cchunks = g.C / KC;
-    a.nk = 9 * a.cchunks;
-    const int bw = g.W < 128 ? g.W : 128, bh = 128 / bw;
+    a.nk = (SH ? 3 : 9) * a.cchunks;
+    const int bw = SH ? CV_SH_ROWS : g.W < 128 ? g.W : 128, bh = SH ? 1 : 128 / bw;
     const long long imgs = (long long)g.M / ((long long)g.H * g.W);
     {
         const long long dims[4] = {g.C, g.W, g.H, imgs};
@@ -723,7 +745,7 @@ int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
         TRY(make_map_nd(&a.tmb, g.B, true, 2, dims, strides, box, 2 * KC));
     }
     a.ntiles = g.M / TC_BM;
-    auto kern = k_conv_tc<BN, EPI, KC>;
+    auto kern = k_conv_tc<BN, EPI, KC, SH>;
     static bool attr[RTM_MAX_DEVICES] = {};
     {
         const int dev = rtm_current_device();
@@ -739,14 +761,27 @@ int conv_tc_launch(const GemmArgs &g, cudaStream_t st)
     return RTM_OK;
 }
 
+int g_conv_shift = 1;  // 1: the shifted-box form where the image rows allow (W % 128 == 0)
+
+// row-segment tiles (W % 128 == 0) take the shifted-box form where its stage
+// (one 136-pixel box and three weight boxes) leaves at least four stages
+template <int BN, int EPI, int KC>
+int conv_tc_bn(const GemmArgs &g, cudaStream_t st)
+{
+    if constexpr (KC == 32 || BN <= 64) {
+        if (g_conv_shift && g.W % 128 == 0) return conv_tc_launch<BN, EPI, KC, true>(g, st);
+    }
+    return conv_tc_launch<BN, EPI, KC, false>(g, st);
+}
+
 template <int EPI, int KC>
 int conv_tc_kc(const GemmArgs &g, cudaStream_t st)
 {
-    if (g.N <= 32) return conv_tc_launch<32, EPI, KC>(g, st);
-    if (g.N <= 64) return conv_tc_launch<64, EPI, KC>(g, st);
-    if (g.N <= 96) return conv_tc_launch<96, EPI, KC>(g, st);
-    if (g.N <= 128) return conv_tc_launch<128, EPI, KC>(g, st);
-    return conv_tc_launch<256, EPI, KC>(g, st);
+    if (g.N <= 32) return conv_tc_bn<32, EPI, KC>(g, st);
+    if (g.N <= 64) return conv_tc_bn<64, EPI, KC>(g, st);
+    if (g.N <= 96) return conv_tc_bn<96, EPI, KC>(g, st);
+    if (g.N <= 128) return conv_tc_bn<128, EPI, KC>(g, st);
+    return conv_tc_launch<256, EPI, KC, false>(g, st);
 }
 
 // True when k_conv_tc covers this GEMM.
@@ -762,6 +797,224 @@ template <int EPI>
 int conv_tc(const GemmArgs &g, cudaStream_t st)
 {
     return g.C % 64 == 0 ? conv_tc_kc<EPI, 64>(g, st) : conv_tc_kc<EPI, 32>(g, st);
+}
+
+// ------------------------------- 3x3 weight gradients by bulk tensor copies
+// dW[co][kw] += sum over pixels p of dY[p][co] X[p + shift(tap(kw))][ci(kw)],
+// kw = tap * Cin + ci: a GEMM with M = kw (128 per CTA), N = Cout, K =
+// pixels, both operands MN-major (channels contiguous in the NHWC tensors):
+// per 64-pixel K step the A tile is four boxes of 32 channels x 64 pixels of
+// X shifted by the tap of each 32-channel chunk of kw (zero padding from the
+// copies' out-of-range fill), the B tile Cout/32 boxes of dY; each box lands
+// as eight 512-byte atoms of 8 pixels x 32 channels with the 64-byte swizzle
+// (MN-major canonical layout: leading offset 4096 bytes between boxes along
+// M/N, stride offset 512 bytes between atoms along K).  The pixel range is
+// split over CTAs; each adds its 128 x Cout partial sums to dW with FP32
+// atomics.  Roles and bounded waits as in k_conv_tc.
+struct WgradArgs {
+    float *dw;        // dW[n * ldc + m]
+    long long ldc;
+    int M, N;         // 9 Cin, Cout
+    int Cin, H, W;
+    int ksteps;       // 64-pixel steps in all
+    int steps_per_cta;
+    int *err;
+    CUtensorMap tmx;  // X + xoff: {Cin, W, H, images}, box {32, min(W,64), 64/min(W,64), 1}
+    CUtensorMap tmy;  // dY: {Cout, W, H, images}, same box
+};
+
+constexpr int WG_K = 64;                           // pixels per K step
+constexpr int WG_BOX = 32 * WG_K * 2;              // bytes of one 32-channel box (4 KB)
+
+template <int BN>
+struct WgCfg {
+    static constexpr int A_BYTES = 4 * WG_BOX;             // 128 kw
+    static constexpr int B_BYTES = (BN / 32) * WG_BOX;
+    static constexpr int STAGE = A_BYTES + B_BYTES;
+    static constexpr int STAGES = (192 * 1024 / STAGE) > 8 ? 8 : (192 * 1024 / STAGE);
+    static constexpr uint32_t NCOLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+    static constexpr size_t SMEM = (size_t)STAGES * STAGE + 1024 + 8 * (2 * STAGES + 1) + 16;
+    static_assert(STAGES >= 4, "stages");
+};
+
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS) k_wgrad_tc(const __grid_constant__ WgradArgs A)
+{
+    using T = WgCfg<BN>;
+    constexpr int S = T::STAGES;
+    extern __shared__ __align__(16) unsigned char wg_raw[];
+    unsigned char *base = wg_raw + ((1024u - ((unsigned)__cvta_generic_to_shared(wg_raw) & 1023u)) & 1023u);
+    unsigned long long *full = reinterpret_cast<unsigned long long *>(base + S * T::STAGE);
+    unsigned long long *empty = full + S, *done = empty + S;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+    int *fail = reinterpret_cast<int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m0 = blockIdx.x * TC_BM;
+    const int k0 = blockIdx.y * A.steps_per_cta, k1 = min(A.ksteps, k0 + A.steps_per_cta);
+    if (k0 >= k1) return;
+    const int nk = k1 - k0;
+    if (warp == 0) {
+        tmem_alloc(tslot, T::NCOLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < S; i++) {
+            mbar_init(&full[i]);
+            mbar_init(&empty[i]);
+        }
+        mbar_init(done);
+        *fail = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const int HW = A.H * A.W, bw = A.W < WG_K ? A.W : WG_K;
+    if (tid == 0) {
+        // the A boxes of this CTA's kw rows: chunk j covers kw m0+32j ..
+        int nbox = 0, tapj[4], cj[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int kw = m0 + 32 * j;
+            tapj[j] = kw < A.M ? kw / A.Cin : -1;
+            cj[j] = kw < A.M ? kw - tapj[j] * A.Cin : 0;
+            nbox += kw < A.M;
+        }
+        const unsigned bytes = (unsigned)((nbox + BN / 32) * WG_BOX);
+        for (int i = 0; i < nk; i++) {
+            const int st = i % S;
+            if (i >= S && !mbar_wait(&empty[st], (unsigned)(((i - S) / S) & 1))) {
+                atomicExch(fail, 1);
+                break;
+            }
+            const int p0 = (k0 + i) * WG_K, img = p0 / HW, rem = p0 - img * HW, y0 = rem / A.W, x0 = rem - y0 * A.W;
+            unsigned char *sa = base + st * T::STAGE, *sb = sa + T::A_BYTES;
+            mbar_expect_tx(&full[st], bytes);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (tapj[j] >= 0) {
+                    const int dy = tapj[j] / 3, dx = tapj[j] - 3 * dy;
+                    tma_load_4d(sa + j * WG_BOX, &A.tmx, cj[j], x0 + dx - 1, y0 + dy - 1, img, &full[st]);
+                }
+#pragma unroll
+            for (int j = 0; j < BN / 32; j++) tma_load_4d(sb + j * WG_BOX, &A.tmy, 32 * j, x0, y0, img, &full[st]);
+            (void)bw;
+        }
+    } else if (tid == 32) {
+        constexpr uint32_t IDESC = umma_idesc_f16(TC_BM, BN, true, true) | (1u << 15) | (1u << 16);
+        for (int i = 0; i < nk; i++) {
+            const int st = i % S;
+            if (!mbar_wait(&full[st], (unsigned)((i / S) & 1))) {
+                atomicExch(fail, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a_addr = smem_u32(base + st * T::STAGE), b_addr = a_addr + T::A_BYTES;
+#pragma unroll
+            for (int k = 0; k < WG_K / 16; k++)
+                umma_f16(tmem, umma_sdesc(a_addr + 1024 * k, WG_BOX, 512, 4), umma_sdesc(b_addr + 1024 * k, WG_BOX, 512, 4),
+                         IDESC, i > 0 || k > 0);
+            umma_commit(&empty[st]);
+        }
+        umma_commit(done);
+    }
+    bool ok = mbar_wait(done, 0);
+    if (!ok) ok = mbar_wait(done, 0);
+    tc_fence_after();
+    if (__syncthreads_or(!ok || *reinterpret_cast<volatile int *>(fail))) {
+        if (tid == 0) {
+            if (A.err) atomicExch(A.err, 1);
+            for (int i = 0; i < nk && i < S; i++) mbar_wait(&full[(nk - 1 - i) % S], (unsigned)(((nk - 1 - i) / S) & 1));
+        }
+    } else {
+        const int m = m0 + 32 * warp + lane;
+#pragma unroll
+        for (int c = 0; c < BN; c += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+            if (m < A.M) {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (c + j < A.N) atomicAdd(A.dw + (long long)(c + j) * A.ldc + m, v[j]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, T::NCOLS);
+}
+
+template <int BN>
+int wgrad_tc_launch(WgradArgs &a, int mtiles, int splits, cudaStream_t st)
+{
+    using T = WgCfg<BN>;
+    auto kern = k_wgrad_tc<BN>;
+    static bool attr[RTM_MAX_DEVICES] = {};
+    {
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!attr[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::SMEM));
+            attr[dev] = true;
+        }
+    }
+    kern<<<dim3(mtiles, splits), TC_THREADS, T::SMEM, st>>>(a);
+    RTM_CUDA(cudaGetLastError());
+    return RTM_OK;
+}
+
+// True when k_wgrad_tc covers the weight gradient of a 3x3 layer with input
+// X (Cin channels, channel stride ldx, offset xoff) and output gradient dY
+// (Cout channels, stride ldy) on n images of H x W.
+bool wgrad_tc_fits(int Cin, int ldx, int xoff, const bf16 *X, int Cout, int ldy, const bf16 *dY, int H, int W,
+                   long long P)
+{
+    if (Cin % 32 || Cout % 32 || Cout > 128 || ldx % 8 || xoff % 8 || ldy % 8) return false;
+    if (!(W % WG_K == 0 || WG_K % W == 0) || ((long long)H * W) % WG_K || P % WG_K) return false;
+    if (((uintptr_t)(X + xoff) & 15) || ((uintptr_t)dY & 15)) return false;
+    return tensor_maps_available();
+}
+
+int wgrad_tc(float *dw, long long ldc, int Cin, const bf16 *X, int ldx, int xoff, int Cout, const bf16 *dY, int ldy,
+             int n, int H, int W, int *err, cudaStream_t st)
+{
+    WgradArgs a;
+    memset(&a, 0, sizeof a);
+    a.dw = dw;
+    a.ldc = ldc;
+    a.M = 9 * Cin;
+    a.N = Cout;
+    a.Cin = Cin;
+    a.H = H;
+    a.W = W;
+    a.err = err;
+    const long long P = (long long)n * H * W;
+    a.ksteps = (int)(P / WG_K);
+    const int bw = W < WG_K ? W : WG_K, bh = WG_K / bw;
+    {
+        const long long dims[4] = {Cin, W, H, n};
+        const long long strides[3] = {2LL * ldx, 2LL * ldx * W, 2LL * ldx * W * H};
+        const int box[4] = {32, bw, bh, 1};
+        TRY(make_map_nd(&a.tmx, X + xoff, true, 4, dims, strides, box, 64));
+    }
+    {
+        const long long dims[4] = {Cout, W, H, n};
+        const long long strides[3] = {2LL * ldy, 2LL * ldy * W, 2LL * ldy * W * H};
+        const int box[4] = {32, bw, bh, 1};
+        TRY(make_map_nd(&a.tmy, dY, true, 4, dims, strides, box, 64));
+    }
+    const int mtiles = (a.M + TC_BM - 1) / TC_BM;
+    // K splits: about three CTAs per SM, at least 16 steps each
+    int splits = std::max(1, std::min(a.ksteps / 16, (3 * eg::device_sm_count() + mtiles - 1) / mtiles));
+    a.steps_per_cta = (a.ksteps + splits - 1) / splits;
+    splits = (a.ksteps + a.steps_per_cta - 1) / a.steps_per_cta;
+    switch ((Cout + 31) / 32) {
+    case 1: return wgrad_tc_launch<32>(a, mtiles, splits, st);
+    case 2: return wgrad_tc_launch<64>(a, mtiles, splits, st);
+    case 3: return wgrad_tc_launch<96>(a, mtiles, splits, st);
+    default: return wgrad_tc_launch<128>(a, mtiles, splits, st);
+    }
 }
 
 int g_gemm_tc = 2;  // 2: 3x3 convolutions by bulk-copied tap boxes, other non-transposed GEMMs on k_gemm_tc;
@@ -1369,35 +1622,41 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     // weight gradient: dW^T[kp][coutp] = col^T[kp][P] * gy[P][coutp]
     const In in = layer_input(u, i);
     GemmArgs g;
-    memset(&g, 0, sizeof g);
-    g.err = u->err.p;
-    if (l.ks == 3 && in.c % 32 == 0) {
-        set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
-    } else if (l.ks == 3) {
-        TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
-        g.A = u->col.p;
-        g.lda = l.kp;
+    if (g_gemm_tc == 2 && l.ks == 3 && in.c % 32 == 0 && l.kp == 9 * in.c &&
+        wgrad_tc_fits(in.c, in.ld, in.off, in.p, l.coutp, ldg, gy, l.H, l.W, P)) {
+        TRY(wgrad_tc(u->gw.p + l.woff, l.kp, in.c, in.p, in.ld, in.off, l.coutp, gy, ldg, n, l.H, l.W, u->err.p,
+                     u->st));
     } else {
-        g.A = in.p;
-        g.lda = in.ld;
+        memset(&g, 0, sizeof g);
+        g.err = u->err.p;
+        if (l.ks == 3 && in.c % 32 == 0) {
+            set_implicit(g, in.p, in.ld, in.off, in.c, l.H, l.W);
+        } else if (l.ks == 3) {
+            TRY(im2col(u, n, l.H, l.W, in.c, in.p, in.ld, in.off, l.kp));
+            g.A = u->col.p;
+            g.lda = l.kp;
+        } else {
+            g.A = in.p;
+            g.lda = in.ld;
+        }
+        g.B = gy;
+        g.ldb = ldg;
+        g.M = l.kp;
+        g.N = l.coutp;
+        const long long Kfull = (P + 31) / 32 * 32;
+        RTM_CHECK_ARG(P % 32 == 0, "pixel count %lld of a U-Net layer is not a multiple of 32", P);
+        g.K = (int)Kfull;
+        // split the pixel reduction so that the grid covers the SMs
+        const int tiles = ((g.M + 255) / 256) * ((g.N + 31) / 32);
+        int splits = (int)std::max(1LL, std::min<long long>(Kfull / 256, (4LL * eg::device_sm_count() + tiles - 1) / tiles));
+        long long kc = (Kfull + splits - 1) / splits;
+        kc = (kc + 31) / 32 * 32;
+        splits = (int)((Kfull + kc - 1) / kc);
+        g.kchunk = (int)kc;
+        g.Cf = u->gw.p + l.woff;
+        g.ldc = l.kp;
+        TRY(gemm(g, true, true, EPI_F32_ATOMIC_T, splits, u->st));
     }
-    g.B = gy;
-    g.ldb = ldg;
-    g.M = l.kp;
-    g.N = l.coutp;
-    const long long Kfull = (P + 31) / 32 * 32;
-    RTM_CHECK_ARG(P % 32 == 0, "pixel count %lld of a U-Net layer is not a multiple of 32", P);
-    g.K = (int)Kfull;
-    // split the pixel reduction so that the grid covers the SMs
-    const int tiles = ((g.M + 255) / 256) * ((g.N + 31) / 32);
-    int splits = (int)std::max(1LL, std::min<long long>(Kfull / 256, (4LL * eg::device_sm_count() + tiles - 1) / tiles));
-    long long kc = (Kfull + splits - 1) / splits;
-    kc = (kc + 31) / 32 * 32;
-    splits = (int)((Kfull + kc - 1) / kc);
-    g.kchunk = (int)kc;
-    g.Cf = u->gw.p + l.woff;
-    g.ldc = l.kp;
-    TRY(gemm(g, true, true, EPI_F32_ATOMIC_T, splits, u->st));
     if (!need_dx) return RTM_OK;
     // input gradient: dX[P][cin] = im2col(gy)[P][ktp] * Wt[cin][ktp]^T
     const GIn gin = layer_ginput(u, i);

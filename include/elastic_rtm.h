@@ -401,6 +401,17 @@ int rtm_debug_umma_probe(int N, unsigned lbo, unsigned sbo, const unsigned short
  * K-major layout that bulk tensor copies produce, multiplied by K/16 MMAs
  * whose descriptors advance 32 bytes along K: D = A B^T (128 x N, FP32). */
 int rtm_debug_umma_probe_sw(int N, int K, const unsigned short *A, const unsigned short *B, float *D);
+/* rtm_debug_umma_probe2: layout variants.  mode 0: A ((128+shift) x K,
+ * K = 32 or 64) in the swizzled K-major layout, the descriptor starting
+ * `shift` rows in (base-offset field (start >> 7) & 7 when boff), D = A[shift
+ * .. shift+127] B^T.  mode 1: A (128 x 32) and B (N x 32, N = 64 or 128)
+ * MN-major with the 128-byte swizzle, atoms of 8 K-rows x 64 MN elements
+ * placed lbo apart along MN and sbo apart along K ((4096, 1024) or
+ * (1024, 2048)), D = A B^T.  mode 2: the same with the 64-byte swizzle (atoms
+ * of 8 K-rows x 32 MN elements, N = 32 .. 128, (lbo, sbo) = (2048, 512) or
+ * (512, 2048)). */
+int rtm_debug_umma_probe2(int N, int K, int mode, int shift, int boff, unsigned lbo, unsigned sbo,
+                          const unsigned short *A, const unsigned short *B, float *D);
 
 /* ------------------------------------------ learned image preconditioner
  * (no counterpart in the reference).  A 4-level 3->3 channel U-Net
