@@ -1261,6 +1261,192 @@ __global__ void k_bias_grad(long long P, int C, int ld, const bf16 *g, float *db
     atomicAdd(db + c, s);
 }
 
+// db[c] += sum_p g[p][c] for C % 8 == 0 and 16-byte aligned rows: a thread
+// reads 8 channels of a pixel as one 16-byte word (G = C/8 channel groups,
+// blockDim/G pixels per pass), sums in shared memory, and one atomic per
+// channel and block goes to global memory.
+__global__ void k_bias_grad8(long long P, int C, int ld, const bf16 *g, float *db)
+{
+    __shared__ float red[256];
+    const int G = C >> 3, R = blockDim.x / G, t = threadIdx.x, cg = t % G, r = t / G;
+    for (int i = t; i < C; i += blockDim.x) red[i] = 0.f;
+    __syncthreads();
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (r < R)
+        for (long long p = (long long)blockIdx.x * R + r; p < P; p += (long long)gridDim.x * R) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(g + p * ld + 8 * cg);
+            const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&v);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 f = __bfloat1622float2(h[j]);
+                s[2 * j] += f.x;
+                s[2 * j + 1] += f.y;
+            }
+        }
+    if (r < R)
+#pragma unroll
+        for (int j = 0; j < 8; j++) atomicAdd(&red[8 * cg + j], s[j]);
+    __syncthreads();
+    for (int i = t; i < C; i += blockDim.x) atomicAdd(db + i, red[i]);
+}
+
+// The activation derivative (g *= LEAK where y <= 0, in place) fused with
+// the bias gradient of the masked g (db[c] += sum_p g[p][c]); layout as
+// k_bias_grad8.
+__global__ void k_relu_bias8(long long P, int C, int ld, const bf16 *y, bf16 *g, float *db)
+{
+    __shared__ float red[256];
+    const int G = C >> 3, R = blockDim.x / G, t = threadIdx.x, cg = t % G, r = t / G;
+    for (int i = t; i < C; i += blockDim.x) red[i] = 0.f;
+    __syncthreads();
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (r < R)
+        for (long long p = (long long)blockIdx.x * R + r; p < P; p += (long long)gridDim.x * R) {
+            const long long o = p * ld + 8 * cg;
+            float yv[8], gv[8];
+            unpack8(*reinterpret_cast<const uint4 *>(y + o), yv);
+            unpack8(*reinterpret_cast<const uint4 *>(g + o), gv);
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (!(yv[k] > 0.f)) gv[k] *= LEAK;
+            const uint4 w = pack8(gv);
+            *reinterpret_cast<uint4 *>(g + o) = w;
+            unpack8(w, gv);  // the bias gradient sums the stored (BF16) values
+#pragma unroll
+            for (int k = 0; k < 8; k++) s[k] += gv[k];
+        }
+    if (r < R)
+#pragma unroll
+        for (int j = 0; j < 8; j++) atomicAdd(&red[8 * cg + j], s[j]);
+    __syncthreads();
+    for (int i = t; i < C; i += blockDim.x) atomicAdd(db + i, red[i]);
+}
+
+// The first layer (CIN input channels, 3x3, pad 1) on the CUDA cores: its
+// K = 9 CIN is too small for a tensor-core GEMM to pay for an im2col.
+// Forward: a thread per pixel gathers its 9 CIN inputs once and forms all
+// COUT outputs from the weights in shared memory (BF16 values, exact FP32
+// products, FP32 sums), bias and leaky ReLU fused, BF16 stores.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_conv_first(int n, int H, int W, const bf16 *x, int ldx, const bf16 *w,
+                                                    int kp, const float *bias, bf16 *y, int ldy)
+{
+    __shared__ float sw[COUT][9 * CIN];
+    __shared__ float sb[COUT];
+    for (int i = threadIdx.x; i < COUT * 9 * CIN; i += blockDim.x)
+        sw[i / (9 * CIN)][i % (9 * CIN)] = __bfloat162float(w[(i / (9 * CIN)) * kp + i % (9 * CIN)]);
+    for (int i = threadIdx.x; i < COUT; i += blockDim.x) sb[i] = bias ? bias[i] : 0.f;
+    __syncthreads();
+    const long long P = (long long)n * H * W;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < P; p += (long long)gridDim.x * blockDim.x) {
+        const int xw = (int)(p % W), yh = (int)((p / W) % H);
+        const long long b = p / ((long long)W * H);
+        float acc[COUT];
+#pragma unroll
+        for (int j = 0; j < COUT; j++) acc[j] = sb[j];
+#pragma unroll 1
+        for (int tap = 0; tap < 9; tap++) {
+            const int yy = yh + tap / 3 - 1, xx = xw + tap % 3 - 1;
+            const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+            float in[CIN];
+#pragma unroll
+            for (int c = 0; c < CIN; c++) in[c] = ok ? __bfloat162float(x[((b * H + yy) * W + xx) * ldx + c]) : 0.f;
+#pragma unroll
+            for (int j = 0; j < COUT; j++)
+#pragma unroll
+                for (int c = 0; c < CIN; c++) acc[j] = fmaf(sw[j][tap * CIN + c], in[c], acc[j]);
+        }
+#pragma unroll
+        for (int c0 = 0; c0 < COUT; c0 += 8) {
+            uint4 v;
+            __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float a0 = acc[c0 + 2 * j], a1 = acc[c0 + 2 * j + 1];
+                h[j] = __floats2bfloat162_rn(a0 > 0.f ? a0 : LEAK * a0, a1 > 0.f ? a1 : LEAK * a1);
+            }
+            *reinterpret_cast<uint4 *>(y + p * ldy + c0) = v;
+        }
+    }
+}
+
+// Weight gradient of the first layer: dW[co][k] += sum_p g[p][co] x_k(p)
+// (k = tap * CIN + c).  A block stages 128 pixels' inputs and output
+// gradients in shared memory; thread t < 3 * 8 * 9 owns the 4 x CIN block
+// (co 4b .. 4b+3, tap, c = 0 .. CIN-1) over the pixels pi = t / 72 (mod 3)
+// of each tile, keeping its sums in registers; at the end the three pixel
+// groups are summed in shared memory and added to dW with one atomic each.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_wgrad_first(int n, int H, int W, const bf16 *x, int ldx, const bf16 *g, int ldg,
+                                                     float *dw, int ldw)
+{
+    constexpr int K = 9 * CIN, NP = 128, NB = (COUT / 4) * 9, NG = 3;
+    static_assert(NB * NG <= 256 && COUT % 4 == 0, "blocking");
+    __shared__ float sx[NP][K + 1];
+    __shared__ float sg[NP][COUT + 1];
+    const long long P = (long long)n * H * W;
+    const long long per = (P + gridDim.x - 1) / gridDim.x;
+    const long long q0 = blockIdx.x * per, q1 = min(P, q0 + per);
+    const int t = threadIdx.x, pg = t / NB, ob = t % NB, co0 = 4 * (ob / 9), tap = ob % 9;
+    float acc[4][CIN];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int c = 0; c < CIN; c++) acc[i][c] = 0.f;
+    for (long long p0 = q0; p0 < q1; p0 += NP) {
+        __syncthreads();
+        for (int i = t; i < NP * K; i += blockDim.x) {
+            const int pi = i / K, k = i % K;
+            const long long p = p0 + pi;
+            float v = 0.f;
+            if (p < q1) {
+                const int tp = k / CIN, c = k % CIN;
+                const int xw = (int)(p % W), yh = (int)((p / W) % H);
+                const long long b = p / ((long long)W * H);
+                const int yy = yh + tp / 3 - 1, xx = xw + tp % 3 - 1;
+                if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = __bfloat162float(x[((b * H + yy) * W + xx) * ldx + c]);
+            }
+            sx[pi][k] = v;
+        }
+        for (int i = t; i < NP * COUT; i += blockDim.x) {
+            const int pi = i / COUT, co = i % COUT;
+            const long long p = p0 + pi;
+            sg[pi][co] = p < q1 ? __bfloat162float(g[p * ldg + co]) : 0.f;
+        }
+        __syncthreads();
+        if (pg < NG)
+            for (int pi = pg; pi < NP; pi += NG) {
+                float gv[4], xv[CIN];
+#pragma unroll
+                for (int i = 0; i < 4; i++) gv[i] = sg[pi][co0 + i];
+#pragma unroll
+                for (int c = 0; c < CIN; c++) xv[c] = sx[pi][tap * CIN + c];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int c = 0; c < CIN; c++) acc[i][c] = fmaf(gv[i], xv[c], acc[i][c]);
+            }
+    }
+    // sum the pixel groups (the tiles' shared memory is free now)
+    __syncthreads();
+    float *part = &sx[0][0];  // NG x NB x 4 x CIN floats
+    if (pg < NG)
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < CIN; c++) part[((pg * NB + ob) * 4 + i) * CIN + c] = acc[i][c];
+    __syncthreads();
+    if (t < NB)
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int c = 0; c < CIN; c++) {
+                float v = 0.f;
+                for (int q = 0; q < NG; q++) v += part[((q * NB + ob) * 4 + i) * CIN + c];
+                atomicAdd(dw + (co0 + i) * ldw + tap * CIN + c, v);
+            }
+}
+
 // FP32 NHWC (C channels) -> BF16
 __global__ void k_to_bf16(long long n, const float *x, bf16 *y)
 {
@@ -1509,6 +1695,13 @@ int conv_fwd(unet *u, int i, int n)
     Layer &l = u->L[i];
     const In in = layer_input(u, i);
     const long long P = (long long)n * l.H * l.W;
+    if (g_gemm_tc == 2 && l.ks == 3 && in.c == 3 && in.off == 0 && l.coutp == 32 && l.relu && i != NCONV - 1) {
+        const int ctas = (int)std::min<long long>((P + 255) / 256, 8LL * eg::device_sm_count());
+        k_conv_first<3, 32><<<ctas, 256, 0, u->st>>>(n, l.H, l.W, in.p, in.ld, l.wb.p, l.kp, u->w.p + l.boff, u->a[i].p,
+                                                     l.coutp);
+        RTM_CUDA(cudaGetLastError());
+        return RTM_OK;
+    }
     GemmArgs g;
     memset(&g, 0, sizeof g);
     g.err = u->err.p;
@@ -1612,12 +1805,21 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
     const bool last = i == NCONV - 1;
     bf16 *gy = last ? u->gout.p : u->ga[i].p;
     const int ldg = last ? 32 : l.coutp;
-    if (l.relu) {
-        k_relu_mask8<<<grid_for(P * l.coutp / 8), 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy);
-        RTM_CUDA(cudaGetLastError());
+    const bool vec = l.coutp % 8 == 0 && ldg % 8 == 0 && l.coutp <= 256;
+    const int rb_ctas = (int)std::min<long long>(4LL * eg::device_sm_count(), std::max<long long>(1, P / 64));
+    if (l.relu && vec) {
+        k_relu_bias8<<<rb_ctas, 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy, u->gw.p + l.boff);
+    } else {
+        if (l.relu) {
+            k_relu_mask8<<<grid_for(P * l.coutp / 8), 256, 0, u->st>>>(P, l.coutp, ldg, u->a[i].p, gy);
+            RTM_CUDA(cudaGetLastError());
+        }
+        if (vec)
+            k_bias_grad8<<<rb_ctas, 256, 0, u->st>>>(P, l.coutp, ldg, gy, u->gw.p + l.boff);
+        else
+            k_bias_grad<<<std::min<long long>(1024, std::max<long long>(1, P / 64)), 128, 0, u->st>>>(
+                P, l.coutp, ldg, gy, u->gw.p + l.boff);
     }
-    k_bias_grad<<<std::min<long long>(1024, std::max<long long>(1, P / 64)), 128, 0, u->st>>>(P, l.coutp, ldg, gy,
-                                                                                        u->gw.p + l.boff);
     RTM_CUDA(cudaGetLastError());
     // weight gradient: dW^T[kp][coutp] = col^T[kp][P] * gy[P][coutp]
     const In in = layer_input(u, i);
@@ -1626,6 +1828,10 @@ int conv_bwd(unet *u, int i, int n, bool need_dx)
         wgrad_tc_fits(in.c, in.ld, in.off, in.p, l.coutp, ldg, gy, l.H, l.W, P)) {
         TRY(wgrad_tc(u->gw.p + l.woff, l.kp, in.c, in.p, in.ld, in.off, l.coutp, gy, ldg, n, l.H, l.W, u->err.p,
                      u->st));
+    } else if (g_gemm_tc == 2 && l.ks == 3 && in.c == 3 && in.off == 0 && l.coutp == 32) {
+        k_wgrad_first<3, 32><<<4 * eg::device_sm_count(), 256, 0, u->st>>>(n, l.H, l.W, in.p, in.ld, gy, ldg,
+                                                                          u->gw.p + l.woff, l.kp);
+        RTM_CUDA(cudaGetLastError());
     } else {
         memset(&g, 0, sizeof g);
         g.err = u->err.p;
