@@ -1395,23 +1395,26 @@ __global__ void __launch_bounds__(256) k_wgrad_first(int n, int H, int W, const 
         for (int c = 0; c < CIN; c++) acc[i][c] = 0.f;
     for (long long p0 = q0; p0 < q1; p0 += NP) {
         __syncthreads();
-        for (int i = t; i < NP * K; i += blockDim.x) {
-            const int pi = i / K, k = i % K;
-            const long long p = p0 + pi;
-            float v = 0.f;
-            if (p < q1) {
-                const int tp = k / CIN, c = k % CIN;
-                const int xw = (int)(p % W), yh = (int)((p / W) % H);
-                const long long b = p / ((long long)W * H);
+        // threads 0 .. NP-1 stage the inputs of pixel p0 + t (its coordinates
+        // worked out once), threads NP .. 2 NP-1 its output gradients
+        if (t < NP) {
+            const long long p = p0 + t;
+            const bool in = p < q1;
+            const int xw = in ? (int)(p % W) : 0, yh = in ? (int)((p / W) % H) : 0;
+            const long long b = in ? p / ((long long)W * H) : 0;
+#pragma unroll
+            for (int tp = 0; tp < 9; tp++) {
                 const int yy = yh + tp / 3 - 1, xx = xw + tp % 3 - 1;
-                if (yy >= 0 && yy < H && xx >= 0 && xx < W) v = __bfloat162float(x[((b * H + yy) * W + xx) * ldx + c]);
+                const bool ok = in && yy >= 0 && yy < H && xx >= 0 && xx < W;
+                const bf16 *src = x + ((b * H + yy) * W + xx) * ldx;
+#pragma unroll
+                for (int c = 0; c < CIN; c++) sx[t][tp * CIN + c] = ok ? __bfloat162float(src[c]) : 0.f;
             }
-            sx[pi][k] = v;
-        }
-        for (int i = t; i < NP * COUT; i += blockDim.x) {
-            const int pi = i / COUT, co = i % COUT;
+        } else if (t < 2 * NP) {
+            const int pi = t - NP;
             const long long p = p0 + pi;
-            sg[pi][co] = p < q1 ? __bfloat162float(g[p * ldg + co]) : 0.f;
+#pragma unroll
+            for (int co = 0; co < COUT; co++) sg[pi][co] = p < q1 ? __bfloat162float(g[p * ldg + co]) : 0.f;
         }
         __syncthreads();
         if (pg < NG)
