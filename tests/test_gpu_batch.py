@@ -215,13 +215,15 @@ def test_batch_tma_staging_is_bit_identical(tile, stages, interval):
     assert np.abs(ref).max() > 0
 
 
-@pytest.mark.parametrize("nz,nx,nt,interval", [(40, 180, 60, 0), (300, 900, 40, 0), (700, 700, 40, 7)])
+@pytest.mark.parametrize("nz,nx,nt,interval", [(40, 180, 60, 0), (300, 900, 40, 0), (700, 700, 40, 7), (280, 900, 40, 0),
+                                                (800, 700, 40, 7)])
 def test_batch_marching_kernels_match_tile_kernels(nz, nx, nt, interval):
     """The passes by the marching kernels (one CTA per SM walking 128-row
     strips in 8-column chunks through rings of staged columns and adjoint
     products): the forward gives the tile kernel's images bit for bit, the
     adjoint agrees to rounding; one strip narrower than the grid of CTAs,
-    several strips with a partial last one, checkpoint-restart mode; the
+    several strips with a partial last one, thin last strips (24 and 32
+    rows) that the adjoint marches in bands, checkpoint-restart mode; the
     autotuner times them beside the tile variants."""
     dx, dt, fp, abc, zs, zr, ns = 10.0, 1e-3, 30.0, 20 if nz > 100 else 10, 8, 8, 20
     wmin, wmax, spacing = (50, 96, 24) if nx < 300 else (150, 400, 200)
