@@ -126,6 +126,88 @@ __global__ void __launch_bounds__(256) k_k3_step(const __grid_constant__ K3Args 
     k3_field<EXACT, 8>(a, p, st);
 }
 
+// Paired form (nz even, 8-byte aligned planes): a thread owns the padded z
+// positions 2m and 2m+1 (cells where they are interior) and reads every
+// tap as an 8-byte pair -- the same offset serves both cells along x and y;
+// along z the two cells' 10 taps fall in 11 consecutive positions, six
+// aligned pairs.  Each cell's sum keeps the reference's order and
+// roundings, so the results equal the scalar kernel's bit for bit.
+template <bool EXACT, int O>
+__device__ __forceinline__ void k3_field2(const K3Args &a, long long p, const long long st[3], bool ok0, bool ok1)
+{
+    const float2 o2 = *reinterpret_cast<const float2 *>(a.out[O] + p);
+    const float2 i2 = __ldg(reinterpret_cast<const float2 *>(a.in1[O] + p));
+    float acc0 = EXACT ? __fadd_rn(o2.x, i2.x) : o2.x + i2.x;
+    float acc1 = EXACT ? __fadd_rn(o2.y, i2.y) : o2.y + i2.y;
+#pragma unroll
+    for (int g = 0; g < K3_NG[O]; g++) {
+        const K3G q = K3_GROUPS[O][g];
+        const float *mm = a.m[q.coef], *ff = a.in[q.field];
+        if (q.axis == AX_Z) {
+            // positions p + q.first - 1 .. p + q.first + 10 (6 aligned pairs
+            // from the even position at or below p + q.first - 1)
+            const int lo = q.first == -5 ? -6 : -4;
+            float mv[12], fv[12];
+#pragma unroll
+            for (int i = 0; i < 6; i++) {
+                const float2 m2 = __ldg(reinterpret_cast<const float2 *>(mm + p + lo + 2 * i));
+                const float2 f2 = __ldg(reinterpret_cast<const float2 *>(ff + p + lo + 2 * i));
+                mv[2 * i] = m2.x; mv[2 * i + 1] = m2.y;
+                fv[2 * i] = f2.x; fv[2 * i + 1] = f2.y;
+            }
+            const int b0 = q.first - lo;  // index of cell 0's first tap
+#pragma unroll
+            for (int t = 0; t < 10; t++) {
+                const float c = a.c[t < 5 ? t : 9 - t];
+                acc0 = k3_term<EXACT>(acc0, mv[b0 + t], c, fv[b0 + t], t < 5);
+                acc1 = k3_term<EXACT>(acc1, mv[b0 + t + 1], c, fv[b0 + t + 1], t < 5);
+            }
+        } else {
+            const long long s = st[q.axis];
+#pragma unroll
+            for (int t = 0; t < 10; t++) {
+                const long long pp = p + (q.first + t) * s;
+                const float2 m2 = __ldg(reinterpret_cast<const float2 *>(mm + pp));
+                const float2 f2 = __ldg(reinterpret_cast<const float2 *>(ff + pp));
+                const float c = a.c[t < 5 ? t : 9 - t];
+                acc0 = k3_term<EXACT>(acc0, m2.x, c, f2.x, t < 5);
+                acc1 = k3_term<EXACT>(acc1, m2.y, c, f2.y, t < 5);
+            }
+        }
+    }
+    if (ok0 && ok1)
+        *reinterpret_cast<float2 *>(a.out[O] + p) = make_float2(acc0, acc1);
+    else if (ok0)
+        a.out[O][p] = acc0;
+    else if (ok1)
+        a.out[O][p + 1] = acc1;
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) k_k3_step2(const __grid_constant__ K3Args a)
+{
+    // padded z pairs 2m, 2m+1 for m = 2 .. (nz + 10) / 2 - 3 cover the interior [5, nz + 5)
+    const int m = 2 + blockIdx.x * 32 + threadIdx.x, ix = blockIdx.y * 4 + threadIdx.y,
+              iy = blockIdx.z * 2 + threadIdx.z;
+    const int zp = 2 * m;
+    if (zp >= a.nz + 5 || ix >= a.nx || iy >= a.ny) return;
+    const bool ok0 = zp >= 5, ok1 = zp + 1 < a.nz + 5;
+    const long long sx = a.nz + 10, sy = (long long)(a.nz + 10) * (a.nx + 10);
+    const long long st[3] = {1, sx, sy};
+    const long long p = (iy + 5) * sy + (ix + 5) * sx + zp;
+    k3_field2<EXACT, 0>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 1>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 2>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 3>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 4>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 5>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 6>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 7>(a, p, st, ok0, ok1);
+    k3_field2<EXACT, 8>(a, p, st, ok0, ok1);
+}
+
+int g_k3_paired = 1;  // 1: the paired form where nz is even and planes are 8-byte aligned
+
 void k3_coefs(float c[5])
 {
     c[0] = (float)(35.0 / 294912.0);
@@ -150,11 +232,24 @@ int k3_launch(int ny, int nz, int nx, const float *const *in, const float *const
     a.nz = nz;
     a.nx = nx;
     k3_coefs(a.c);
-    const dim3 block(32, 4, 2), grid((nz + 31) / 32, (nx + 3) / 4, (ny + 1) / 2);
-    if (exact)
-        k_k3_step<true><<<grid, block, 0, st>>>(a);
-    else
-        k_k3_step<false><<<grid, block, 0, st>>>(a);
+    bool paired = g_k3_paired && nz % 2 == 0;
+    for (int i = 0; i < 9 && paired; i++) paired = !((uintptr_t)in[i] & 7) && !((uintptr_t)in1[i] & 7) && !((uintptr_t)out[i] & 7);
+    for (int i = 0; i < 6 && paired; i++) paired = !((uintptr_t)m[i] & 7);
+    const dim3 block(32, 4, 2);
+    if (paired) {
+        const int pairs = (nz + 10) / 2 - 4;  // m = 2 .. (nz + 10)/2 - 3
+        const dim3 grid((pairs + 31) / 32, (nx + 3) / 4, (ny + 1) / 2);
+        if (exact)
+            k_k3_step2<true><<<grid, block, 0, st>>>(a);
+        else
+            k_k3_step2<false><<<grid, block, 0, st>>>(a);
+    } else {
+        const dim3 grid((nz + 31) / 32, (nx + 3) / 4, (ny + 1) / 2);
+        if (exact)
+            k_k3_step<true><<<grid, block, 0, st>>>(a);
+        else
+            k_k3_step<false><<<grid, block, 0, st>>>(a);
+    }
     RTM_CUDA(cudaGetLastError());
     return RTM_OK;
 }
