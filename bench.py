@@ -900,6 +900,89 @@ def run_elastic3d(args):
     print(json.dumps(elastic3d_block(args, args.steps, args.warmup, args.n3)), flush=True)
 
 
+# --------------------------------------------------------------- PML Born modelling
+PML_BYTES = 332  # algorithmic bytes per cell and level: background 35 planes, scattered 48
+
+
+def pml_block(args, steps=3, warmup=3, Tt=0.5, cpu_levels=12):
+    """The reference's split-field PML Born modelling program
+    (working_Src/born.f90: background and scattered wavefields, 20 split
+    planes each, PML 60 cells wide, Ricker source, receiver lines, two
+    snapshots) on the 2000 x 800 survey grid, dx = 10 m, Ttime = 0.5 s
+    (nt = 707 levels); model resident in HBM, exact arithmetic (bit-identical
+    to the reference's CPU execution).  A step is one whole modelling run."""
+    import torch
+    from elastic_gb300 import pml
+    nz, nx, abc = 800, 2000, 60
+    rng = np.random.default_rng(5)
+    z = np.arange(nz)[None, :]
+    vp = (np.where(z < nz // 3, 2000.0, np.where(z < 2 * nz // 3, 2600.0, 3200.0)) * np.ones((nx, 1))
+          * (1 + 0.02 * rng.standard_normal((nx, nz)))).astype(np.float32)
+    vs = (vp / 1.73).astype(np.float32)
+    rho = (310.0 * vp.astype(np.float64) ** 0.25).astype(np.float32)
+    dvp, dvs = (0.1 * vp).astype(np.float32), (0.1 * vs).astype(np.float32)
+    drho = (rho * rng.uniform(0.01, 0.05, (nx, nz))).astype(np.float32)
+    model = [vp, vs, rho, dvp, dvs, drho]
+    P = pml.params(10.0, Tt, fp=25.0)
+    nt, nseis, nsnap = P["nt"], P["nseis"], 2
+    kw = dict(dx=10.0, dt=P["dt"], nt=nt, xsource=nx // 2, zsource=70, nsource=P["nsource"], fp=25.0, abc=abc,
+              zrec=70)
+    dev = [torch.from_numpy(a).cuda() for a in model]
+    seis = [torch.empty((nx - 2 * abc, nseis), device="cuda") for _ in range(6)]
+    snap = [torch.empty((nsnap, nx, nz), device="cuda") for _ in range(6)]
+    for _ in range(warmup):
+        pml.born_dev(dev, seis, snap, **kw)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        ev0.record()
+        for _ in range(steps):
+            pml.born_dev(dev, seis, snap, **kw)
+        ev1.record()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    launches = pml.launches()
+    cells = nz * nx * nt
+    rate = cells / (ms * 1e-3) / 1e9
+    peak, kind = measured_peaks()
+    te = time.perf_counter()
+    pml.born(*model, nsnap=nsnap, nseis=nseis, **kw)
+    e2e_s = time.perf_counter() - te
+    del dev, seis, snap
+    torch.cuda.empty_cache()
+    out = {"metric": "Gcell-updates/s (PML Born modelling, background + scattered)", "value": round(rate, 3),
+           "unit": "Gcell/s", "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "split-field PML Born modelling, 2000 x 800 cells, 60-cell PML, nt = %d, "
+                                  "2 snapshots, exact arithmetic" % nt, "inputs_vs_l2": "inputs larger than L2"},
+           "e2e": {"value": round(cells / e2e_s / 1e9, 3), "unit": "Gcell/s",
+                   "h2d_bytes_per_step": 6 * 4 * nz * nx,
+                   "d2h_bytes_per_step": 4 * 6 * ((nx - 2 * abc) * nseis + nsnap * nz * nx)},
+           "gpu_launches": steps * launches,
+           "roofline": {"bound": "hbm", "achieved": round(rate * PML_BYTES, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(rate * PML_BYTES / peak, 4), "peak_kind": kind,
+                        "kernel": "k_pml_step (332 algorithmic B per cell and level: background reads 25 planes "
+                                  "and 5 coefficients, writes 10; scattered reads 28 planes and 10 coefficients, "
+                                  "writes 10)", "traffic": None},
+           "clocks": clk.summary()}
+    if not args.no_cpu:
+        # the oracle (C restatement, all host threads) on the first levels
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        kc = dict(kw, nt=cpu_levels)
+        t0 = time.perf_counter()
+        O.pml_born(*model, nsnap=1, nseis=nseis, **kc)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nz * nx * cpu_levels / cs / 1e9, 4), "unit": "Gcell/s",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": "the oracle's restatement on the same grid, first %d levels" % cpu_levels}
+    return out
+
+
+def run_pml(args):
+    print(json.dumps(pml_block(args, steps=args.steps, warmup=args.warmup)), flush=True)
+
+
 # --------------------------------------------------------------- config 5 sample
 def c5_block(args, warmup=1, steps=1):
     """One 4-shot group of the 256-shot survey (6000 x 2000 cells, dx=5 m,
@@ -972,6 +1055,7 @@ def run_default(args):
             sec = {}
             sec["acoustic3d"] = acoustic3d_block(args, steps=3, warmup=3)
             sec["elastic3d"] = elastic3d_block(args, steps=10, warmup=3, n=384)
+            sec["pml_born"] = pml_block(args)
             sec["rtm2d_256shot_group"] = c5_block(args)
             sec["precond"] = precond_block(args, steps=100, warmup=5, pairs=args.sec_pairs,
                                            train_steps=args.sec_train_steps, ntest=2)
@@ -993,7 +1077,7 @@ def main():
     ap.add_argument("--group", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--tune-steps", type=int, default=20)
-    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond", "unet", "elastic3d"])
+    ap.add_argument("--workload", default="rtm2d", choices=["rtm2d", "rtm2d_c5", "acoustic3d", "precond", "unet", "elastic3d", "pml"])
     ap.add_argument("--pairs", type=int, default=None, help="training pairs of the precond workload")
     ap.add_argument("--train-steps", type=int, default=None, help="Adam steps of the precond workload")
     ap.add_argument("--staging", default="tma", choices=["cpasync", "tma"], help="step-kernel tile staging")
@@ -1026,6 +1110,8 @@ def main():
         run_unet(args)
     elif args.workload == "elastic3d":
         run_elastic3d(args)
+    elif args.workload == "pml":
+        run_pml(args)
     elif args.workload == "precond":
         run_precond(args)
     elif args.workload == "rtm2d":

@@ -294,6 +294,35 @@ int rtm3d_set_exact(int exact);
 int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *const *in1, float *const *out,
                    const float *const *m, int exact);
 
+/* -------------------------------------------- split-field PML Born modelling
+ * The reference's PML Born modelling program (2d_rtm_restart/working_Src/
+ * born.f90 -> born_mod's elastic_init + elastic_op, born-mod.f90:32-78):
+ * background and scattered wavefields with split-field PML (pml-mod.f90),
+ * Ricker source at (zsource, xsource), receiver lines at row zrec, nsnap
+ * snapshots.  Arguments are elastic_init's and elastic_op's (dz is unused
+ * by the reference and omitted); grid indices are 1-based; planes are
+ * Fortran-ordered (nz, nx).  nt, dt, nsource and nseis are derived by the
+ * caller as the reference's main program does (born.f90:67-73, 251, 255).
+ * lame = 0: vp0, vs0, rho0 / dvp, dvs, drho are velocities and densities;
+ * lame = 1: vp0, vs0 hold lambda, mu (and dvp, dvs their perturbations).
+ * seis[6] = Vx, Vz, P, Vx_b, Vz_b, P_b receiver lines (nseis, nx - 2 abc);
+ * snap[6] the same six as (nz, nx, nsnap) cubes.  Every output is fully
+ * written; cells the reference never sets are zero.  Requires nz, nx >= 11,
+ * 1 <= nsnap <= nt, 0 <= abc <= min(nz, nx), 2 <= zrec <= nz.  Bit-identical
+ * to the reference's CPU execution.
+ * pml_born_c_: host arrays.  pml_born_dev: model[6] = vp0, vs0, rho0, dvp,
+ * dvs, drho and the outputs are device pointers, work on `stream` (a
+ * cudaStream_t, NULL for the default stream); returns without waiting.
+ * pml_born_launches: kernels launched by the last call. */
+int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsource, int zsource, int nsource, float fp, int nsnap,
+                int nseis, int abc, int zrec, int free_surface, int lame, const float *vp0, const float *vs0,
+                const float *rho0, const float *dvp, const float *dvs, const float *drho, float *const *seis,
+                float *const *snap);
+int pml_born_dev(int nz, int nx, int nt, float dx, float dt, int xsource, int zsource, int nsource, float fp, int nsnap,
+                 int nseis, int abc, int zrec, int free_surface, int lame, const float *const *model,
+                 float *const *seis, float *const *snap, void *stream);
+long long pml_born_launches(void);
+
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the
  * shots of a survey, each on its own subgrid [x0, x0+nxs) of the full model

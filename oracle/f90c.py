@@ -410,9 +410,9 @@ def parse_decl(text, storage):
     return out
 
 
-def parse_files(src_dir):
+def parse_files(src_dir, files=MODULE_FILES):
     modules = {}
-    for fname in MODULE_FILES:
+    for fname in files:
         path = os.path.join(src_dir, fname)
         stmts = read_statements(path)
         parse_module_file(stmts, path, modules)
@@ -622,8 +622,10 @@ def parse_stmt(s, mod, no):
 
 # --------------------------------------------------------------------------- code generation
 class Gen:
-    def __init__(self, modules):
+    def __init__(self, modules, hooks=None, header="ref90.h"):
         self.mods = modules
+        self.hooks = HOOKS if hooks is None else hooks
+        self.header = header
         self.needed = []
         self.seen = set()
         self.tmp = 0
@@ -711,7 +713,7 @@ class Gen:
             s = self.lookup_var(proc, e[1])
             if s is not None:
                 return s.typ
-            if e[1] in ("exp", "sqrt", "abs", "sin", "cos", "min", "max"):
+            if e[1] in ("exp", "log", "sqrt", "abs", "sin", "cos", "min", "max"):
                 return self.etype(e[2][0], proc)
             if e[1] in ("mod", "int", "nint"):
                 return "int"
@@ -812,7 +814,10 @@ class Gen:
                 return self.elem(s, subs)
             name, args = e[1], e[2]
             ca = [self.cexpr(a, proc, loop) for a in args]
-            if name in ("exp", "sqrt", "abs", "sin", "cos"):
+            if name == "nint":
+                ty = self.etype(args[0], proc)
+                return "((int)lround%s(%s))" % ("f" if ty == "real" else "", ca[0])
+            if name in ("exp", "log", "sqrt", "abs", "sin", "cos"):
                 ty = self.etype(args[0], proc)
                 fn = {"abs": "fabs"}.get(name, name)
                 if ty == "int" and name == "abs":
@@ -940,7 +945,7 @@ class Gen:
                 raise F90Error("unknown subroutine %s called from %s" % (name, proc.name))
             self.require(callee)
             pre = []
-            hook = HOOKS.get((proc.name, name))
+            hook = self.hooks.get((proc.name, name))
             if hook:
                 pre = [pad + "%s();" % hook]
             return pre + [pad + "%s(%s);" % (callee.cname, ", ".join(self.actuals(proc, callee, args)))]
@@ -1133,7 +1138,7 @@ class Gen:
             if not p.bind:
                 bodies[(p.module.name, p.name)] = self.proc_body(p)
             i += 1
-        out = [C_PRELUDE]
+        out = [C_PRELUDE.replace('"ref90.h"', '"%s"' % self.header)]
         # module variables
         for mod in self.mods.values():
             for s in mod.syms.values():
@@ -1142,7 +1147,8 @@ class Gen:
                 else:
                     init = self.const_init(s, mod)
                     out.append("static %s %s = %s;" % (CTYPE[s.typ], s.cname, init))
-        out.append("void ref90_hook_forward(void);")
+        for h in sorted(set(self.hooks.values())):
+            out.append("void %s(void);" % h)
         for p in self.needed:
             if p.bind:
                 out.append("extern " + self.proto(p) + ";")
@@ -1212,20 +1218,60 @@ void F_rtm_mod_adj_rtm_op2(int *a_adj, rarr a_dm1_in, rarr a_dm2_in, rarr a_dm3_
 """
 
 
+# The split-field PML Born modelling program of 2d_rtm_restart/working_Src
+# (born.f90 -> born-mod.f90 with bornlib-mod.f90, pml-mod.f90, source-mod.f90,
+# seis-mod-born.f90, snap-mod-born.f90).  born-mod.f90:521-545 calls
+# explosive_sourcex/explosive_sourcez with six arguments, while
+# source-mod.f90:77-100 defines them with four; pml_source_shim.f90 (beside
+# this script) supplies the six-argument forms with the four-argument bodies.
+PML_FILES = ["source-mod.f90", "seis-mod-born.f90", "bornlib-mod.f90", "snap-mod-born.f90", "pml-mod.f90",
+             "born-mod.f90"]
+PML_ENTRIES = [("born_mod", "elastic_init"), ("born_mod", "elastic_op")]
+PML_SHIM = "pml_source_shim.f90"
+
+H_PML = r"""/* Descriptors of the translated reference PML Born modules (test infrastructure). */
+#ifndef REFPML_H
+#define REFPML_H
+typedef struct { float *p; long n[3]; } rarr;
+typedef struct { double *p; long n[3]; } darr;
+typedef struct { int *p; long n[3]; } iarr;
+struct ref90_var { const char *name; rarr *arr; };
+extern const struct ref90_var ref90_vars[];
+#endif
+"""
+
+
+def load_pml(src_dir):
+    mods = parse_files(src_dir, PML_FILES)
+    shim = {}
+    here = os.path.dirname(os.path.abspath(__file__))
+    parse_module_file(read_statements(os.path.join(here, PML_SHIM)), os.path.join(here, PML_SHIM), shim)
+    src = mods["source_mod"]
+    for name, proc in shim["source_shim"].procs.items():
+        proc.module = src
+        src.procs[name] = proc
+    return mods
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--src", required=True, help="directory of the reference's Fortran modules")
     ap.add_argument("--out", required=True, help="output directory")
+    ap.add_argument("--set", default="rtm", choices=["rtm", "pml"],
+                    help="rtm: Src_working's RTM modules; pml: working_Src's PML Born modelling modules")
     a = ap.parse_args()
-    mods = parse_files(a.src)
-    g = Gen(mods)
-    text = g.generate(ENTRIES)
+    if a.set == "rtm":
+        mods, entries, hooks, base, header = parse_files(a.src), ENTRIES, HOOKS, "ref90", H_TEXT
+    else:
+        mods, entries, hooks, base, header = load_pml(a.src), PML_ENTRIES, {}, "refpml", H_PML
+    g = Gen(mods, hooks, base + ".h")
+    text = g.generate(entries)
     os.makedirs(a.out, exist_ok=True)
-    with open(os.path.join(a.out, "ref90.c"), "w") as f:
+    with open(os.path.join(a.out, base + ".c"), "w") as f:
         f.write(text)
-    with open(os.path.join(a.out, "ref90.h"), "w") as f:
-        f.write(H_TEXT)
-    print("ref90: %d procedures translated" % sum(1 for p in g.needed if not p.bind), file=sys.stderr)
+    with open(os.path.join(a.out, base + ".h"), "w") as f:
+        f.write(header)
+    print("%s: %d procedures translated" % (base, sum(1 for p in g.needed if not p.bind)), file=sys.stderr)
 
 
 if __name__ == "__main__":

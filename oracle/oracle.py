@@ -437,3 +437,112 @@ def k3_reference_check(binary=K3_CHECK, plant=False, timeout=600):
         env["K3_PLANT"] = "1"
     r = subprocess.run([binary], capture_output=True, text=True, env=env, timeout=timeout)
     return r.stderr
+
+
+# ------------------------------------------------------------------ PML Born modelling (working_Src)
+REFPML_PATH = os.path.join(HERE, "_ref", "librefpml.so")
+_refpml = None
+PML_SEIS = ("Vx", "Vz", "P", "Vx_b", "Vz_b", "P_b")
+
+
+def pml_params(nz, nx, dx, Tt, fp=25.0, dtseis=0.002):
+    """nt, dt, nsource and nseis as the reference's main program derives them
+    (working_Src/born.f90:67-73, 251, 255): dt = 0.2 dx / (sqrt(2) 2000)."""
+    F = np.float32
+    dt = F(F(F(0.2) * F(dx)) / F(F(np.sqrt(F(2.0))) * F(2000.0)))
+    nseis = int(F(F(Tt) / F(dtseis)) + F(1))
+    nt = int(F(F(Tt) / dt))
+    x = F(F(F(F(np.sqrt(F(6.0))) / F(3.14159265)) / F(fp)) / dt)
+    nsource = 4 * int(np.floor(x + 0.5))  # NINT: halves away from zero
+    return {"nt": nt, "dt": float(dt), "nsource": nsource, "nseis": nseis}
+
+
+def refpml_available():
+    return os.path.exists(REFPML_PATH) or ref_root() is not None
+
+
+def refpml():
+    """The reference's PML Born modules translated to C (f90c.py --set pml),
+    driven like its main program (refpml_driver.c)."""
+    global _refpml
+    if _refpml is None:
+        if not os.path.exists(REFPML_PATH):
+            build(ref=True)
+        _refpml = ctypes.CDLL(REFPML_PATH)
+    return _refpml
+
+
+def _pml_call(fn, vp0, vs0, rho0, dvp, dvs, drho, dx, dt, nt, xsource, zsource, nsource, fp, nsnap, nseis, abc,
+              zrec, free_surface, lame):
+    nx, nz = vp0.shape
+    m = [np.array(x, np.float32, order="C") for x in (vp0, vs0, rho0, dvp, dvs, drho)]
+    seis = [np.zeros((nx - 2 * abc, nseis), np.float32) for _ in range(6)]
+    snap = [np.zeros((nsnap, nx, nz), np.float32) for _ in range(6)]
+    S = (ctypes.c_void_p * 6)(*[_p(a).value for a in seis])
+    C = (ctypes.c_void_p * 6)(*[_p(a).value for a in snap])
+    F = ctypes.c_float
+    st = fn(nz, nx, nt, F(dx), F(dt), xsource, zsource, nsource, F(fp), nsnap, nseis, abc, zrec, int(free_surface),
+            int(lame), *[_p(x) for x in m], S, C)
+    return st, seis, snap
+
+
+def refpml_born(vp0, vs0, rho0, dvp, dvs, drho, dx, dt, nt, xsource, zsource, nsource, fp, nsnap, nseis, abc, zrec,
+                free_surface=False, lame=False):
+    """elastic_init + elastic_op of the reference's PML Born modelling
+    program (working_Src/born.f90:282-293), float32.  Model planes [nx, nz];
+    grid indices 1-based.  Returns (seis, snap): six receiver lines
+    [nx-2abc, nseis] (Vx, Vz, P, then the scattered Vx_b, Vz_b, P_b) and six
+    snapshot cubes [nsnap, nx, nz]."""
+    st, seis, snap = _pml_call(refpml().refpml_born, vp0, vs0, rho0, dvp, dvs, drho, dx, dt, nt, xsource, zsource,
+                               nsource, fp, nsnap, nseis, abc, zrec, free_surface, lame)
+    if st != 0:
+        raise RuntimeError("reference elastic_op returned %d" % st)
+    return seis, snap
+
+
+def pml_born(vp0, vs0, rho0, dvp, dvs, drho, dx, dt, nt, xsource, zsource, nsource, fp, nsnap, nseis, abc, zrec,
+             free_surface=False, lame=False):
+    """The oracle's restatement of the same program (pml2d.c); same
+    arguments and results as refpml_born."""
+    L = lib()
+    L.ora_pml_born.restype = None
+    _, seis, snap = _pml_call(L.ora_pml_born, vp0, vs0, rho0, dvp, dvs, drho, dx, dt, nt, xsource, zsource, nsource,
+                              fp, nsnap, nseis, abc, zrec, free_surface, lame)
+    return seis, snap
+
+
+def pml_model(vp0, vs0, rho0, dvp, dvs, drho, dx, dt, lame=False):
+    """The program's model set-up (born-mod.f90:331-389): rho_Vx, rho_Vz, l,
+    mi, l2mi, dl, dmi, dl2mi, drho_Vx, drho_Vz as [nx, nz] planes."""
+    nx, nz = vp0.shape
+    m = [np.array(x, np.float32, order="C") for x in (vp0, vs0, rho0, dvp, dvs, drho)]
+    C = [np.zeros((nx, nz), np.float32) for _ in range(10)]
+    Cp = (ctypes.c_void_p * 10)(*[_p(a).value for a in C])
+    lib().ora_pml_model(nz, nx, ctypes.c_float(dx), ctypes.c_float(dt), int(lame), *[_p(x) for x in m], Cp)
+    return C
+
+
+PML_TABLES = ("pml0_xl", "pml0_xr", "pml1_xl", "pml1_xr", "pml0_zt", "pml0_zb", "pml1_zt", "pml1_zb")
+
+
+def pml_tables(vp0, dx, dt, abc, free_surface=False):
+    """The oracle's PML factor tables (pml-mod.f90:23-89) in PML_TABLES
+    order: x tables [abc, nz], z tables [nx, abc] (Fortran (nz, abc) and
+    (abc, nx))."""
+    nx, nz = vp0.shape
+    vp = np.ascontiguousarray(vp0, np.float32)
+    out = [np.zeros((abc, nz), np.float32) for _ in range(4)] + [np.zeros((nx, abc), np.float32) for _ in range(4)]
+    P = (ctypes.c_void_p * 8)(*[_p(a).value for a in out])
+    lib().ora_pml_tables(nz, nx, ctypes.c_float(dx), ctypes.c_float(dt), abc, _p(vp), int(free_surface), P)
+    return out
+
+
+def refpml_get(name, shape):
+    """A module array of the translated reference after a refpml_born call."""
+    r = refpml()
+    r.refpml_get.restype = ctypes.c_long
+    out = np.zeros(shape, np.float32)
+    n = r.refpml_get(name.encode(), _p(out), ctypes.c_long(out.size))
+    if n != out.size:
+        raise ValueError("%s holds %d values, %d expected" % (name, n, out.size))
+    return out

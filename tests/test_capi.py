@@ -62,3 +62,11 @@ def test_argument_checks_before_device_work(lib):
     assert lib.rtm_batch_set_tma(None, 1) == 1
     assert lib.rtm_batch_set_stages(None, 1, 1, 256, 256) == 1
     assert lib.rtm_batch_set_checkpoint(None, 4) == 1
+    # PML Born modelling: geometry checked before any device work
+    P6 = (ctypes.c_void_p * 6)(*[p] * 6)
+    for bad in [dict(nz=8), dict(nsnap=0), dict(abc=40), dict(zrec=1), dict(xsource=0)]:
+        g = dict(nz=40, nx=40, nt=10, xsource=20, zsource=10, nsource=20, nsnap=2, nseis=5, abc=5, zrec=8)
+        g.update(bad)
+        st = lib.pml_born_c_(g["nz"], g["nx"], g["nt"], 10.0, 1e-3, g["xsource"], g["zsource"], g["nsource"], 25.0,
+                             g["nsnap"], g["nseis"], g["abc"], g["zrec"], 0, 0, *[p] * 6, P6, P6)
+        assert st == 1, bad
