@@ -913,6 +913,7 @@ def pml_block(args, steps=3, warmup=3, Tt=0.5, cpu_levels=12):
     to the reference's CPU execution).  A step is one whole modelling run."""
     import torch
     from elastic_gb300 import pml
+    pml.set_kernel(args.pml_kernel)
     nz, nx, abc = 800, 2000, 60
     rng = np.random.default_rng(5)
     z = np.arange(nz)[None, :]
@@ -954,7 +955,8 @@ def pml_block(args, steps=3, warmup=3, Tt=0.5, cpu_levels=12):
            "unit": "Gcell/s", "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "split-field PML Born modelling, 2000 x 800 cells, 60-cell PML, nt = %d, "
-                                  "2 snapshots, exact arithmetic" % nt, "inputs_vs_l2": "inputs larger than L2"},
+                                  "2 snapshots, exact arithmetic" % nt, "inputs_vs_l2": "inputs larger than L2",
+                      "kernel": args.pml_kernel},
            "e2e": {"value": round(cells / e2e_s / 1e9, 3), "unit": "Gcell/s",
                    "h2d_bytes_per_step": 6 * 4 * nz * nx,
                    "d2h_bytes_per_step": 4 * 6 * ((nx - 2 * abc) * nseis + nsnap * nz * nx)},
@@ -1087,6 +1089,9 @@ def main():
     ap.add_argument("--gemm", default="tma", choices=["tma", "tc", "mma"],
                     help="U-Net GEMMs of the forward and backward-data passes: tcgen05 with bulk-copied "
                          "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")
+    ap.add_argument("--pml-kernel", default="cell-prefetch",
+                    choices=["rows4", "cell", "rows4-prefetch", "cell-prefetch", "tile", "tile-prefetch"],
+                    help="PML Born step kernel form")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")
     ap.add_argument("--no-secondary", action="store_true", help="skip the secondary workload blocks")

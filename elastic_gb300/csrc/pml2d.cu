@@ -14,16 +14,22 @@
 // The background wavefield carries the Ricker source; the scattered one adds
 // the Born terms S1..S8 built from the background's new and current levels.
 //
-// Layout in HBM: Fortran-ordered (nz, nx) planes, z fastest, leading
-// dimension nz: the 6 model planes, 10 coefficient planes (rho_Vx, rho_Vz,
-// l, mi, l2mi, dl, dmi, dl2mi, drho_Vx, drho_Vz), 2 wavefields x 3 levels x
-// 10 parts, the PML tables (nz x abc per x side, abc x nx per z side; pml0
-// and pml1), the receiver lines and the snapshot cubes.  Levels rotate by
-// pointer.
+// Layout in HBM: the caller's model planes and outputs are Fortran-ordered
+// (nz, nx), z fastest.  The working planes -- 10 coefficient planes
+// (rho_Vx, rho_Vz, l, mi, l2mi, dl, dmi, dl2mi, drho_Vx, drho_Vz) and
+// 2 wavefields x 3 levels x 10 parts -- are padded: column ix starts 32
+// guard rows before row 1 and is ldz (a multiple of 32, >= nz + 44) floats
+// long, so that row 1 starts a 128-byte line, every 4-row group starts on a
+// 16-byte boundary and the aligned 20-row window of a z-stencil stays inside
+// its column; guard rows stay zero.  Then the PML tables (nz x abc per x side, abc x nx per z side;
+// pml0 and pml1).  Levels rotate by pointer.
 //
-// Kernels: one thread per cell, 32 (z) x 8 (x) blocks, every tap a
-// read-only load served by L1/L2.  One launch advances the background, one
-// the scattered wavefield (it needs the background's new level at its
+// Kernels: each thread owns 4 consecutive rows of one column (blocks of
+// 32 x 8 threads: 128 rows x 8 columns), reads a stencil's taps as 16-byte
+// words through L1 (10 per x-stencil and 5 per z-stencil for its 4 cells),
+// and evaluates each distinct stencil of a field once (D and F share one,
+// E and G, S3 and S5, S4 and S6 too).  One launch advances the background,
+// one the scattered wavefield (it needs the background's new level at its
 // neighbours); receiver lines and snapshots are separate small launches on
 // the levels that record.  Every product and sum is a separately rounded
 // _rn intrinsic in the reference's order, so the result is bit-identical
@@ -36,6 +42,7 @@
 
 #include "../../include/elastic_rtm.h"
 #include "common.cuh"
+#include "elastic2d_v2.cuh"
 #include "engine.h"
 
 using namespace eg;
@@ -108,8 +115,10 @@ struct PmlTabs {
     int abc;
 };
 
+constexpr int GZ = 32;  // guard rows above row 1 of a padded column (row 1 starts a 128-byte line)
+
 struct StepArgs {
-    int nz, nx;
+    int nz, nx, ldz;
     float *nw[NF];
     const float *cur[NF];
     const float *old[NF];
@@ -119,29 +128,24 @@ struct StepArgs {
     PmlTabs t;
     int zs, xs;
     float src;
+    int prefetch;
 };
 
-template <int K>
-__device__ __forceinline__ bool in_range(int nz, int nx, int iz, int ix)
-{
-    constexpr StK k = stk(K);
-    return iz >= k.z0 && iz <= nz - k.zoff && ix >= k.x0 && ix <= nx - k.xoff;
-}
+__device__ __forceinline__ float4 ld4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+__device__ __forceinline__ float at(const float4 &v, int r) { return r == 0 ? v.x : r == 1 ? v.y : r == 2 ? v.z : v.w; }
 
-// c1*(m[hi1]-m[lo1]) + ... + c5*(m[hi5]-m[lo5]), left to right
+// x range of a stencil kind for column ix (uniform over a thread's rows)
 template <int K>
-__device__ __forceinline__ float sten(const float *__restrict__ m, long long p, long long ld)
+__device__ __forceinline__ bool x_in(int nx, int ix)
 {
     constexpr StK k = stk(K);
-    const long long st = k.axis == 0 ? ld : 1;
-    float acc = 0.0f;
-#pragma unroll
-    for (int j = 1; j <= 5; ++j) {
-        const float d = sub_rn(__ldg(m + p + (5 - j + k.s) * st), __ldg(m + p - (6 - j - k.s) * st));
-        const float t = mul_rn(StagCoef<float>::c(j - 1), d);
-        acc = j == 1 ? t : add_rn(acc, t);
-    }
-    return acc;
+    return ix >= k.x0 && ix <= nx - k.xoff;
+}
+template <int K>
+__device__ __forceinline__ bool z_in(int nz, int iz)
+{
+    constexpr StK k = stk(K);
+    return iz >= k.z0 && iz <= nz - k.zoff;
 }
 
 // v * PML factor of a part at (iz, ix): the left / top side first, then the
@@ -174,56 +178,457 @@ __device__ __forceinline__ float pml_apply(const PmlTabs &T, int nz, int nx, int
     return v;
 }
 
-template <int F, bool BORN>
-__device__ __forceinline__ void advance_part(const StepArgs &a, int iz, int ix, long long p)
+// Stencil sums c1*(m[hi1]-m[lo1]) + ... + c5*(m[hi5]-m[lo5]) (left to right)
+// of the 4 rows starting at padded offset q.  x: ten 16-byte words from the
+// tap columns; z: the aligned window of rows q-8 .. q+11 (five words).
+template <int K>
+__device__ __forceinline__ void sten4(const float *__restrict__ m, long long q, long long ld, float out[4])
+{
+    constexpr StK k = stk(K);
+    if constexpr (k.axis == 0) {
+#pragma unroll
+        for (int j = 1; j <= 5; ++j) {
+            const float4 hi = ld4(m + q + (5 - j + k.s) * ld), lo = ld4(m + q - (6 - j - k.s) * ld);
+            const float c = StagCoef<float>::c(j - 1);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float t = mul_rn(c, sub_rn(at(hi, r), at(lo, r)));
+                out[r] = j == 1 ? t : add_rn(out[r], t);
+            }
+        }
+    } else {
+        float w[20];
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            const float4 v = ld4(m + q - 8 + 4 * b);
+            w[4 * b] = v.x;
+            w[4 * b + 1] = v.y;
+            w[4 * b + 2] = v.z;
+            w[4 * b + 3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int j = 1; j <= 5; ++j) {
+                const float t = mul_rn(StagCoef<float>::c(j - 1), sub_rn(w[8 + r + 5 - j + k.s], w[8 + r - 6 + j + k.s]));
+                out[r] = j == 1 ? t : add_rn(out[r], t);
+            }
+        }
+    }
+}
+
+// One thread's 4 cells of column ix, rows iz0 .. iz0+3, padded offset q.
+struct Cell4 {
+    int iz0, ix;
+    long long q;
+    int nrow;  // rows of the 4 inside the grid
+};
+
+// Finishes part F: v = 0 + cf*sa + cf*sb (where the operator runs)
+// + K0*old [+ source] [+ Born terms from ba, bb or S1/S2], then K1, stored.
+template <int F, bool BORN, bool FAST>
+__device__ __forceinline__ void finish(const StepArgs &a, const Cell4 &c, bool op_x, const float sa[4],
+                                       const float sb[4], bool born_x, const float ba[4], const float bb[4])
+{
+    constexpr Part P = part_of(F);
+    float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (FAST || op_x) {
+        const float4 cf = ld4(a.cf[P.coef] + c.q);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (FAST || z_in<P.st>(a.nz, c.iz0 + r)) {
+                v[r] = add_rn(v[r], mul_rn(at(cf, r), sa[r]));
+                v[r] = add_rn(v[r], mul_rn(at(cf, r), sb[r]));
+            }
+    }
+    const float4 o = ld4(a.old[F] + c.q);
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        v[r] = add_rn(v[r], FAST ? at(o, r)
+                            : r < c.nrow ? pml_apply<P.axis, P.avg, 0>(a.t, a.nz, a.nx, c.iz0 + r, c.ix, at(o, r))
+                                         : 0.0f);
+    if constexpr (!BORN && P.src) {
+        if (c.ix == a.xs && a.zs >= c.iz0 && a.zs < c.iz0 + 4) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (c.iz0 + r == a.zs) v[r] = add_rn(v[r], a.src);
+        }
+    }
+    if constexpr (BORN) {
+        constexpr BornT B = born_of(F);
+        if constexpr (B.st < 0) {
+            const float4 n = ld4(a.bgn[B.a] + c.q), u = ld4(a.bgc[B.a] + c.q), d = ld4(a.cf[B.coef] + c.q);
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (FAST || (c.iz0 + r >= 6 && c.iz0 + r <= a.nz - 5))
+                    v[r] = add_rn(v[r], mul_rn(sub_rn(at(n, r), at(u, r)), at(d, r)));
+        } else {
+            constexpr int KB = B.st < 0 ? 0 : B.st;
+            if (FAST || born_x) {
+                const float4 cf = ld4(a.cf[B.coef] + c.q);
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (FAST || z_in<KB>(a.nz, c.iz0 + r)) {
+                        v[r] = add_rn(v[r], mul_rn(at(cf, r), ba[r]));
+                        v[r] = add_rn(v[r], mul_rn(at(cf, r), bb[r]));
+                    }
+            }
+        }
+    }
+    if (!FAST) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (r < c.nrow) v[r] = pml_apply<P.axis, P.avg, 1>(a.t, a.nz, a.nx, c.iz0 + r, c.ix, v[r]);
+    }
+    float *dst = a.nw[F] + c.q;
+    if (c.nrow == 4) {
+        *reinterpret_cast<float4 *>(dst) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+            if (r < c.nrow) dst[r] = v[r];
+    }
+}
+
+// true when any of the 4 rows lies in the z range of stencil kind K
+template <int K>
+__device__ __forceinline__ bool any_z(int nz, int iz0)
+{
+    constexpr StK k = stk(K);
+    return iz0 + 3 >= k.z0 && iz0 <= nz - k.zoff;
+}
+
+// Parts F (and G, sharing F's stencils when G >= 0): the operator's two
+// stencils of cur[a], cur[b] and, for the scattered step, the Born
+// stencils of bgn[a], bgn[b] are evaluated once.
+template <int F, int G, bool BORN, bool FAST>
+__device__ __forceinline__ void part4(const StepArgs &a, const Cell4 &c)
+{
+    constexpr Part P = part_of(F);
+    float sa[4] = {}, sb[4] = {}, ba[4] = {}, bb[4] = {};
+    const bool op_x = FAST || (x_in<P.st>(a.nx, c.ix) && any_z<P.st>(a.nz, c.iz0));
+    if (op_x) {
+        sten4<P.st>(a.cur[P.a], c.q, a.ldz, sa);
+        sten4<P.st>(a.cur[P.b], c.q, a.ldz, sb);
+    }
+    bool born_x = false;
+    if constexpr (BORN) {
+        constexpr BornT B = born_of(F);
+        if constexpr (B.st >= 0) {
+            constexpr int KB = B.st < 0 ? 0 : B.st;
+            born_x = FAST || (x_in<KB>(a.nx, c.ix) && any_z<KB>(a.nz, c.iz0));
+            if (born_x) {
+                sten4<KB>(a.bgn[B.a], c.q, a.ldz, ba);
+                sten4<KB>(a.bgn[B.b], c.q, a.ldz, bb);
+            }
+        }
+    }
+    finish<F, BORN, FAST>(a, c, op_x, sa, sb, born_x, ba, bb);
+    if constexpr (G >= 0) finish<G, BORN, FAST>(a, c, op_x, sa, sb, born_x, ba, bb);
+}
+
+template <bool BORN, bool FAST>
+__device__ __forceinline__ void cell4(const StepArgs &a, const Cell4 &c)
+{
+    part4<VXX, -1, BORN, FAST>(a, c);
+    part4<VXZ, -1, BORN, FAST>(a, c);
+    part4<VZX, -1, BORN, FAST>(a, c);
+    part4<VZZ, -1, BORN, FAST>(a, c);
+    part4<SXXX, SZZX, BORN, FAST>(a, c);  // D, F on Vx (S3, S5 on the background's Vx)
+    part4<SXXZ, SZZZ, BORN, FAST>(a, c);  // E, G on Vz (S4, S6)
+    part4<SXZX, -1, BORN, FAST>(a, c);
+    part4<SXZZ, -1, BORN, FAST>(a, c);
+}
+
+constexpr int BZ = 32, BX = 8;  // threads: 32 x 4 = 128 rows, 8 columns
+
+__device__ __forceinline__ void prefetch_l2(const void *p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// The lines a thread's cells miss on first touch (own cells of the current
+// and old levels, the coefficients; for the scattered step the background's
+// levels), requested together at the start so that they are in flight at
+// once instead of one part after another.
+template <bool BORN>
+__device__ __forceinline__ void prefetch_cells(const StepArgs &a, long long q)
+{
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        prefetch_l2(a.cur[f] + q);
+        prefetch_l2(a.old[f] + q);
+    }
+#pragma unroll
+    for (int k = 0; k < (BORN ? NC : C_DL); ++k) prefetch_l2(a.cf[k] + q);
+    if (BORN) {
+#pragma unroll
+        for (int f = 0; f < 4; ++f) {
+            prefetch_l2(a.bgn[f] + q);
+            prefetch_l2(a.bgc[f] + q);
+        }
+    }
+}
+
+template <bool BORN>
+__global__ void __launch_bounds__(BZ * BX) k_pml_step(const StepArgs a)
+{
+    Cell4 c;
+    c.iz0 = (blockIdx.x * BZ + threadIdx.x) * 4 + 1;
+    c.ix = blockIdx.y * BX + threadIdx.y + 1;
+    if (c.iz0 > a.nz || c.ix > a.nx) return;
+    c.q = (long long)(c.ix - 1) * a.ldz + GZ + c.iz0 - 1;
+    c.nrow = a.nz - c.iz0 + 1 < 4 ? a.nz - c.iz0 + 1 : 4;
+    if (a.prefetch) prefetch_cells<BORN>(a, c.q);
+    const int e = a.t.abc + 5;  // interior without PML: rows, columns e+1 .. n-e
+    if (c.iz0 > e && c.iz0 + 3 <= a.nz - e && c.ix > e && c.ix <= a.nx - e) cell4<BORN, true>(a, c);
+    else cell4<BORN, false>(a, c);
+}
+
+// Staged form: a CTA of 128 threads owns a tile of 64 rows x 8 columns; the
+// 5760-byte staged arrays (80 x 18 floats) keep 128-byte alignment; the
+// planes its stencils read (background: the 10 current parts; scattered:
+// its 10 current parts and the background's 4 new velocity parts) arrive as
+// one bulk tensor copy each of 80 rows x 18 columns (8-row and 5-column
+// halos, zero outside the grid) on one mbarrier, so every staged byte of the
+// tile is in flight at once; thread t owns rows 4 (t % 16) .. +3 of column
+// t / 16 and reads taps as 16-byte shared words.  The pointwise operands
+// (old level, coefficients) are requested into L2 while the copies run.
+constexpr int TT_Z = 64, TT_X = 8, TT_LZ = TT_Z + 16, TT_LX = TT_X + 10, TT_SIZE = TT_LZ * TT_LX;
+constexpr int TT_THREADS = (TT_Z / 4) * TT_X;
+
+struct TileArgs {
+    int plane[14];  // staged planes: index into the field planes of the tensor map
+    int *err;       // set when a tile's copies did not arrive in time
+};
+
+template <int K>
+__device__ __forceinline__ void sten4s(const float *sm, int col, int row, float out[4])
+{
+    constexpr StK k = stk(K);
+    if constexpr (k.axis == 0) {
+#pragma unroll
+        for (int j = 1; j <= 5; ++j) {
+            const float4 hi = *reinterpret_cast<const float4 *>(sm + (col + 5 - j + k.s) * TT_LZ + row);
+            const float4 lo = *reinterpret_cast<const float4 *>(sm + (col - (6 - j - k.s)) * TT_LZ + row);
+            const float c = StagCoef<float>::c(j - 1);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float t = mul_rn(c, sub_rn(at(hi, r), at(lo, r)));
+                out[r] = j == 1 ? t : add_rn(out[r], t);
+            }
+        }
+    } else {
+        float w[20];
+#pragma unroll
+        for (int b = 0; b < 5; ++b) {
+            const float4 v = *reinterpret_cast<const float4 *>(sm + col * TT_LZ + row - 8 + 4 * b);
+            w[4 * b] = v.x;
+            w[4 * b + 1] = v.y;
+            w[4 * b + 2] = v.z;
+            w[4 * b + 3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int j = 1; j <= 5; ++j) {
+                const float t = mul_rn(StagCoef<float>::c(j - 1), sub_rn(w[8 + r + 5 - j + k.s], w[8 + r - 6 + j + k.s]));
+                out[r] = j == 1 ? t : add_rn(out[r], t);
+            }
+        }
+    }
+}
+
+// staged slot of a current part (0..9) and of a background new velocity
+// part (10..13)
+template <int F, int G, bool BORN>
+__device__ __forceinline__ void part_t(const StepArgs &a, const Cell4 &c, const float *sm, int col, int row)
+{
+    constexpr Part P = part_of(F);
+    float sa[4] = {}, sb[4] = {}, ba[4] = {}, bb[4] = {};
+    const bool op_x = x_in<P.st>(a.nx, c.ix) && any_z<P.st>(a.nz, c.iz0);
+    if (op_x) {
+        sten4s<P.st>(sm + P.a * TT_SIZE, col, row, sa);
+        sten4s<P.st>(sm + P.b * TT_SIZE, col, row, sb);
+    }
+    bool born_x = false;
+    if constexpr (BORN) {
+        constexpr BornT B = born_of(F);
+        if constexpr (B.st >= 0) {
+            constexpr int KB = B.st < 0 ? 0 : B.st;
+            born_x = x_in<KB>(a.nx, c.ix) && any_z<KB>(a.nz, c.iz0);
+            if (born_x) {
+                sten4s<KB>(sm + (10 + B.a) * TT_SIZE, col, row, ba);
+                sten4s<KB>(sm + (10 + B.b) * TT_SIZE, col, row, bb);
+            }
+        }
+    }
+    finish<F, BORN, false>(a, c, op_x, sa, sb, born_x, ba, bb);
+    if constexpr (G >= 0) finish<G, BORN, false>(a, c, op_x, sa, sb, born_x, ba, bb);
+}
+
+template <bool BORN>
+__global__ void __launch_bounds__(TT_THREADS) k_pml_tile(const StepArgs a, const TileArgs ta,
+                                                         const __grid_constant__ CUtensorMap tm)
+{
+    constexpr int NS = BORN ? 14 : 10;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // staged arrays start on a 128-byte boundary (the launch adds 128 bytes)
+    float *smem = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) unsigned long long bar;
+    const int z0 = blockIdx.x * TT_Z + 1, x0 = blockIdx.y * TT_X + 1;  // first row, column (1-based)
+    const int t = threadIdx.x;
+    if (t == 0) {
+        mbar_init(&bar);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (t == 0) {
+        mbar_expect_tx(&bar, NS * TT_SIZE * 4);
+        // padded row of z0 - 8 (a multiple of 4), column x0 - 5 (may be < 0:
+        // zero fill)
+        const int r0 = GZ + z0 - 1 - 8, c0 = x0 - 1 - 5;
+#pragma unroll 1
+        for (int sl = 0; sl < NS; ++sl) tma_load_3d(smem + sl * TT_SIZE, &tm, r0, c0, ta.plane[sl], &bar);
+    }
+    Cell4 c;
+    const int cx = t / (TT_Z / 4), g = t % (TT_Z / 4);
+    c.iz0 = z0 + 4 * g;
+    c.ix = x0 + cx;
+    const bool live = c.iz0 <= a.nz && c.ix <= a.nx;
+    c.q = (long long)(c.ix - 1) * a.ldz + GZ + c.iz0 - 1;
+    c.nrow = a.nz - c.iz0 + 1 < 4 ? a.nz - c.iz0 + 1 : 4;
+    if (live && a.prefetch) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) prefetch_l2(a.old[f] + c.q);
+#pragma unroll
+        for (int k = 0; k < (BORN ? NC : C_DL); ++k) prefetch_l2(a.cf[k] + c.q);
+        if (BORN) {
+#pragma unroll
+            for (int f = 0; f < 4; ++f) prefetch_l2(a.bgc[f] + c.q);
+        }
+    }
+    if (!mbar_wait(&bar, 0)) {
+        if (t == 0) atomicExch(ta.err, 1);
+        return;
+    }
+    if (!live) return;
+    const int col = cx + 5, row = 8 + 4 * g;
+    part_t<VXX, -1, BORN>(a, c, smem, col, row);
+    part_t<VXZ, -1, BORN>(a, c, smem, col, row);
+    part_t<VZX, -1, BORN>(a, c, smem, col, row);
+    part_t<VZZ, -1, BORN>(a, c, smem, col, row);
+    part_t<SXXX, SZZX, BORN>(a, c, smem, col, row);
+    part_t<SXXZ, SZZZ, BORN>(a, c, smem, col, row);
+    part_t<SXZX, -1, BORN>(a, c, smem, col, row);
+    part_t<SXZZ, -1, BORN>(a, c, smem, col, row);
+}
+
+// One thread per cell form of the same step (blocks of 32 x 8 cells): every
+// tap a 4-byte load through L1, each distinct stencil evaluated once; with
+// 40 registers a thread, 64 warps fit on an SM.
+template <int K>
+__device__ __forceinline__ float sten1(const float *__restrict__ m, long long p, long long ld)
+{
+    constexpr StK k = stk(K);
+    const long long st = k.axis == 0 ? ld : 1;
+    float acc = 0.0f;
+#pragma unroll
+    for (int j = 1; j <= 5; ++j) {
+        const float d = sub_rn(__ldg(m + p + (5 - j + k.s) * st), __ldg(m + p - (6 - j - k.s) * st));
+        const float t = mul_rn(StagCoef<float>::c(j - 1), d);
+        acc = j == 1 ? t : add_rn(acc, t);
+    }
+    return acc;
+}
+
+// Finishes part F of one cell from its operator stencils sa, sb and Born
+// stencils ba, bb (evaluated by the caller where they apply).
+template <int F, bool BORN, bool FAST>
+__device__ __forceinline__ void finish1(const StepArgs &a, int iz, int ix, long long p, bool op, float sa, float sb,
+                                        bool born, float ba, float bb)
 {
     constexpr Part P = part_of(F);
     float v = 0.0f;
-    if (in_range<P.st>(a.nz, a.nx, iz, ix)) {
+    if (FAST || op) {
         const float cf = __ldg(a.cf[P.coef] + p);
-        v = add_rn(v, mul_rn(cf, sten<P.st>(a.cur[P.a], p, a.nz)));
-        v = add_rn(v, mul_rn(cf, sten<P.st>(a.cur[P.b], p, a.nz)));
+        v = add_rn(v, mul_rn(cf, sa));
+        v = add_rn(v, mul_rn(cf, sb));
     }
-    v = add_rn(v, pml_apply<P.axis, P.avg, 0>(a.t, a.nz, a.nx, iz, ix, __ldg(a.old[F] + p)));
+    const float o = __ldg(a.old[F] + p);
+    v = add_rn(v, FAST ? o : pml_apply<P.axis, P.avg, 0>(a.t, a.nz, a.nx, iz, ix, o));
     if constexpr (!BORN && P.src) {
         if (iz == a.zs && ix == a.xs) v = add_rn(v, a.src);
     }
     if constexpr (BORN) {
         constexpr BornT B = born_of(F);
         if constexpr (B.st < 0) {
-            if (iz >= 6 && iz <= a.nz - 5)
+            if (FAST || (iz >= 6 && iz <= a.nz - 5))
                 v = add_rn(v, mul_rn(sub_rn(__ldg(a.bgn[B.a] + p), __ldg(a.bgc[B.a] + p)), __ldg(a.cf[B.coef] + p)));
-        } else {
+        } else if (FAST || born) {
+            const float cf = __ldg(a.cf[B.coef] + p);
+            v = add_rn(v, mul_rn(cf, ba));
+            v = add_rn(v, mul_rn(cf, bb));
+        }
+    }
+    a.nw[F][p] = FAST ? v : pml_apply<P.axis, P.avg, 1>(a.t, a.nz, a.nx, iz, ix, v);
+}
+
+// Parts F and (G >= 0) G sharing F's stencils, for one cell.  FAST: the
+// cell lies where every operator runs and no PML factor applies (the same
+// operations without the range checks and the factors of 1).
+template <int F, int G, bool BORN, bool FAST>
+__device__ __forceinline__ void part1(const StepArgs &a, int iz, int ix, long long p)
+{
+    constexpr Part P = part_of(F);
+    float sa = 0.0f, sb = 0.0f, ba = 0.0f, bb = 0.0f;
+    const bool op = FAST || (x_in<P.st>(a.nx, ix) && z_in<P.st>(a.nz, iz));
+    if (op) {
+        sa = sten1<P.st>(a.cur[P.a], p, a.ldz);
+        sb = sten1<P.st>(a.cur[P.b], p, a.ldz);
+    }
+    bool born = false;
+    if constexpr (BORN) {
+        constexpr BornT B = born_of(F);
+        if constexpr (B.st >= 0) {
             constexpr int KB = B.st < 0 ? 0 : B.st;
-            if (in_range<KB>(a.nz, a.nx, iz, ix)) {
-                const float cf = __ldg(a.cf[B.coef] + p);
-                v = add_rn(v, mul_rn(cf, sten<KB>(a.bgn[B.a], p, a.nz)));
-                v = add_rn(v, mul_rn(cf, sten<KB>(a.bgn[B.b], p, a.nz)));
+            born = FAST || (x_in<KB>(a.nx, ix) && z_in<KB>(a.nz, iz));
+            if (born) {
+                ba = sten1<KB>(a.bgn[B.a], p, a.ldz);
+                bb = sten1<KB>(a.bgn[B.b], p, a.ldz);
             }
         }
     }
-    a.nw[F][p] = pml_apply<P.axis, P.avg, 1>(a.t, a.nz, a.nx, iz, ix, v);
+    finish1<F, BORN, FAST>(a, iz, ix, p, op, sa, sb, born, ba, bb);
+    if constexpr (G >= 0) finish1<G, BORN, FAST>(a, iz, ix, p, op, sa, sb, born, ba, bb);
 }
 
-constexpr int BZ = 32, BX = 8;
+template <bool BORN, bool FAST>
+__device__ __forceinline__ void cell1(const StepArgs &a, int iz, int ix, long long p)
+{
+    part1<VXX, -1, BORN, FAST>(a, iz, ix, p);
+    part1<VXZ, -1, BORN, FAST>(a, iz, ix, p);
+    part1<VZX, -1, BORN, FAST>(a, iz, ix, p);
+    part1<VZZ, -1, BORN, FAST>(a, iz, ix, p);
+    part1<SXXX, SZZX, BORN, FAST>(a, iz, ix, p);  // D, F (S3, S5) share their stencils
+    part1<SXXZ, SZZZ, BORN, FAST>(a, iz, ix, p);  // E, G (S4, S6)
+    part1<SXZX, -1, BORN, FAST>(a, iz, ix, p);
+    part1<SXZZ, -1, BORN, FAST>(a, iz, ix, p);
+}
 
 template <bool BORN>
-__global__ void __launch_bounds__(BZ * BX) k_pml_step(const StepArgs a)
+__global__ void __launch_bounds__(BZ * BX) k_pml_step1(const StepArgs a)
 {
     const int iz = blockIdx.x * BZ + threadIdx.x + 1;
     const int ix = blockIdx.y * BX + threadIdx.y + 1;
     if (iz > a.nz || ix > a.nx) return;
-    const long long p = (long long)(ix - 1) * a.nz + iz - 1;
-    advance_part<VXX, BORN>(a, iz, ix, p);
-    advance_part<VXZ, BORN>(a, iz, ix, p);
-    advance_part<VZX, BORN>(a, iz, ix, p);
-    advance_part<VZZ, BORN>(a, iz, ix, p);
-    advance_part<SXXX, BORN>(a, iz, ix, p);
-    advance_part<SXXZ, BORN>(a, iz, ix, p);
-    advance_part<SZZX, BORN>(a, iz, ix, p);
-    advance_part<SZZZ, BORN>(a, iz, ix, p);
-    advance_part<SXZX, BORN>(a, iz, ix, p);
-    advance_part<SXZZ, BORN>(a, iz, ix, p);
+    const long long p = (long long)(ix - 1) * a.ldz + GZ + iz - 1;
+    if (a.prefetch) prefetch_cells<BORN>(a, p);
+    // every operator's range and no PML row or column: rows abc+6 ..
+    // nz-abc-5, columns abc+6 .. nx-abc-5
+    const int e = a.t.abc + 5;
+    if (iz > e && iz <= a.nz - e && ix > e && ix <= a.nx - e) cell1<BORN, true>(a, iz, ix, p);
+    else cell1<BORN, false>(a, iz, ix, p);
 }
 
 // Model set-up (born-mod.f90:331-389).  The harmonic averages are written in
@@ -231,7 +636,7 @@ __global__ void __launch_bounds__(BZ * BX) k_pml_step(const StepArgs a)
 // ((iz+1, ix), (iz, ix+1), (iz+1, ix+1)) is still unaveraged then, so each
 // cell here recomputes its neighbours' unaveraged values from the inputs.
 struct ModelArgs {
-    int nz, nx, lame;
+    int nz, nx, ldz, lame;
     float aux1;
     const float *vp0, *vs0, *rho0, *dvp, *dvs, *drho;
     float *cf[NC];
@@ -274,22 +679,23 @@ __global__ void k_pml_model(const ModelArgs m)
     const int iz = blockIdx.x * BZ + threadIdx.x + 1;
     const int ix = blockIdx.y * BX + threadIdx.y + 1;
     if (iz > m.nz || ix > m.nx) return;
-    const long long nz = m.nz, p = (ix - 1) * nz + iz - 1;
+    // p: the caller's (nz, nx) planes; w: the padded coefficient planes
+    const long long nz = m.nz, p = (ix - 1) * nz + iz - 1, w = (long long)(ix - 1) * m.ldz + GZ + iz - 1;
     const float aux1 = m.aux1;
     // densities on the staggered grids (:360-384)
     if (iz < m.nz) {
-        m.cf[C_RVX][p] = div_rn(mul_rn(aux1, 1.0f), mul_rn(0.5f, add_rn(m.rho0[p + 1], m.rho0[p])));
-        m.cf[C_DRVX][p] = -add_rn(div_rn(m.drho[p + 1], m.rho0[p + 1]), div_rn(m.drho[p], m.rho0[p]));
+        m.cf[C_RVX][w] = div_rn(mul_rn(aux1, 1.0f), mul_rn(0.5f, add_rn(m.rho0[p + 1], m.rho0[p])));
+        m.cf[C_DRVX][w] = -add_rn(div_rn(m.drho[p + 1], m.rho0[p + 1]), div_rn(m.drho[p], m.rho0[p]));
     } else {
-        m.cf[C_RVX][p] = mul_rn(aux1, div_rn(1.0f, m.rho0[p]));
-        m.cf[C_DRVX][p] = -div_rn(m.drho[p], m.rho0[p]);
+        m.cf[C_RVX][w] = mul_rn(aux1, div_rn(1.0f, m.rho0[p]));
+        m.cf[C_DRVX][w] = -div_rn(m.drho[p], m.rho0[p]);
     }
     if (ix < m.nx) {
-        m.cf[C_RVZ][p] = div_rn(mul_rn(aux1, 1.0f), mul_rn(0.5f, add_rn(m.rho0[p + nz], m.rho0[p])));
-        m.cf[C_DRVZ][p] = -add_rn(div_rn(m.drho[p + nz], m.rho0[p + nz]), div_rn(m.drho[p], m.rho0[p]));
+        m.cf[C_RVZ][w] = div_rn(mul_rn(aux1, 1.0f), mul_rn(0.5f, add_rn(m.rho0[p + nz], m.rho0[p])));
+        m.cf[C_DRVZ][w] = -add_rn(div_rn(m.drho[p + nz], m.rho0[p + nz]), div_rn(m.drho[p], m.rho0[p]));
     } else {
-        m.cf[C_RVZ][p] = mul_rn(aux1, div_rn(1.0f, m.rho0[p]));
-        m.cf[C_DRVZ][p] = -div_rn(m.drho[p], m.rho0[p]);
+        m.cf[C_RVZ][w] = mul_rn(aux1, div_rn(1.0f, m.rho0[p]));
+        m.cf[C_DRVZ][w] = -div_rn(m.drho[p], m.rho0[p]);
     }
     // Lame parameters, harmonic averages inside the outermost ring (:386-407)
     const Raw r = raw_at(m, p);
@@ -305,12 +711,12 @@ __global__ void k_pml_model(const ModelArgs m)
         l2mi = add_rn(l, mul_rn(2.0f, mi));
         dl2mi = add_rn(dl, mul_rn(2.0f, dmi));
     }
-    m.cf[C_L][p] = l;
-    m.cf[C_MI][p] = mi;
-    m.cf[C_L2MI][p] = l2mi;
-    m.cf[C_DL][p] = dl;
-    m.cf[C_DMI][p] = dmi;
-    m.cf[C_DL2MI][p] = dl2mi;
+    m.cf[C_L][w] = l;
+    m.cf[C_MI][w] = mi;
+    m.cf[C_L2MI][w] = l2mi;
+    m.cf[C_DL][w] = dl;
+    m.cf[C_DMI][w] = dmi;
+    m.cf[C_DL2MI][w] = dl2mi;
 }
 
 // PML tables (pml-mod.f90:23-89).  d0 = log(1/R) (1.5 vp) / (abc dx) with
@@ -360,7 +766,7 @@ __global__ void k_pml_tables(const TabArgs t)
 // Receiver lines of one recorded level (seis-mod-born.f90:36-98): for
 // ix = 1..nx-2a-1 (a = abc, or 1 when abc = 0), column c = ix + a.
 struct RecArgs {
-    int nz, nx, a, nseis, zrec, count;
+    int nz, nx, ldz, a, nseis, zrec, count;
     const float *w[2][NF];  // background, scattered new level
     float *seis[6];         // Vx, Vz, P, Vx_b, Vz_b, P_b: (nseis, nx - 2 abc)
 };
@@ -369,9 +775,9 @@ __global__ void k_pml_record(const RecArgs r)
 {
     const int ix = blockIdx.x * blockDim.x + threadIdx.x + 1;
     if (ix > r.nx - 2 * r.a - 1) return;
-    const long long nz = r.nz, c = ix + r.a;
+    const long long nz = r.ldz, c = ix + r.a;  // nz: the padded column stride
     const long long q = (long long)(ix - 1) * r.nseis + r.count - 1;
-    const long long pr = (c - 1) * nz + r.zrec - 1;  // (zrec, c)
+    const long long pr = (c - 1) * nz + GZ + r.zrec - 1;  // (zrec, c)
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
         const float *const *f = r.w[w];
@@ -386,7 +792,7 @@ __global__ void k_pml_record(const RecArgs r)
 // Snapshots of one level (snap-mod-born.f90:33-68), rows and columns
 // 2..n-2 of the (nz, nx, nsnap) cubes.
 struct SnapArgs {
-    int nz, nx;
+    int nz, nx, ldz;
     long long off;
     const float *w[2][NF];
     float *snap[6];
@@ -397,7 +803,8 @@ __global__ void k_pml_snap(const SnapArgs s)
     const int iz = blockIdx.x * BZ + threadIdx.x + 1;
     const int ix = blockIdx.y * BX + threadIdx.y + 1;
     if (iz < 2 || iz > s.nz - 2 || ix < 2 || ix > s.nx - 2) return;
-    const long long p = (long long)(ix - 1) * s.nz + iz - 1, o = s.off + p;
+    const long long p = (long long)(ix - 1) * s.ldz + GZ + iz - 1;
+    const long long o = s.off + (long long)(ix - 1) * s.nz + iz - 1;
 #pragma unroll
     for (int w = 0; w < 2; ++w) {
         const float *const *f = s.w[w];
@@ -423,8 +830,15 @@ float pml_source(int it, int nsource, float fp, float dt, float dx)
     return ((0.7e7f * src) * (dt / (dx * dx))) * 0.25f;
 }
 
+// Step kernel form: 0 four rows per thread, 1 one cell per thread, 4 the
+// staged tiles; +2 requests each thread's first-touch lines into L2 at the
+// start.
+int g_pml_kind = 3;
+
 struct PmlState {
     DevBuf<float> buf;
+    DevBuf<int> err;
+    bool attr_set[RTM_MAX_DEVICES] = {};
     double last_ms = 0.0;
     long long launches = 0;
 };
@@ -460,21 +874,47 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
 {
     TRY(check_geom(g));
     TRY(ensure_device());
-    const long long n = (long long)g.nz * g.nx;
+    // padded working planes: ldz >= nz + GZ + 12 rows (GZ guard rows above,
+    // the rest below), a multiple of 32 floats
+    const int ldz = (g.nz + GZ + 12 + 31) / 32 * 32;
+    const long long n = (long long)ldz * g.nx, nf = (long long)g.nz * g.nx;
     const long long ntab = 4LL * g.nz * g.abc + 4LL * g.abc * g.nx;
     TRY(g_pml.buf.alloc((size_t)(NC * n + 60 * n + ntab + 1)));
+    TRY(g_pml.err.alloc(1));
     float *cf = g_pml.buf.p, *fld = cf + NC * n, *tab = fld + 60 * n;
-    RTM_CUDA(cudaMemsetAsync(fld, 0, sizeof(float) * 60 * n, st));
+    RTM_CUDA(cudaMemsetAsync(cf, 0, sizeof(float) * (NC + 60) * n, st));
+    RTM_CUDA(cudaMemsetAsync(g_pml.err.p, 0, sizeof(int), st));
+    const bool tile = (g_pml_kind & 4) != 0;
+    CUtensorMap tm;
+    if (tile) {
+        RTM_CHECK_ARG(tensor_maps_available(), "bulk tensor copies are not available");
+        // all 60 field planes: padded rows x columns x planes
+        const long long dims[3] = {ldz, g.nx, 60}, strides[2] = {4LL * ldz, 4LL * n};
+        const int box[3] = {TT_LZ, TT_LX, 1};
+        TRY(make_map_nd(&tm, fld, false, 3, dims, strides, box, 0));
+        const int dev = rtm_current_device();
+        std::lock_guard<std::mutex> lk(rtm_device_state_lock());
+        if (!g_pml.attr_set[dev]) {
+            RTM_CUDA(cudaFuncSetAttribute(k_pml_tile<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          10 * TT_SIZE * 4 + 128));
+            RTM_CUDA(cudaFuncSetAttribute(k_pml_tile<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          14 * TT_SIZE * 4 + 128));
+            g_pml.attr_set[dev] = true;
+        }
+    }
+    const dim3 grdt(ceil_div(g.nz, TT_Z), ceil_div(g.nx, TT_X));
     for (int k = 0; k < 6; ++k) {
         RTM_CUDA(cudaMemsetAsync(seis[k], 0, sizeof(float) * g.seis_n(), st));
         RTM_CUDA(cudaMemsetAsync(snap[k], 0, sizeof(float) * g.snap_n(), st));
     }
     long long launches = 0;
-    const dim3 blk(BZ, BX), grd(ceil_div(g.nz, BZ), ceil_div(g.nx, BX));
+    // per-cell kernels: one thread per cell; step kernels: 4 rows per thread
+    const dim3 blk(BZ, BX), grd(ceil_div(g.nz, BZ), ceil_div(g.nx, BX)), grd4(ceil_div(g.nz, 4 * BZ), ceil_div(g.nx, BX));
     {
         ModelArgs m;
         m.nz = g.nz;
         m.nx = g.nx;
+        m.ldz = ldz;
         m.lame = g.lame;
         m.aux1 = g.dt / g.dx;
         m.vp0 = model[0];
@@ -530,6 +970,9 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
     StepArgs a;
     a.nz = g.nz;
     a.nx = g.nx;
+    a.ldz = ldz;
+    a.prefetch = (g_pml_kind & 2) != 0;
+    const bool one = (g_pml_kind & 1) != 0;
     for (int k = 0; k < NC; ++k) a.cf[k] = cf + k * n;
     a.t = T;
     a.zs = g.zs;
@@ -545,12 +988,20 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
                 a.bgn[f] = lv[0][inew][f];
                 a.bgc[f] = lv[0][icur][f];
             }
-            if (w == 0) {
-                a.src = pml_source(it, g.nsource, g.fp, g.dt, g.dx);
-                k_pml_step<false><<<grd, blk, 0, st>>>(a);
+            a.src = w == 0 ? pml_source(it, g.nsource, g.fp, g.dt, g.dx) : 0.0f;
+            if (tile) {
+                TileArgs ta;
+                ta.err = g_pml.err.p;
+                for (int f = 0; f < NF; ++f) ta.plane[f] = (w * 3 + icur) * NF + f;
+                for (int f = 0; f < 4; ++f) ta.plane[NF + f] = inew * NF + f;
+                if (w == 0) k_pml_tile<false><<<grdt, TT_THREADS, 10 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
+                else k_pml_tile<true><<<grdt, TT_THREADS, 14 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
+            } else if (one) {
+                if (w == 0) k_pml_step1<false><<<grd, blk, 0, st>>>(a);
+                else k_pml_step1<true><<<grd, blk, 0, st>>>(a);
             } else {
-                a.src = 0.0f;
-                k_pml_step<true><<<grd, blk, 0, st>>>(a);
+                if (w == 0) k_pml_step<false><<<grd4, blk, 0, st>>>(a);
+                else k_pml_step<true><<<grd4, blk, 0, st>>>(a);
             }
             RTM_CUDA(cudaGetLastError());
             ++launches;
@@ -559,6 +1010,7 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
             RecArgs r;
             r.nz = g.nz;
             r.nx = g.nx;
+            r.ldz = ldz;
             r.a = g.abc == 0 ? 1 : g.abc;
             r.nseis = g.nseis;
             r.zrec = g.zrec;
@@ -578,7 +1030,8 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
             SnapArgs s;
             s.nz = g.nz;
             s.nx = g.nx;
-            s.off = (long long)(countsnap - 1) * n;
+            s.ldz = ldz;
+            s.off = (long long)(countsnap - 1) * nf;
             for (int w = 0; w < 2; ++w)
                 for (int f = 0; f < NF; ++f) s.w[w][f] = lv[w][inew][f];
             for (int k = 0; k < 6; ++k) s.snap[k] = snap[k];
@@ -593,6 +1046,13 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
         inew = t;
     }
     g_pml.launches = launches;
+    int err = 0;
+    RTM_CUDA(cudaMemcpyAsync(&err, g_pml.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RTM_CUDA(cudaStreamSynchronize(st));
+    if (err) {
+        rtm_set_error("a PML step tile's copies did not arrive within the time limit");
+        return RTM_ERR_TIMEOUT;
+    }
     return RTM_OK;
 }
 
@@ -665,3 +1125,10 @@ extern "C" int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsour
 }
 
 extern "C" long long pml_born_launches(void) { return g_pml.launches; }
+
+extern "C" int pml_set_kernel(int kind)
+{
+    RTM_CHECK_ARG(kind >= 0 && kind <= 7 && kind != 5 && kind != 7, "kernel kind %d", kind);
+    g_pml_kind = kind;
+    return RTM_OK;
+}

@@ -72,6 +72,16 @@ def born_dev(model, seis, snap, dx, dt, nt, xsource, zsource, nsource, fp, abc, 
                               ctypes.c_void_p(stream.cuda_stream)))
 
 
+KERNELS = {"rows4": 0, "cell": 1, "rows4-prefetch": 2, "cell-prefetch": 3, "tile": 4, "tile-prefetch": 6}
+
+
+def set_kernel(kind="cell-prefetch"):
+    """Step kernel form (every form gives the same bits): tiles staged by
+    bulk tensor copies, four rows per thread, or one cell per thread; with or
+    without an L2 prefetch of each thread's first-touch lines."""
+    check(load().pml_set_kernel(KERNELS[kind]))
+
+
 def launches():
     """Kernels launched by the last call."""
     return int(load().pml_born_launches())

@@ -312,8 +312,13 @@ int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *
  * to the reference's CPU execution.
  * pml_born_c_: host arrays.  pml_born_dev: model[6] = vp0, vs0, rho0, dvp,
  * dvs, drho and the outputs are device pointers, work on `stream` (a
- * cudaStream_t, NULL for the default stream); returns without waiting.
- * pml_born_launches: kernels launched by the last call. */
+ * cudaStream_t, NULL for the default stream) and returns when it is done.
+ * pml_born_launches: kernels launched by the last call.
+ * pml_set_kernel: step kernel form, 0 four rows per thread, 1 one cell per
+ * thread, 4 tiles staged by bulk tensor copies; + 2 to request each
+ * thread's first-touch lines into L2 first (default 3); every form gives
+ * the same bits.  A staged tile whose copies do not arrive within about a
+ * second makes the call return status 4. */
 int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsource, int zsource, int nsource, float fp, int nsnap,
                 int nseis, int abc, int zrec, int free_surface, int lame, const float *vp0, const float *vs0,
                 const float *rho0, const float *dvp, const float *dvs, const float *drho, float *const *seis,
@@ -322,6 +327,7 @@ int pml_born_dev(int nz, int nx, int nt, float dx, float dt, int xsource, int zs
                  int nseis, int abc, int zrec, int free_surface, int lame, const float *const *model,
                  float *const *seis, float *const *snap, void *stream);
 long long pml_born_launches(void);
+int pml_set_kernel(int kind);
 
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the

@@ -33,6 +33,13 @@ def test_gpu_matches_reference_fixtures(gold, name):
     assert pml.launches() >= 2 * kw["nt"]
 
 
+@pytest.fixture(params=list(pml.KERNELS))
+def kernel(request):
+    pml.set_kernel(request.param)
+    yield request.param
+    pml.set_kernel()
+
+
 @pytest.mark.parametrize("nz,nx,abc,fs,lame,seed", [
     (29, 30, 12, False, False, 1),    # left and right PML columns overlap
     (26, 52, 11, True, False, 2),     # top and bottom PML rows overlap
@@ -40,7 +47,7 @@ def test_gpu_matches_reference_fixtures(gold, name):
     (130, 97, 16, False, True, 4),    # ragged against the 32 x 8 blocks
     (257, 66, 30, True, False, 5),
 ])
-def test_gpu_matches_oracle(nz, nx, abc, fs, lame, seed):
+def test_gpu_matches_oracle(nz, nx, abc, fs, lame, seed, kernel):
     m = G.model(nz, nx, seed, lame)
     P = O.pml_params(nz, nx, 10.0, 0.08, fp=60.0)
     kw = dict(dx=10.0, dt=P["dt"], nt=P["nt"], xsource=max(1, nx // 2), zsource=min(12, nz - 3),
