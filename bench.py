@@ -1089,8 +1089,9 @@ def main():
     ap.add_argument("--gemm", default="tma", choices=["tma", "tc", "mma"],
                     help="U-Net GEMMs of the forward and backward-data passes: tcgen05 with bulk-copied "
                          "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")
-    ap.add_argument("--pml-kernel", default="cell-prefetch",
-                    choices=["rows4", "cell", "rows4-prefetch", "cell-prefetch", "tile", "tile-prefetch"],
+    ap.add_argument("--pml-kernel", default="cell-prefetch-b6",
+                    choices=["rows4", "cell", "rows4-prefetch", "cell-prefetch", "tile", "tile-prefetch",
+                             "cell-prefetch-b5", "cell-prefetch-b6"],
                     help="PML Born step kernel form")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")

@@ -617,7 +617,7 @@ __device__ __forceinline__ void cell1(const StepArgs &a, int iz, int ix, long lo
 }
 
 template <bool BORN>
-__global__ void __launch_bounds__(BZ * BX) k_pml_step1(const StepArgs a)
+__device__ __forceinline__ void step1_body(const StepArgs &a)
 {
     const int iz = blockIdx.x * BZ + threadIdx.x + 1;
     const int ix = blockIdx.y * BX + threadIdx.y + 1;
@@ -629,6 +629,19 @@ __global__ void __launch_bounds__(BZ * BX) k_pml_step1(const StepArgs a)
     const int e = a.t.abc + 5;
     if (iz > e && iz <= a.nz - e && ix > e && ix <= a.nx - e) cell1<BORN, true>(a, iz, ix, p);
     else cell1<BORN, false>(a, iz, ix, p);
+}
+
+template <bool BORN>
+__global__ void __launch_bounds__(BZ * BX) k_pml_step1(const StepArgs a)
+{
+    step1_body<BORN>(a);
+}
+
+// the same with a register bound of MINB blocks of 256 threads an SM
+template <bool BORN, int MINB>
+__global__ void __launch_bounds__(BZ * BX, MINB) k_pml_step1b(const StepArgs a)
+{
+    step1_body<BORN>(a);
 }
 
 // Model set-up (born-mod.f90:331-389).  The harmonic averages are written in
@@ -830,10 +843,12 @@ float pml_source(int it, int nsource, float fp, float dt, float dx)
     return ((0.7e7f * src) * (dt / (dx * dx))) * 0.25f;
 }
 
-// Step kernel form: 0 four rows per thread, 1 one cell per thread, 4 the
-// staged tiles; +2 requests each thread's first-touch lines into L2 at the
-// start.
-int g_pml_kind = 3;
+// Step kernel form (kind & 15): 0 four rows per thread, 1 one cell per
+// thread, 4 the staged tiles; +2 requests each thread's first-touch lines
+// into L2 at the start.  kind >> 4: for the one-cell form, a register bound
+// of 5 or 6 blocks of 256 threads an SM (0: the compiler's choice).
+// Default: one cell, prefetch, 6 blocks (40 registers; measured fastest).
+int g_pml_kind = 3 + 6 * 16;
 
 struct PmlState {
     DevBuf<float> buf;
@@ -973,6 +988,7 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
     a.ldz = ldz;
     a.prefetch = (g_pml_kind & 2) != 0;
     const bool one = (g_pml_kind & 1) != 0;
+    const int minb = g_pml_kind >> 4;
     for (int k = 0; k < NC; ++k) a.cf[k] = cf + k * n;
     a.t = T;
     a.zs = g.zs;
@@ -997,8 +1013,17 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
                 if (w == 0) k_pml_tile<false><<<grdt, TT_THREADS, 10 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
                 else k_pml_tile<true><<<grdt, TT_THREADS, 14 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
             } else if (one) {
-                if (w == 0) k_pml_step1<false><<<grd, blk, 0, st>>>(a);
-                else k_pml_step1<true><<<grd, blk, 0, st>>>(a);
+                // register bound: at least MINB blocks of 256 threads an SM
+                if (minb == 6) {
+                    if (w == 0) k_pml_step1b<false, 6><<<grd, blk, 0, st>>>(a);
+                    else k_pml_step1b<true, 6><<<grd, blk, 0, st>>>(a);
+                } else if (minb == 5) {
+                    if (w == 0) k_pml_step1b<false, 5><<<grd, blk, 0, st>>>(a);
+                    else k_pml_step1b<true, 5><<<grd, blk, 0, st>>>(a);
+                } else {
+                    if (w == 0) k_pml_step1<false><<<grd, blk, 0, st>>>(a);
+                    else k_pml_step1<true><<<grd, blk, 0, st>>>(a);
+                }
             } else {
                 if (w == 0) k_pml_step<false><<<grd4, blk, 0, st>>>(a);
                 else k_pml_step<true><<<grd4, blk, 0, st>>>(a);
@@ -1128,7 +1153,9 @@ extern "C" long long pml_born_launches(void) { return g_pml.launches; }
 
 extern "C" int pml_set_kernel(int kind)
 {
-    RTM_CHECK_ARG(kind >= 0 && kind <= 7 && kind != 5 && kind != 7, "kernel kind %d", kind);
+    const int base = kind & 15, minb = kind >> 4;
+    RTM_CHECK_ARG(base <= 7 && base != 5 && base != 7 && kind >= 0 && (minb == 0 || minb == 5 || minb == 6),
+                  "kernel kind %d", kind);
     g_pml_kind = kind;
     return RTM_OK;
 }

@@ -72,10 +72,11 @@ def born_dev(model, seis, snap, dx, dt, nt, xsource, zsource, nsource, fp, abc, 
                               ctypes.c_void_p(stream.cuda_stream)))
 
 
-KERNELS = {"rows4": 0, "cell": 1, "rows4-prefetch": 2, "cell-prefetch": 3, "tile": 4, "tile-prefetch": 6}
+KERNELS = {"rows4": 0, "cell": 1, "rows4-prefetch": 2, "cell-prefetch": 3, "tile": 4, "tile-prefetch": 6,
+           "cell-prefetch-b5": 3 + 5 * 16, "cell-prefetch-b6": 3 + 6 * 16}
 
 
-def set_kernel(kind="cell-prefetch"):
+def set_kernel(kind="cell-prefetch-b6"):
     """Step kernel form (every form gives the same bits): tiles staged by
     bulk tensor copies, four rows per thread, or one cell per thread; with or
     without an L2 prefetch of each thread's first-touch lines."""
