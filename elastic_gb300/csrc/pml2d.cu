@@ -846,7 +846,7 @@ float pml_source(int it, int nsource, float fp, float dt, float dx)
 // Step kernel form (kind & 15): 0 four rows per thread, 1 one cell per
 // thread, 4 the staged tiles; +2 requests each thread's first-touch lines
 // into L2 at the start.  kind >> 4: for the one-cell form, a register bound
-// of 5 or 6 blocks of 256 threads an SM (0: the compiler's choice).
+// of 5, 6 or 8 blocks of 256 threads an SM (0: the compiler's choice).
 // Default: one cell, prefetch, 6 blocks (40 registers; measured fastest).
 int g_pml_kind = 3 + 6 * 16;
 
@@ -1014,7 +1014,10 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
                 else k_pml_tile<true><<<grdt, TT_THREADS, 14 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
             } else if (one) {
                 // register bound: at least MINB blocks of 256 threads an SM
-                if (minb == 6) {
+                if (minb == 8) {
+                    if (w == 0) k_pml_step1b<false, 8><<<grd, blk, 0, st>>>(a);
+                    else k_pml_step1b<true, 8><<<grd, blk, 0, st>>>(a);
+                } else if (minb == 6) {
                     if (w == 0) k_pml_step1b<false, 6><<<grd, blk, 0, st>>>(a);
                     else k_pml_step1b<true, 6><<<grd, blk, 0, st>>>(a);
                 } else if (minb == 5) {
@@ -1154,7 +1157,7 @@ extern "C" long long pml_born_launches(void) { return g_pml.launches; }
 extern "C" int pml_set_kernel(int kind)
 {
     const int base = kind & 15, minb = kind >> 4;
-    RTM_CHECK_ARG(base <= 7 && base != 5 && base != 7 && kind >= 0 && (minb == 0 || minb == 5 || minb == 6),
+    RTM_CHECK_ARG(base <= 7 && base != 5 && base != 7 && kind >= 0 && (minb == 0 || minb == 5 || minb == 6 || minb == 8),
                   "kernel kind %d", kind);
     g_pml_kind = kind;
     return RTM_OK;

@@ -317,7 +317,7 @@ int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *
  * pml_set_kernel: step kernel form, kind & 15: 0 four rows per thread, 1 one
  * cell per thread, 4 tiles staged by bulk tensor copies; + 2 to request
  * each thread's first-touch lines into L2 first; kind >> 4 (one-cell form):
- * 0, or a register bound of 5 or 6 blocks of 256 threads an SM.  Default
+ * 0, or a register bound of 5, 6 or 8 blocks of 256 threads an SM.  Default
  * 3 + 6 * 16.  Every form gives the same bits.  A staged tile whose copies do not arrive within about a
  * second makes the call return status 4. */
 int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsource, int zsource, int nsource, float fp, int nsnap,
