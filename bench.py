@@ -1091,7 +1091,7 @@ def main():
                          "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")
     ap.add_argument("--pml-kernel", default="cell-prefetch-b6",
                     choices=["rows4", "cell", "rows4-prefetch", "cell-prefetch", "tile", "tile-prefetch",
-                             "cell-prefetch-b5", "cell-prefetch-b6", "cell-prefetch-b8"],
+                             "cell-prefetch-b5", "cell-prefetch-b6", "cell-prefetch-b8", "fused"],
                     help="PML Born step kernel form")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the float64 error block")

@@ -644,6 +644,50 @@ __global__ void __launch_bounds__(BZ * BX, MINB) k_pml_step1b(const StepArgs a)
     step1_body<BORN>(a);
 }
 
+// One launch for both wavefields: the background's level t (b) and the
+// scattered wavefield's level t-1 (s), whose Born terms read the
+// background's levels t-1 and t-2 -- the current and old levels the
+// background step of this launch reads at the same cells.  BG / SC drop
+// the background step of the launch after the last level or the scattered
+// step of the first launch.
+template <bool BG, bool SC>
+__global__ void __launch_bounds__(BZ * BX, 6) k_pml_fused(const StepArgs b, const StepArgs s)
+{
+    const int iz = blockIdx.x * BZ + threadIdx.x + 1;
+    const int ix = blockIdx.y * BX + threadIdx.y + 1;
+    if (iz > b.nz || ix > b.nx) return;
+    const long long p = (long long)(ix - 1) * b.ldz + GZ + iz - 1;
+    if (b.prefetch) {
+        if (BG) prefetch_cells<false>(b, p);
+        if (SC) {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) {
+                prefetch_l2(s.cur[f] + p);
+                prefetch_l2(s.old[f] + p);
+            }
+#pragma unroll
+            for (int k = C_DL; k < NC; ++k) prefetch_l2(s.cf[k] + p);
+            if (!BG) {
+#pragma unroll
+                for (int f = 0; f < 4; ++f) {
+                    prefetch_l2(s.bgn[f] + p);
+                    prefetch_l2(s.bgc[f] + p);
+                }
+            }
+        }
+    }
+    const int e = b.t.abc + 5;
+    const bool fast = iz > e && iz <= b.nz - e && ix > e && ix <= b.nx - e;
+    if (BG) {
+        if (fast) cell1<false, true>(b, iz, ix, p);
+        else cell1<false, false>(b, iz, ix, p);
+    }
+    if (SC) {
+        if (fast) cell1<true, true>(s, iz, ix, p);
+        else cell1<true, false>(s, iz, ix, p);
+    }
+}
+
 // Model set-up (born-mod.f90:331-389).  The harmonic averages are written in
 // place column by column in the reference, but every neighbour it reads
 // ((iz+1, ix), (iz, ix+1), (iz+1, ix+1)) is still unaveraged then, so each
@@ -845,8 +889,10 @@ float pml_source(int it, int nsource, float fp, float dt, float dx)
 
 // Step kernel form (kind & 15): 0 four rows per thread, 1 one cell per
 // thread, 4 the staged tiles; +2 requests each thread's first-touch lines
-// into L2 at the start.  kind >> 4: for the one-cell form, a register bound
-// of 5, 6 or 8 blocks of 256 threads an SM (0: the compiler's choice).
+// into L2 at the start; 8 one launch a level for both wavefields (one cell
+// a thread, prefetch, 6 blocks an SM).  kind >> 4: for the one-cell form, a
+// register bound of 5, 6 or 8 blocks of 256 threads an SM (0: the
+// compiler's choice).
 // Default: one cell, prefetch, 6 blocks (40 registers; measured fastest).
 int g_pml_kind = 3 + 6 * 16;
 
@@ -988,12 +1034,98 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
     a.ldz = ldz;
     a.prefetch = (g_pml_kind & 2) != 0;
     const bool one = (g_pml_kind & 1) != 0;
+    const bool fused = (g_pml_kind & 15) == 8;
     const int minb = g_pml_kind >> 4;
     for (int k = 0; k < NC; ++k) a.cf[k] = cf + k * n;
     a.t = T;
     a.zs = g.zs;
     a.xs = g.xs;
-    for (int it = 1; it <= g.nt; ++it) {
+    // receiver lines and snapshots of level it, from its background and
+    // scattered parts
+    auto record_level = [&](int it, float *const *bgf, float *const *scf) -> int {
+        if ((float)it > nsource2 && it % dseis == 0 && countseis <= g.nseis) {
+            RecArgs r;
+            r.nz = g.nz;
+            r.nx = g.nx;
+            r.ldz = ldz;
+            r.a = g.abc == 0 ? 1 : g.abc;
+            r.nseis = g.nseis;
+            r.zrec = g.zrec;
+            r.count = countseis;
+            for (int f = 0; f < NF; ++f) {
+                r.w[0][f] = bgf[f];
+                r.w[1][f] = scf[f];
+            }
+            for (int k = 0; k < 6; ++k) r.seis[k] = seis[k];
+            const int nrec = g.nx - 2 * r.a - 1;
+            if (nrec > 0) {
+                k_pml_record<<<ceil_div(nrec, 128), 128, 0, st>>>(r);
+                RTM_CUDA(cudaGetLastError());
+                ++launches;
+            }
+            countseis++;
+        }
+        if (it % dsnap == 0 && countsnap <= g.nsnap) {
+            SnapArgs sa;
+            sa.nz = g.nz;
+            sa.nx = g.nx;
+            sa.ldz = ldz;
+            sa.off = (long long)(countsnap - 1) * nf;
+            for (int f = 0; f < NF; ++f) {
+                sa.w[0][f] = bgf[f];
+                sa.w[1][f] = scf[f];
+            }
+            for (int k = 0; k < 6; ++k) sa.snap[k] = snap[k];
+            k_pml_snap<<<grd, blk, 0, st>>>(sa);
+            RTM_CUDA(cudaGetLastError());
+            ++launches;
+            countsnap++;
+        }
+        return RTM_OK;
+    };
+    if (fused) {
+        // launch L: background level L (L <= nt) and scattered level L-1
+        // (L >= 2); each wavefield rotates its own three levels
+        int bn = 0, bc = 1, bo = 2, sn = 0, sc = 1, so = 2;
+        StepArgs b = a, c = a;
+        b.prefetch = c.prefetch = 1;
+        for (int L = 1; L <= g.nt + 1; ++L) {
+            const bool BG = L <= g.nt, SC = L >= 2;
+            for (int f = 0; f < NF; ++f) {
+                b.nw[f] = lv[0][bn][f];
+                b.cur[f] = lv[0][bc][f];
+                b.old[f] = lv[0][bo][f];
+                c.nw[f] = lv[1][sn][f];
+                c.cur[f] = lv[1][sc][f];
+                c.old[f] = lv[1][so][f];
+            }
+            for (int f = 0; f < 4; ++f) {
+                c.bgn[f] = lv[0][bc][f];  // background level L-1
+                c.bgc[f] = lv[0][bo][f];  // background level L-2
+            }
+            b.src = BG ? pml_source(L, g.nsource, g.fp, g.dt, g.dx) : 0.0f;
+            c.src = 0.0f;
+            if (BG && SC) k_pml_fused<true, true><<<grd, blk, 0, st>>>(b, c);
+            else if (BG) k_pml_fused<true, false><<<grd, blk, 0, st>>>(b, c);
+            else k_pml_fused<false, true><<<grd, blk, 0, st>>>(b, c);
+            RTM_CUDA(cudaGetLastError());
+            ++launches;
+            if (SC) TRY(record_level(L - 1, lv[0][bc], lv[1][sn]));
+            if (BG) {
+                const int t = bo;
+                bo = bc;
+                bc = bn;
+                bn = t;
+            }
+            if (SC) {
+                const int t = so;
+                so = sc;
+                sc = sn;
+                sn = t;
+            }
+        }
+    }
+    for (int it = 1; !fused && it <= g.nt; ++it) {
         for (int w = 0; w < 2; ++w) {
             for (int f = 0; f < NF; ++f) {
                 a.nw[f] = lv[w][inew][f];
@@ -1034,40 +1166,7 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
             RTM_CUDA(cudaGetLastError());
             ++launches;
         }
-        if ((float)it > nsource2 && it % dseis == 0 && countseis <= g.nseis) {
-            RecArgs r;
-            r.nz = g.nz;
-            r.nx = g.nx;
-            r.ldz = ldz;
-            r.a = g.abc == 0 ? 1 : g.abc;
-            r.nseis = g.nseis;
-            r.zrec = g.zrec;
-            r.count = countseis;
-            for (int w = 0; w < 2; ++w)
-                for (int f = 0; f < NF; ++f) r.w[w][f] = lv[w][inew][f];
-            for (int k = 0; k < 6; ++k) r.seis[k] = seis[k];
-            const int nrec = g.nx - 2 * r.a - 1;
-            if (nrec > 0) {
-                k_pml_record<<<ceil_div(nrec, 128), 128, 0, st>>>(r);
-                RTM_CUDA(cudaGetLastError());
-                ++launches;
-            }
-            countseis++;
-        }
-        if (it % dsnap == 0 && countsnap <= g.nsnap) {
-            SnapArgs s;
-            s.nz = g.nz;
-            s.nx = g.nx;
-            s.ldz = ldz;
-            s.off = (long long)(countsnap - 1) * nf;
-            for (int w = 0; w < 2; ++w)
-                for (int f = 0; f < NF; ++f) s.w[w][f] = lv[w][inew][f];
-            for (int k = 0; k < 6; ++k) s.snap[k] = snap[k];
-            k_pml_snap<<<grd, blk, 0, st>>>(s);
-            RTM_CUDA(cudaGetLastError());
-            ++launches;
-            countsnap++;
-        }
+        TRY(record_level(it, lv[0][inew], lv[1][inew]));
         const int t = iold;
         iold = icur;
         icur = inew;
@@ -1157,7 +1256,7 @@ extern "C" long long pml_born_launches(void) { return g_pml.launches; }
 extern "C" int pml_set_kernel(int kind)
 {
     const int base = kind & 15, minb = kind >> 4;
-    RTM_CHECK_ARG(base <= 7 && base != 5 && base != 7 && kind >= 0 && (minb == 0 || minb == 5 || minb == 6 || minb == 8),
+    RTM_CHECK_ARG((base <= 8 && base != 5 && base != 7 && kind >= 0 && (minb == 0 || minb == 5 || minb == 6 || minb == 8)),
                   "kernel kind %d", kind);
     g_pml_kind = kind;
     return RTM_OK;

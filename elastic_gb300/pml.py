@@ -73,7 +73,8 @@ def born_dev(model, seis, snap, dx, dt, nt, xsource, zsource, nsource, fp, abc, 
 
 
 KERNELS = {"rows4": 0, "cell": 1, "rows4-prefetch": 2, "cell-prefetch": 3, "tile": 4, "tile-prefetch": 6,
-           "cell-prefetch-b5": 3 + 5 * 16, "cell-prefetch-b6": 3 + 6 * 16, "cell-prefetch-b8": 3 + 8 * 16}
+           "cell-prefetch-b5": 3 + 5 * 16, "cell-prefetch-b6": 3 + 6 * 16, "cell-prefetch-b8": 3 + 8 * 16,
+           "fused": 8}
 
 
 def set_kernel(kind="cell-prefetch-b6"):

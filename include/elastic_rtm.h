@@ -315,7 +315,8 @@ int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *
  * cudaStream_t, NULL for the default stream) and returns when it is done.
  * pml_born_launches: kernels launched by the last call.
  * pml_set_kernel: step kernel form, kind & 15: 0 four rows per thread, 1 one
- * cell per thread, 4 tiles staged by bulk tensor copies; + 2 to request
+ * cell per thread, 4 tiles staged by bulk tensor copies, 8 one launch a
+ * level for both wavefields (scattered one level behind); + 2 to request
  * each thread's first-touch lines into L2 first; kind >> 4 (one-cell form):
  * 0, or a register bound of 5, 6 or 8 blocks of 256 threads an SM.  Default
  * 3 + 6 * 16.  Every form gives the same bits.  A staged tile whose copies do not arrive within about a
