@@ -92,6 +92,7 @@ SIGNATURES = {
     "pml_born_dev": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 6 + [_P] * 4),
     "pml_born_launches": (ctypes.c_longlong, []),
     "pml_set_kernel": (_c_int, [_c_int]),
+    "pml_set_test_stall": (_c_int, [_c_int]),
     "rtm_debug_umma_desc": (_c_int, [_c_int, _c_int, _c_int, _c_int, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
                                      ctypes.c_uint, _P]),
     "rtm_debug_umma_probe": (_c_int, [_c_int, ctypes.c_uint, ctypes.c_uint, _P, _P, _P]),

@@ -398,8 +398,9 @@ constexpr int TT_Z = 64, TT_X = 8, TT_LZ = TT_Z + 16, TT_LX = TT_X + 10, TT_SIZE
 constexpr int TT_THREADS = (TT_Z / 4) * TT_X;
 
 struct TileArgs {
-    int plane[14];  // staged planes: index into the field planes of the tensor map
-    int *err;       // set when a tile's copies did not arrive in time
+    int plane[14];     // staged planes: index into the field planes of the tensor map
+    int *err;          // set when a tile's copies did not arrive in time
+    const int *stall;  // test hook (null in normal use): a zeroed flag that nothing sets
 };
 
 template <int K>
@@ -483,6 +484,17 @@ __global__ void __launch_bounds__(TT_THREADS) k_pml_tile(const StepArgs a, const
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
+    if (ta.stall) {
+        // test hook: wait for a flag that nothing sets, with the same time
+        // limit as the copies' wait; no copy has been issued yet
+        const long long t0 = clock64();
+        while (*(volatile const int *)ta.stall == 0) {
+            if (clock64() - t0 > 2000000000LL) {
+                if (t == 0) atomicExch(ta.err, 1);
+                return;
+            }
+        }
+    }
     if (t == 0) {
         mbar_expect_tx(&bar, NS * TT_SIZE * 4);
         // padded row of z0 - 8 (a multiple of 4), column x0 - 5 (may be < 0:
@@ -899,6 +911,8 @@ int g_pml_kind = 3 + 6 * 16;
 struct PmlState {
     DevBuf<float> buf;
     DevBuf<int> err;
+    DevBuf<int> stall;  // zeroed flag for the test hook
+    bool test_stall = false;
     bool attr_set[RTM_MAX_DEVICES] = {};
     double last_ms = 0.0;
     long long launches = 0;
@@ -942,6 +956,8 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
     const long long ntab = 4LL * g.nz * g.abc + 4LL * g.abc * g.nx;
     TRY(g_pml.buf.alloc((size_t)(NC * n + 60 * n + ntab + 1)));
     TRY(g_pml.err.alloc(1));
+    TRY(g_pml.stall.alloc(1));
+    RTM_CUDA(cudaMemsetAsync(g_pml.stall.p, 0, sizeof(int), st));
     float *cf = g_pml.buf.p, *fld = cf + NC * n, *tab = fld + 60 * n;
     RTM_CUDA(cudaMemsetAsync(cf, 0, sizeof(float) * (NC + 60) * n, st));
     RTM_CUDA(cudaMemsetAsync(g_pml.err.p, 0, sizeof(int), st));
@@ -1140,6 +1156,7 @@ int pml_run(const Geom &g, const float *const *model, float *const *seis, float 
             if (tile) {
                 TileArgs ta;
                 ta.err = g_pml.err.p;
+                ta.stall = g_pml.test_stall && it == 1 && w == 0 ? g_pml.stall.p : nullptr;
                 for (int f = 0; f < NF; ++f) ta.plane[f] = (w * 3 + icur) * NF + f;
                 for (int f = 0; f < 4; ++f) ta.plane[NF + f] = inew * NF + f;
                 if (w == 0) k_pml_tile<false><<<grdt, TT_THREADS, 10 * TT_SIZE * 4 + 128, st>>>(a, ta, tm);
@@ -1252,6 +1269,12 @@ extern "C" int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsour
 }
 
 extern "C" long long pml_born_launches(void) { return g_pml.launches; }
+
+extern "C" int pml_set_test_stall(int on)
+{
+    g_pml.test_stall = on != 0;
+    return RTM_OK;
+}
 
 extern "C" int pml_set_kernel(int kind)
 {

@@ -84,6 +84,12 @@ def set_kernel(kind="cell-prefetch-b6"):
     check(load().pml_set_kernel(KERNELS[kind]))
 
 
+def set_test_stall(on):
+    """Test hook: the staged-tile form's first launch waits on a flag that
+    nothing sets and the call returns status 4 (see pml_set_test_stall)."""
+    check(load().pml_set_test_stall(1 if on else 0))
+
+
 def launches():
     """Kernels launched by the last call."""
     return int(load().pml_born_launches())

@@ -330,6 +330,11 @@ int pml_born_dev(int nz, int nx, int nt, float dx, float dt, int xsource, int zs
                  float *const *seis, float *const *snap, void *stream);
 long long pml_born_launches(void);
 int pml_set_kernel(int kind);
+/* Test hook of the failure path: with on = 1, the staged-tile form's first
+ * launch of every later call waits on a flag that nothing sets instead of
+ * its copies, gives up after about a second, and the call returns status 4
+ * (no copy is in flight when a CTA gives up).  0 restores normal runs. */
+int pml_set_test_stall(int on);
 
 /* -------------------------------------------- batched multi-shot RTM
  * No counterpart in the reference (one shot per run, W/rtm.f90:46-47): the

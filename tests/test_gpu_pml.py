@@ -75,6 +75,25 @@ def test_device_entry_matches_host_entry(gold):
         assert same_bits(seis[k].cpu().numpy(), hs[k]) and same_bits(snap[k].cpu().numpy(), hc[k])
 
 
+def test_tile_wait_limit_reports_status_4(gold):
+    """The staged-tile form's bounded wait: a flag that nothing sets makes
+    its first launch give up after about a second; the call returns status
+    4, and the next call (hook off) gives the reference's bits again."""
+    from elastic_gb300._lib import RtmError
+    m, kw = case_args(gold, "noabc")
+    pml.set_kernel("tile-prefetch")
+    try:
+        pml.set_test_stall(True)
+        with pytest.raises(RtmError, match="status 4"):
+            pml.born(*m, **kw)
+        pml.set_test_stall(False)
+        seis, snap = pml.born(*m, **kw)
+        check_against_fixture(gold, "noabc", seis, snap)
+    finally:
+        pml.set_test_stall(False)
+        pml.set_kernel()
+
+
 def survey_grid_case(seed=11):
     """2000 x 800 cells (the survey grid), two layers, 60-cell PML."""
     nz, nx = 800, 2000
