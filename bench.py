@@ -856,6 +856,7 @@ def elastic3d_block(args, steps, warmup, n=None):
     HBM; exact arithmetic (bit-identical to the reference's CPU step)."""
     import torch
     from elastic_gb300 import elastic3d as E
+    E.set_kernel(args.k3_kernel)
     n = n or 384
     g = torch.Generator(device="cuda").manual_seed(11)
     shape = (n + 10, n + 10, n + 10)
@@ -886,7 +887,8 @@ def elastic3d_block(args, steps, warmup, n=None):
             "steps": steps, "warmup": warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"3D elastic kernel test step, {n}^3 interior (nine fields, six coefficients), "
-                                   "exact arithmetic", "inputs_vs_l2": "inputs larger than L2"},
+                                   "exact arithmetic", "inputs_vs_l2": "inputs larger than L2",
+                       "kernel": args.k3_kernel},
             "e2e": {"value": round(cells / e2e_s / 1e9, 3), "unit": "Gcell/s",
                     "h2d_bytes_per_step": 33 * 4 * (n + 10) ** 3, "d2h_bytes_per_step": 9 * 4 * (n + 10) ** 3},
             "gpu_launches": steps,
@@ -1089,6 +1091,9 @@ def main():
     ap.add_argument("--gemm", default="tma", choices=["tma", "tc", "mma"],
                     help="U-Net GEMMs of the forward and backward-data passes: tcgen05 with bulk-copied "
                          "convolution taps, tcgen05 with thread-gathered operands, or mma.sync")
+    ap.add_argument("--k3-kernel", default="paired-bound",
+                    choices=["cell", "paired", "paired-prefetch", "paired-bound", "paired-prefetch-bound"],
+                    help="3D elastic step kernel form")
     ap.add_argument("--pml-kernel", default="cell-prefetch-b6",
                     choices=["rows4", "cell", "rows4-prefetch", "cell-prefetch", "tile", "tile-prefetch",
                              "cell-prefetch-b5", "cell-prefetch-b6", "cell-prefetch-b8", "fused"],

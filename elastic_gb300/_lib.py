@@ -87,6 +87,7 @@ SIGNATURES = {
     "rtm3d_gpu_func": (None, [_c_int] * 3 + [_P] * 35),
     "rtm3d_gpu_final": (None, []),
     "rtm3d_set_exact": (_c_int, [_c_int]),
+    "rtm3d_set_kernel": (_c_int, [_c_int]),
     "rtm3d_step_dev": (_c_int, [_c_int] * 3 + [_P] * 4 + [_c_int]),
     "pml_born_c_": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 6 + [_P] * 8),
     "pml_born_dev": (_c_int, [_c_int] * 3 + [_c_float] * 2 + [_c_int] * 3 + [_c_float] + [_c_int] * 6 + [_P] * 4),

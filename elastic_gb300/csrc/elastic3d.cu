@@ -183,8 +183,8 @@ __device__ __forceinline__ void k3_field2(const K3Args &a, long long p, const lo
         a.out[O][p + 1] = acc1;
 }
 
-template <bool EXACT>
-__global__ void __launch_bounds__(256) k_k3_step2(const __grid_constant__ K3Args a)
+template <bool EXACT, bool PF>
+__device__ __forceinline__ void k3_step2_body(const K3Args &a)
 {
     // padded z pairs 2m, 2m+1 for m = 2 .. (nz + 10) / 2 - 3 cover the interior [5, nz + 5)
     const int m = 2 + blockIdx.x * 32 + threadIdx.x, ix = blockIdx.y * 4 + threadIdx.y,
@@ -195,6 +195,18 @@ __global__ void __launch_bounds__(256) k_k3_step2(const __grid_constant__ K3Args
     const long long sx = a.nz + 10, sy = (long long)(a.nz + 10) * (a.nx + 10);
     const long long st[3] = {1, sx, sy};
     const long long p = (iy + 5) * sy + (ix + 5) * sx + zp;
+    if (PF) {
+        // the lines of the thread's own cells, first touched here, requested
+        // into L2 together before the taps
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.in[i] + p));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.in1[i] + p));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.out[i] + p));
+        }
+#pragma unroll
+        for (int i = 0; i < 6; i++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a.m[i] + p));
+    }
     k3_field2<EXACT, 0>(a, p, st, ok0, ok1);
     k3_field2<EXACT, 1>(a, p, st, ok0, ok1);
     k3_field2<EXACT, 2>(a, p, st, ok0, ok1);
@@ -206,7 +218,25 @@ __global__ void __launch_bounds__(256) k_k3_step2(const __grid_constant__ K3Args
     k3_field2<EXACT, 8>(a, p, st, ok0, ok1);
 }
 
-int g_k3_paired = 1;  // 1: the paired form where nz is even and planes are 8-byte aligned
+template <bool EXACT, bool PF>
+__global__ void __launch_bounds__(256) k_k3_step2(const __grid_constant__ K3Args a)
+{
+    k3_step2_body<EXACT, PF>(a);
+}
+
+// the same with a register bound of 4 blocks of 256 threads an SM (64
+// registers)
+template <bool EXACT, bool PF>
+__global__ void __launch_bounds__(256, 4) k_k3_step2b(const __grid_constant__ K3Args a)
+{
+    k3_step2_body<EXACT, PF>(a);
+}
+
+// 0: one cell a thread; 1: the paired form where nz is even and planes are
+// 8-byte aligned; + 2: L2 prefetch of the own cells' lines; + 4: register
+// bound of 4 blocks an SM.  Default: paired, bounded (measured fastest at
+// 384^3: 4.75 ms against 5.30 ms unbounded; the prefetch costs 35 %)
+int g_k3_paired = 5;
 
 void k3_coefs(float c[5])
 {
@@ -239,10 +269,18 @@ int k3_launch(int ny, int nz, int nx, const float *const *in, const float *const
     if (paired) {
         const int pairs = (nz + 10) / 2 - 4;  // m = 2 .. (nz + 10)/2 - 3
         const dim3 grid((pairs + 31) / 32, (nx + 3) / 4, (ny + 1) / 2);
-        if (exact)
-            k_k3_step2<true><<<grid, block, 0, st>>>(a);
-        else
-            k_k3_step2<false><<<grid, block, 0, st>>>(a);
+        const bool pf = (g_k3_paired & 2) != 0, bound = (g_k3_paired & 4) != 0;
+        if (bound) {
+            if (exact && pf) k_k3_step2b<true, true><<<grid, block, 0, st>>>(a);
+            else if (exact) k_k3_step2b<true, false><<<grid, block, 0, st>>>(a);
+            else if (pf) k_k3_step2b<false, true><<<grid, block, 0, st>>>(a);
+            else k_k3_step2b<false, false><<<grid, block, 0, st>>>(a);
+        } else {
+            if (exact && pf) k_k3_step2<true, true><<<grid, block, 0, st>>>(a);
+            else if (exact) k_k3_step2<true, false><<<grid, block, 0, st>>>(a);
+            else if (pf) k_k3_step2<false, true><<<grid, block, 0, st>>>(a);
+            else k_k3_step2<false, false><<<grid, block, 0, st>>>(a);
+        }
     } else {
         const dim3 grid((nz + 31) / 32, (nx + 3) / 4, (ny + 1) / 2);
         if (exact)
@@ -263,6 +301,14 @@ K3State g_k3;
 int g_k3_exact = 1;
 
 }  // namespace
+
+extern "C" int rtm3d_set_kernel(int kind)
+{
+    RTM_CHECK_ARG(kind == 0 || (kind & 1), "kernel kind %d", kind);
+    RTM_CHECK_ARG(kind >= 0 && kind <= 7, "kernel kind %d", kind);
+    g_k3_paired = kind;
+    return RTM_OK;
+}
 
 extern "C" int rtm3d_set_exact(int exact)
 {

@@ -15,6 +15,14 @@ FIELDS = ("vy", "vx", "vz", "syy", "sxx", "szz", "sxy", "sxz", "syz")
 COEFS = ("m1y", "m1x", "m1z", "m2", "m3", "m2m3")
 
 
+KERNELS = {"cell": 0, "paired": 1, "paired-prefetch": 3, "paired-bound": 5, "paired-prefetch-bound": 7}
+
+
+def set_kernel(kind="paired-bound"):
+    """Step kernel form (every form gives the same bits)."""
+    check(load().rtm3d_set_kernel(KERNELS[kind]))
+
+
 def _ptrs(arrs):
     P = ctypes.c_void_p * len(arrs)
     return P(*[(a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data) for a in arrs])

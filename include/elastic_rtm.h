@@ -291,6 +291,12 @@ void rtm3d_gpu_func(int ny, int nz, int nx, float *vy0, float *vx0, float *vz0, 
                     float *m2, float *m3, float *m2m3, float *debug, float *gpu_kernel_time);
 void rtm3d_gpu_final(void);
 int rtm3d_set_exact(int exact);
+/* Step kernel form, every form bit-identical: 0 one cell a thread; 1 two z
+ * cells a thread with 8-byte taps (where nz is even and the planes 8-byte
+ * aligned, else the one-cell form); + 2 requests the own cells' lines into
+ * L2 first; + 4 bounds registers to 4 blocks of 256 threads an SM
+ * (default 5). */
+int rtm3d_set_kernel(int kind);
 int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *const *in1, float *const *out,
                    const float *const *m, int exact);
 

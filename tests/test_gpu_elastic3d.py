@@ -35,9 +35,16 @@ def planes(ny, nx, nz, seed, halo_zero=True):
     return inp, in1, out, m
 
 
+@pytest.fixture(params=list(E.KERNELS))
+def kernel(request):
+    E.set_kernel(request.param)
+    yield request.param
+    E.set_kernel()
+
+
 @pytest.mark.parametrize("size", SIZES, ids=lambda s: "%dx%dx%d" % s)
 @pytest.mark.parametrize("halo_zero", [True, False], ids=["zero_halo", "random_halo"])
-def test_step_dev_exact_equals_oracle(size, halo_zero):
+def test_step_dev_exact_equals_oracle(size, halo_zero, kernel):
     import torch
     ny, nx, nz = size
     inp, in1, out, m = planes(ny, nx, nz, seed=ny * nx + nz, halo_zero=halo_zero)
