@@ -918,6 +918,8 @@ struct PmlState {
     long long launches = 0;
 };
 PmlState g_pml;
+// the working planes are shared by the calls of a process: one call at a time
+std::mutex g_pml_mutex;
 
 struct Geom {
     int nz, nx, nt, nsnap, nseis, abc, zrec, xs, zs, nsource, free_surface, lame;
@@ -1232,6 +1234,7 @@ extern "C" int pml_born_dev(int nz, int nx, int nt, float dx, float dt, int xsou
     for (int k = 0; k < 6; ++k) RTM_CHECK_ARG(model[k] && seis[k] && snap[k], "null plane");
     const Geom g = make_geom(nz, nx, nt, dx, dt, xsource, zsource, nsource, fp, nsnap, nseis, abc, zrec, free_surface,
                              lame);
+    std::lock_guard<std::mutex> lk(g_pml_mutex);
     return pml_run(g, model, seis, snap, (cudaStream_t)stream);
 }
 
@@ -1246,6 +1249,7 @@ extern "C" int pml_born_c_(int nz, int nx, int nt, float dx, float dt, int xsour
                              lame);
     TRY(check_geom(g));
     TRY(ensure_device());
+    std::lock_guard<std::mutex> lk(g_pml_mutex);
     const long long n = (long long)nz * nx;
     static DevBuf<float> io;
     TRY(io.alloc((size_t)(6 * n + 6 * g.seis_n() + 6 * g.snap_n())));

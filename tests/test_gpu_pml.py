@@ -15,7 +15,8 @@ from elastic_gb300 import pml
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
 import make_golden_pml as G  # noqa: E402
-from test_pml_oracle import CASES, GOLD, case_args, check_against_fixture, same_bits  # noqa: E402
+from test_pml_oracle import (CASES, EDGE_CASES, GOLD, case_args, check_against_fixture, edge_case_args,  # noqa: E402
+                             same_bits)
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +59,18 @@ def test_gpu_matches_oracle(nz, nx, abc, fs, lame, seed, kernel):
     for k in range(6):
         assert same_bits(gs[k], os_[k]), ("seis", O.PML_SEIS[k])
         assert same_bits(gc[k], oc[k]), ("snap", O.PML_SEIS[k])
+
+
+@pytest.mark.parametrize("case", EDGE_CASES, ids=lambda c: "%dx%d_abc%d_seed%d" % (c[0], c[1], c[2], c[5]))
+def test_gpu_edge_cases_match_oracle(case):
+    """The edge cases the oracle is held to against the reference (widest
+    PML, sources outside the operators' ranges and inside the PML,
+    receivers on the second and the last row), GPU against the oracle."""
+    m, kw = edge_case_args(*case)
+    os_, oc = O.pml_born(*m, **kw)
+    gs, gc = pml.born(*m, **kw)
+    for k in range(6):
+        assert same_bits(gs[k], os_[k]) and same_bits(gc[k], oc[k]), O.PML_SEIS[k]
 
 
 def test_device_entry_matches_host_entry(gold):

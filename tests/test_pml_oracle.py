@@ -78,19 +78,33 @@ def test_main_program_parameters():
 needs_ref = pytest.mark.skipif(not O.refpml_available(), reason="reference tree not present")
 
 
-@needs_ref
-@pytest.mark.parametrize("nz,nx,abc,fs,lame,seed", [
-    (29, 30, 12, False, False, 1),   # left and right PML columns overlap (14..17)
-    (26, 52, 11, True, False, 2),    # top and bottom PML rows overlap
-    (41, 39, 1, False, True, 3),
-    (64, 33, 5, True, True, 4),
-])
-def test_oracle_matches_translated_reference(nz, nx, abc, fs, lame, seed):
+# (nz, nx, abc, free surface, lame, seed, source (z, x) or None, zrec)
+EDGE_CASES = [
+    (29, 30, 12, False, False, 1, None, 8),   # left and right PML columns overlap (14..17)
+    (26, 52, 11, True, False, 2, None, 8),    # top and bottom PML rows overlap
+    (41, 39, 1, False, True, 3, None, 8),
+    (64, 33, 5, True, True, 4, None, 8),
+    (30, 30, 14, False, False, 5, None, 8),   # widest PML: both axes overlap, nx - 2 abc = 2
+    (36, 40, 8, False, False, 6, (3, 3), 2),  # source outside every operator's range, receivers at row 2
+    (36, 40, 8, True, False, 7, (9, 8), 36),  # source inside the top-left PML, receivers at the last row
+]
+
+
+def edge_case_args(nz, nx, abc, fs, lame, seed, src, zrec):
     import make_golden_pml as G
     m = G.model(nz, nx, seed, lame)
     P = O.pml_params(nz, nx, 10.0, 0.08, fp=60.0)
-    kw = dict(dx=10.0, dt=P["dt"], nt=P["nt"], xsource=nx // 2, zsource=min(12, nz - 6), nsource=P["nsource"],
-              fp=60.0, nsnap=3, nseis=P["nseis"], abc=abc, zrec=8, free_surface=fs, lame=lame)
+    zs, xs = src if src else (min(12, nz - 6), nx // 2)
+    kw = dict(dx=10.0, dt=P["dt"], nt=P["nt"], xsource=xs, zsource=zs, nsource=P["nsource"], fp=60.0, nsnap=3,
+              nseis=P["nseis"], abc=abc, zrec=zrec, free_surface=fs, lame=lame)
+    return m, kw
+
+
+@needs_ref
+@pytest.mark.parametrize("case", EDGE_CASES, ids=lambda c: "%dx%d_abc%d" % c[:3] + ("_fs" if c[3] else "") +
+                         ("_lame" if c[4] else "") + ("_src%d,%d" % c[6] if c[6] else "") + "_zrec%d" % c[7])
+def test_oracle_matches_translated_reference(case):
+    m, kw = edge_case_args(*case)
     rs, rc = O.refpml_born(*m, **kw)
     os_, oc = O.pml_born(*m, **kw)
     for k in range(6):
