@@ -319,6 +319,7 @@ int rtm3d_step_dev(int ny, int nz, int nx, const float *const *in, const float *
  * pml_born_c_: host arrays.  pml_born_dev: model[6] = vp0, vs0, rho0, dvp,
  * dvs, drho and the outputs are device pointers, work on `stream` (a
  * cudaStream_t, NULL for the default stream) and returns when it is done.
+ * Calls of a process are serialized (one set of working planes).
  * pml_born_launches: kernels launched by the last call.
  * pml_set_kernel: step kernel form, kind & 15: 0 four rows per thread, 1 one
  * cell per thread, 4 tiles staged by bulk tensor copies, 8 one launch a
