@@ -180,7 +180,8 @@ def run_gpu(args):
     widest = max(groups, key=lambda g: int(eng.nxs[g[0]:g[0] + g[1]].sum()))
     tune = eng.autotune(widest[0], widest[1], steps=args.tune_steps)
     # shard groups over ranks (shots are independent)
-    mine = groups[rank::world]
+    from elastic_gb300.shard import aggregate, shard_groups
+    mine = shard_groups(groups, rank, world)
     tmax = max(eng.trace_count(s, n) for s, n in groups)
     traces_host = synth.synthetic_traces(tmax, seed=c["seed"])
     # device-resident copy for the `value` measurement; pinned host copy for e2e
@@ -248,15 +249,9 @@ def run_gpu(args):
     e2e_wall = time.perf_counter() - te0
     h2d = 4 * sum(eng.trace_count(*mine[k % len(mine)]) for k in range(args.steps)) / args.steps + 4 * pf
     d2h = 4 * pf
-    # max over ranks
-    times = torch.tensor([dev_ms / 1e3, e2e_wall], dtype=torch.float64, device=f"cuda:{local}")
-    tot = torch.tensor([cells_done, shots_done, e2e_cells], dtype=torch.float64, device=f"cuda:{local}")
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
-    t_dev, t_e2e = times.tolist()
-    cells_all, shots_all, e2e_cells_all = tot.tolist()
+    # max over ranks of the times, sum of the work
+    (t_dev, t_e2e), (cells_all, shots_all, e2e_cells_all) = aggregate(
+        [dev_ms / 1e3, e2e_wall], [cells_done, shots_done, e2e_cells], device=f"cuda:{local}")
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
