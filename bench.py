@@ -943,6 +943,9 @@ def pml_block(args, steps=3, warmup=3, Tt=0.5, cpu_levels=12):
     cells = nz * nx * nt
     rate = cells / (ms * 1e-3) / 1e9
     peak, kind = measured_peaks()
+    # e2e: the host-array entry (copies in, run, copies out), one untimed
+    # call first (its staging buffers are allocated on first use)
+    pml.born(*model, nsnap=nsnap, nseis=nseis, **kw)
     te = time.perf_counter()
     pml.born(*model, nsnap=nsnap, nseis=nseis, **kw)
     e2e_s = time.perf_counter() - te
