@@ -38,6 +38,13 @@ Deliberate departures, none of which changes a computed value:
 
 Only the procedures reachable from the requested entry points are emitted;
 anything outside the supported subset inside them is an error.
+
+--set pml translates the split-field PML Born modelling program of
+2d_rtm_restart/working_Src (born-mod.f90 with bornlib-mod.f90, pml-mod.f90,
+source-mod.f90, seis-mod-born.f90, snap-mod-born.f90; entries elastic_init
+and elastic_op) into refpml.c, with the two six-argument source routines
+that born-mod.f90 calls taken from pml_source_shim.f90 (source-mod.f90
+defines them with four arguments).  LOG and NINT are supported for it.
 """
 import argparse
 import os
